@@ -1,0 +1,163 @@
+/*
+ * pico_gpu — GB300 (sm_103a) implementation of the Pico path tracer's
+ * rendering hot path behind a plain C ABI.
+ *
+ * The entry points replace these reference interfaces (paths relative to the
+ * Pico source tree):
+ *
+ *   pico_gpu_scene_upload      Scene's BLAS/TLAS construction: LowerLevelMeshBVH's
+ *                              constructor (Core/LowerLevelMeshBVH.cpp:11-79),
+ *                              UpperLevelBVH::add_lower_level_bvh / build
+ *                              (Core/UpperLevelBVH.cpp:22-57), the light list of
+ *                              Scene::add_mesh_instance (Core/Scene.cpp:406-412)
+ *   pico_gpu_trace_closest     UpperLevelBVH::get_closest_intersection
+ *                              (Core/UpperLevelBVH.hpp:36, Core/UpperLevelBVH.cpp:12-20)
+ *   pico_gpu_render            Scene::render_scene_to_memory
+ *                              (Core/Scene.hpp:68, Core/Scene.cpp:143-235) with the
+ *                              Monte_Carlo_Integrator it runs per pixel
+ *                              (Render/Integrators.hpp:33-57)
+ *   pico_gpu_denoiser_inputs   Scene::generate_denoiser_inputs (Core/Scene.cpp:248-294)
+ *   pico_gpu_atrous            Util::atrous_denoise (Util/Denoisers.hpp:9)
+ *
+ * Conventions: every function returns PICO_OK (0) or a negative PICO_ERR_*
+ * code; host buffers are caller-owned and the call returns when they hold
+ * the result (synchronous semantics); a context belongs to one host thread.
+ * Matrices are column-major 4x4 (glm layout).
+ */
+#ifndef PICO_GPU_H
+#define PICO_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum pico_status {
+    PICO_OK = 0,
+    PICO_ERR_INVALID_ARG = -1,
+    PICO_ERR_CUDA = -2,
+    PICO_ERR_OUT_OF_MEMORY = -3,
+    PICO_ERR_STACK_OVERFLOW = -4,   /* a ray needed a deeper traversal stack than the kernel has */
+    PICO_ERR_TIMEOUT = -5,          /* a bounded device loop gave up */
+    PICO_ERR_CANCELLED = -6,        /* *should_quit became non-zero */
+    PICO_ERR_NO_DEVICE = -7,
+    PICO_ERR_UNSUPPORTED = -8
+};
+
+/* BSRDF kinds, numbered like Render::BSRDF_Type (Render/BSRDF.hpp:32-39). */
+enum pico_bsdf {
+    PICO_BSDF_DIFFUSE = 0,
+    PICO_BSDF_SPECULAR = 1,
+    PICO_BSDF_DIELECTRIC = 2,
+    PICO_BSDF_BTDF = 3,             /* not supported on the GPU path */
+    PICO_BSDF_LIGHT = 4
+};
+
+typedef struct pico_gpu_ctx pico_gpu_ctx;
+typedef struct pico_gpu_scene pico_gpu_scene;
+
+/* An indexed triangle mesh, as LowerLevelMeshBVH copies it out of an aiMesh. */
+typedef struct {
+    uint32_t nverts, ntris;
+    const float* positions;         /* nverts * 3 */
+    const float* normals;           /* nverts * 3 */
+    const float* uvs;               /* nverts * 2, or NULL */
+    const uint32_t* indices;        /* ntris * 3 */
+    float aabb_min[3], aabb_max[3]; /* aiMesh::mAABB */
+} pico_mesh;
+
+/* One UpperLevelBVH::Entry: mesh, object->world transform, BSRDF and material. */
+typedef struct {
+    uint32_t mesh, bsdf, material, reserved;
+    float transform[16];
+} pico_instance;
+
+/* Core::EvaluatedMaterial of a constant material (Core/MaterialManager.hpp:17-46). */
+typedef struct {
+    float diffuse[3], specular[3], roughness, emissive[3];
+} pico_material;
+
+typedef struct {
+    const pico_mesh* meshes; uint32_t nmeshes;
+    const pico_instance* instances; uint32_t ninstances;
+    const pico_material* materials; uint32_t nmaterials;
+    float sky_rgb[3];               /* constant sky radiance (the black 1x1 sky of Scene.cpp:683-690) */
+} pico_scene_desc;
+
+/* Core::Ray's origin (vec4) and direction; dir[3] carries mLenght (the far distance). */
+typedef struct { float org[4]; float dir[4]; } pico_ray;
+
+/* Closest hit: instance (insertion index), triangle (mesh index), world distance
+ * |T * P(u,v) - O| exactly as lower_level_intersector::intersects computes it,
+ * and the barycentrics.  A miss has inst = prim = 0xffffffff and t = +inf. */
+typedef struct { uint32_t inst, prim; float t, u, v; } pico_hit;
+
+/* Scene::Camera members (Core/Camera.hpp:98-107); the FOV is carried but, as in
+ * the reference, rays use an image plane at distance 1 with half-height 0.5. */
+typedef struct {
+    float position[3], direction[3], up[3];
+    uint32_t resolution[2];
+    float aspect, near_plane, far_plane, fov;
+} pico_camera;
+
+/* Scene::RenderParams (Core/Scene.hpp:30-43) without the buffers, plus the seed
+ * that replaces the reference's std::random_device draw. */
+typedef struct {
+    uint32_t max_ray_depth;
+    uint32_t max_samples;
+    float max_variance;
+    uint32_t height, width;
+    int32_t tonemap, denoise;
+    uint32_t reserved;
+    uint64_t seed;
+} pico_render_config;
+
+/* ---- context ------------------------------------------------------------ */
+int pico_gpu_init(int device, pico_gpu_ctx** out);
+void pico_gpu_shutdown(pico_gpu_ctx* ctx);
+const char* pico_gpu_status_string(int status);
+const char* pico_gpu_last_error(const pico_gpu_ctx* ctx);
+
+/* ---- scene -------------------------------------------------------------- */
+int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out);
+void pico_gpu_scene_free(pico_gpu_scene* scene);
+/* Sizes of the flattened scene: [0] TLAS nodes, [1] BLAS nodes, [2] triangles,
+ * [3] instances, [4] device bytes, [5] lights. */
+int pico_gpu_scene_info(const pico_gpu_scene* scene, uint64_t* out6);
+
+/* ---- closest hit (UpperLevelBVH::get_closest_intersection) --------------- */
+int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
+                           const pico_ray* rays, uint64_t n, pico_hit* hits);
+/* Device-pointer variant on a caller stream (cudaStream_t, NULL = legacy default). */
+int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
+                                  const pico_ray* d_rays, uint64_t n, pico_hit* d_hits,
+                                  void* stream);
+/* Waits for `stream` and returns the status the device-pointer calls latched
+ * since the last check (traversal stack overflow, loop bound), clearing it. */
+int pico_gpu_check(pico_gpu_ctx* ctx, void* stream);
+/* Counts, over a ray batch, the nodes visited, triangles tested and instance
+ * entries transformed by this library's traversal (out3 = {nodes, tris, instances}). */
+int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
+                         const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
+
+/* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
+int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                    const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
+                    float* variance_rgb, const volatile int32_t* should_quit);
+
+/* ---- denoiser ------------------------------------------------------------ */
+int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                             float* normals, float* positions, float* diffuse);
+int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals, const float* positions,
+                    const float* diffuse, uint32_t width, uint32_t height, float* out);
+/* Device-pointer variant; all buffers are W*H*3 floats. */
+int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float* d_normals,
+                           const float* d_positions, const float* d_diffuse, uint32_t width,
+                           uint32_t height, float* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,149 @@
+/*
+ * Oracle (test infrastructure only): denoiser inputs and the a-trous denoiser.
+ *
+ *   Scene::generate_denoiser_inputs   Core/Scene.cpp:248-294
+ *   Camera::getViewMatrix             Core/Camera.cpp:90-93 (glm::lookAtRH,
+ *                                     glm/gtc/matrix_transform.inl:754-774)
+ *   Util::atrous_denoise              Util/Denoisers.cpp:107-126
+ *   blend_pixel (per 64x64 tile)      Util/Denoisers.cpp:18-101
+ *   Tiler tile walk                   Util/Tiler.hpp:20-49
+ *
+ * The 5x5 kernel table keeps the reference's 0.09563 entry at index 17.
+ * std::min(std::exp(x), 1.0f) is restated as `(1 < e) ? 1 : e`, which keeps
+ * a NaN weight NaN exactly as the reference does.
+ */
+#include "po_internal.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+void po_view_matrix(const po_camera* c, float* out)
+{
+    const po_v3 eye = v3(c->position[0], c->position[1], c->position[2]);
+    const po_v3 dir = v3(c->direction[0], c->direction[1], c->direction[2]);
+    const po_v3 up = v3(c->up[0], c->up[1], c->up[2]);
+    const po_v3 center = v3_add(eye, dir);
+    const po_v3 f = v3_normalize(v3_sub(center, eye));
+    const po_v3 s = v3_normalize(v3_cross(f, up));
+    const po_v3 u = v3_cross(s, f);
+    float m[4][4];
+    memset(m, 0, sizeof m);
+    m[0][0] = s.x; m[1][0] = s.y; m[2][0] = s.z;
+    m[0][1] = u.x; m[1][1] = u.y; m[2][1] = u.z;
+    m[0][2] = -f.x; m[1][2] = -f.y; m[2][2] = -f.z;
+    m[3][0] = -v3_dot(s, eye); m[3][1] = -v3_dot(u, eye); m[3][2] = v3_dot(f, eye);
+    m[3][3] = 1.0f;
+    memcpy(out, m, sizeof m);
+}
+
+void po_denoiser_inputs(const po_scene* s, const po_camera* cam, uint32_t W, uint32_t H,
+                        float* normals, float* positions, float* diffuse)
+{
+    po_m4 view;
+    po_view_matrix(cam, &view.m[0][0]);
+    for (uint32_t y = 0; y < H; ++y) {
+        for (uint32_t x = 0; x < W; ++x) {
+            const size_t flat = (size_t)y * W + x;
+            po_ray r;
+            po_generate_ray(cam, 0.0f, 0.0f, x, y, &r);
+            const po_v3 d = v3(r.dir[0], r.dir[1], r.dir[2]);
+            po_fragment f;
+            if (po_closest_hit(s, v4(r.org[0], r.org[1], r.org[2], r.org[3]), d, &f, NULL)) {
+                memcpy(normals + 3 * flat, f.normal, sizeof(float) * 3);
+                const po_v4 p = m4_mul_v4(&view, v4(f.position[0], f.position[1], f.position[2], f.position[3]));
+                positions[3 * flat] = p.x; positions[3 * flat + 1] = p.y; positions[3 * flat + 2] = p.z;
+                memcpy(diffuse + 3 * flat, s->materials[s->instances[f.inst].material].diffuse, sizeof(float) * 3);
+            } else {
+                normals[3 * flat] = -d.x; normals[3 * flat + 1] = -d.y; normals[3 * flat + 2] = -d.z;
+                positions[3 * flat] = d.x * r.dir[3];
+                positions[3 * flat + 1] = d.y * r.dir[3];
+                positions[3 * flat + 2] = d.z * r.dir[3];
+                diffuse[3 * flat] = diffuse[3 * flat + 1] = diffuse[3 * flat + 2] = 0.0f;
+            }
+        }
+    }
+}
+
+static const float kWeights[25] = {
+    (float)0.00292, (float)0.01306, (float)0.02154, (float)0.01306, (float)0.00292,
+    (float)0.01306, (float)0.05855, (float)0.09653, (float)0.05855, (float)0.01306,
+    (float)0.02154, (float)0.09653, (float)0.15915, (float)0.09653, (float)0.02154,
+    (float)0.01306, (float)0.05855, (float)0.09563, (float)0.05855, (float)0.01306,
+    (float)0.00292, (float)0.01306, (float)0.02154, (float)0.01306, (float)0.00292};
+
+static float lum(const float* c)
+{
+    return v3_dot(v3(c[0], c[1], c[2]), v3(0.2126f, 0.587f, 0.114f));
+}
+static int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+static float min1(float e) { return (1.0f < e) ? 1.0f : e; }
+
+static void blend_tile(uint32_t x0, uint32_t y0, uint32_t tw, uint32_t th, uint32_t W, uint32_t H,
+                       uint32_t level, const float* pix, const float* nrm, const float* pos,
+                       const float* dif, float* out)
+{
+    const int scale = (int)pow(2, (double)level);
+    float white = 0.0f, mind = INFINITY, maxd = -INFINITY;
+    for (uint32_t x = x0; x < x0 + tw; ++x)
+        for (uint32_t y = y0; y < y0 + th; ++y)
+            for (int u = 0; u < 25; ++u) {
+                const int ix = clampi((int)x + (u % 5 - 2) * scale, 0, (int)W - 1);
+                const int iy = clampi((int)y + (u / 5 - 2) * scale, 0, (int)H - 1);
+                const size_t f = (size_t)iy * W + (size_t)ix;
+                white = f_max(white, lum(pix + 3 * f));
+                const float len = v3_length(v3(pos[3 * f], pos[3 * f + 1], pos[3 * f + 2]));
+                mind = f_min(mind, len);
+                maxd = f_max(maxd, len);
+            }
+    const float range = maxd - mind;
+    for (uint32_t x = x0; x < x0 + tw; ++x)
+        for (uint32_t y = y0; y < y0 + th; ++y) {
+            const size_t c = (size_t)y * W + x;
+            float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f, wsum = 0.0f;
+            for (int u = 0; u < 25; ++u) {
+                const int ix = clampi((int)x + (u % 5 - 2) * scale, 0, (int)W - 1);
+                const int iy = clampi((int)y + (u / 5 - 2) * scale, 0, (int)H - 1);
+                const size_t f = (size_t)iy * W + (size_t)ix;
+                po_v3 t = v3_sub(v3(nrm[3 * c], nrm[3 * c + 1], nrm[3 * c + 2]),
+                                 v3(nrm[3 * f], nrm[3 * f + 1], nrm[3 * f + 2]));
+                float dist = v3_dot(t, t);
+                const float nw = min1(expf(-dist / 0.25f));
+                t = v3_sub(v3(pos[3 * c], pos[3 * c + 1], pos[3 * c + 2]), v3(pos[3 * f], pos[3 * f + 1], pos[3 * f + 2]));
+                dist = v3_dot(t, t);
+                const float pw = min1(expf(-dist / (range * range)));
+                t = v3_sub(v3(dif[3 * c], dif[3 * c + 1], dif[3 * c + 2]), v3(dif[3 * f], dif[3 * f + 1], dif[3 * f + 2]));
+                dist = v3_dot(t, t);
+                const float dw = min1(expf(-dist / (white * white)));
+                const float w = kWeights[u] * nw * pw * dw;
+                r0 = r0 + pix[3 * f] * w;
+                r1 = r1 + pix[3 * f + 1] * w;
+                r2 = r2 + pix[3 * f + 2] * w;
+                wsum = wsum + w;
+            }
+            out[3 * c] = r0 / wsum;
+            out[3 * c + 1] = r1 / wsum;
+            out[3 * c + 2] = r2 / wsum;
+        }
+}
+
+void po_atrous_denoise(const float* pixels, const float* normals, const float* positions,
+                       const float* diffuse, uint32_t W, uint32_t H, float* out)
+{
+    const size_t n = (size_t)W * H * 3;
+    float* buf[2];
+    buf[0] = (float*)malloc(sizeof(float) * (n ? n : 1));
+    buf[1] = out;
+    memcpy(buf[0], pixels, sizeof(float) * n);
+    for (uint32_t level = 0; level < 5; ++level) {
+        const float* src = buf[level % 2];
+        float* dst = buf[(level + 1) % 2];
+        for (uint32_t x = 0; x < W; x += 64)
+            for (uint32_t y = 0; y < H; y += 64) {
+                const uint32_t tw = (x + 64 > W) ? W - x : 64;
+                const uint32_t th = (y + 64 > H) ? H - y : 64;
+                blend_tile(x, y, tw, th, W, H, level, src, normals, positions, diffuse, dst);
+            }
+    }
+    free(buf[0]);
+}

@@ -1,0 +1,205 @@
+"""pico_gb300: the Pico path tracer's rendering hot path on one GB300.
+
+The compute path is libpico_gpu.so (hand-written sm_103a kernels behind the C
+ABI of include/pico_gpu.h).  This package loads it with ctypes and offers
+thin Python handles mirroring the reference's entry points:
+
+    Context.upload(scene)            Scene construction (BLAS/TLAS build + upload)
+    GpuScene.trace_closest(rays)     UpperLevelBVH::get_closest_intersection
+    GpuScene.render(camera, params)  Scene::render_scene_to_memory
+    Context.atrous(...)              Util::atrous_denoise
+
+There is no CPU fallback: if the library is missing, loading fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .types import (CCamera, CRenderConfig, CSceneDesc, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
+                    MarshalledScene, Material, Mesh, SceneData, DIFFUSE, SPECULAR, DIELECTRIC, LIGHT, MISS)
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpico_gpu.so"
+
+PICO_OK = 0
+STATUS_NAMES = {0: "PICO_OK", -1: "PICO_ERR_INVALID_ARG", -2: "PICO_ERR_CUDA", -3: "PICO_ERR_OUT_OF_MEMORY",
+                -4: "PICO_ERR_STACK_OVERFLOW", -5: "PICO_ERR_TIMEOUT", -6: "PICO_ERR_CANCELLED",
+                -7: "PICO_ERR_NO_DEVICE", -8: "PICO_ERR_UNSUPPORTED"}
+
+# Every symbol include/pico_gpu.h declares, with its ctypes signature.
+_vp, _u32, _u64, _i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int32
+_fp = C.POINTER(C.c_float)
+SIGNATURES = {
+    "pico_gpu_init": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "pico_gpu_shutdown": (None, [_vp]),
+    "pico_gpu_status_string": (C.c_char_p, [C.c_int]),
+    "pico_gpu_last_error": (C.c_char_p, [_vp]),
+    "pico_gpu_scene_upload": (C.c_int, [_vp, C.POINTER(CSceneDesc), C.POINTER(_vp)]),
+    "pico_gpu_scene_free": (None, [_vp]),
+    "pico_gpu_scene_info": (C.c_int, [_vp, C.POINTER(_u64)]),
+    "pico_gpu_trace_closest": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
+    "pico_gpu_trace_closest_device": (C.c_int, [_vp, _vp, _vp, _u64, _vp, _vp]),
+    "pico_gpu_check": (C.c_int, [_vp, _vp]),
+    "pico_gpu_trace_stats": (C.c_int, [_vp, _vp, _vp, _u64, C.POINTER(_u64), _vp]),
+    "pico_gpu_render": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _fp,
+                                  C.POINTER(_u32), _fp, C.POINTER(_i32)]),
+    "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
+    "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
+    "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
+}
+
+_lib = None
+
+
+class PicoError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Loads libpico_gpu.so and binds every declared entry point."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _f32(a: np.ndarray):
+    return a.ctypes.data_as(_fp)
+
+
+class Context:
+    """pico_gpu_ctx: one device, its streams and scratch buffers."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load_library()
+        h = _vp()
+        st = self.lib.pico_gpu_init(device, C.byref(h))
+        if st != PICO_OK:
+            raise PicoError(st, "pico_gpu_init")
+        self.handle = h
+
+    def check(self, status: int, what: str):
+        if status != PICO_OK:
+            msg = self.lib.pico_gpu_last_error(self.handle) or b""
+            raise PicoError(status, f"{what}: {msg.decode()}")
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.pico_gpu_shutdown(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, scene: SceneData) -> "GpuScene":
+        return GpuScene(self, scene)
+
+    def atrous(self, pixels, normals, positions, diffuse, width: int, height: int) -> np.ndarray:
+        arrs = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (pixels, normals, positions, diffuse)]
+        out = np.empty(width * height * 3, np.float32)
+        self.check(self.lib.pico_gpu_atrous(self.handle, *map(_f32, arrs), width, height, _f32(out)), "atrous")
+        return out.reshape(height, width, 3)
+
+    def atrous_device(self, d_pixels: int, d_normals: int, d_positions: int, d_diffuse: int, width: int,
+                      height: int, d_out: int, stream: int = 0):
+        self.check(self.lib.pico_gpu_atrous_device(self.handle, d_pixels, d_normals, d_positions, d_diffuse,
+                                                   width, height, d_out, stream or None), "atrous_device")
+
+
+class GpuScene:
+    """pico_gpu_scene: the flattened BVHs, instances, materials and lights in HBM."""
+
+    def __init__(self, ctx: Context, scene: SceneData):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        m = MarshalledScene(scene)
+        h = _vp()
+        ctx.check(self.lib.pico_gpu_scene_upload(ctx.handle, C.byref(m.desc), C.byref(h)), "scene_upload")
+        self.handle = h
+
+    def info(self) -> dict:
+        out = (C.c_uint64 * 6)()
+        self.ctx.check(self.lib.pico_gpu_scene_info(self.handle, out), "scene_info")
+        keys = ["tlas_nodes", "blas_nodes", "triangles", "instances", "device_bytes", "lights"]
+        return dict(zip(keys, [int(x) for x in out]))
+
+    def free(self):
+        if getattr(self, "handle", None):
+            self.lib.pico_gpu_scene_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def trace_closest(self, rays: np.ndarray) -> np.ndarray:
+        """Host-buffer closest hit: rays (n,) RAY_DTYPE or (n, 8) float32 -> (n,) HIT_DTYPE."""
+        r = np.ascontiguousarray(rays).view(np.float32).reshape(-1, 8)
+        hits = np.empty(len(r), HIT_DTYPE)
+        self.ctx.check(self.lib.pico_gpu_trace_closest(self.ctx.handle, self.handle, r.ctypes.data, len(r),
+                                                       hits.ctypes.data), "trace_closest")
+        return hits
+
+    def trace_closest_ptr(self, rays_ptr: int, n: int, hits_ptr: int):
+        """Host-buffer closest hit on raw host pointers (for pinned buffers)."""
+        self.ctx.check(self.lib.pico_gpu_trace_closest(self.ctx.handle, self.handle, rays_ptr, n, hits_ptr),
+                       "trace_closest")
+
+    def trace_closest_device(self, d_rays: int, n: int, d_hits: int, stream: int = 0):
+        self.ctx.check(self.lib.pico_gpu_trace_closest_device(self.ctx.handle, self.handle, d_rays, n, d_hits,
+                                                              stream or None), "trace_closest_device")
+
+    def check(self, stream: int = 0):
+        self.ctx.check(self.lib.pico_gpu_check(self.ctx.handle, stream or None), "device status")
+
+    def trace_stats(self, d_rays: int, n: int, stream: int = 0) -> dict:
+        out = (C.c_uint64 * 3)()
+        self.ctx.check(self.lib.pico_gpu_trace_stats(self.ctx.handle, self.handle, d_rays, n, out, stream or None),
+                       "trace_stats")
+        return {"nodes": int(out[0]), "tris": int(out[1]), "instances": int(out[2])}
+
+    def render(self, camera: Camera, max_depth: int, max_samples: int, seed: int = 1, pixels=None,
+               sample_count=None, variance=None, max_variance: float = 0.0, denoise: bool = False,
+               tonemap: bool = False, should_quit=None):
+        """Scene::render_scene_to_memory into (H, W, 3) buffers that are updated in place."""
+        W, H = int(camera.resolution[0]), int(camera.resolution[1])
+        if pixels is None:
+            pixels = np.zeros((H, W, 3), np.float32)
+        if sample_count is None:
+            sample_count = np.zeros((H, W), np.uint32)
+        if variance is None:
+            variance = np.zeros((H, W, 3), np.float32)
+        cfg = CRenderConfig(max_depth, max_samples, max_variance, H, W, int(tonemap), int(denoise), 0, seed)
+        cam = camera.to_c()
+        quit_flag = should_quit if should_quit is not None else C.c_int32(0)
+        self.ctx.check(self.lib.pico_gpu_render(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),
+                                                _f32(pixels), sample_count.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                _f32(variance), C.byref(quit_flag)), "render")
+        return pixels, sample_count, variance
+
+    def denoiser_inputs(self, camera: Camera):
+        W, H = int(camera.resolution[0]), int(camera.resolution[1])
+        n, p, d = (np.empty((H, W, 3), np.float32) for _ in range(3))
+        cam = camera.to_c()
+        self.ctx.check(self.lib.pico_gpu_denoiser_inputs(self.ctx.handle, self.handle, C.byref(cam), _f32(n),
+                                                         _f32(p), _f32(d)), "denoiser_inputs")
+        return n, p, d

@@ -1,0 +1,284 @@
+// The C ABI of libpico_gpu (include/pico_gpu.h): contexts, scene upload and
+// the closest-hit entry points.  Rendering and denoising live in render.cpp.
+#include "capi_internal.h"
+
+#include <cstring>
+#include <new>
+
+using namespace pico;
+
+namespace pico {
+
+int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what)
+{
+    if (e == cudaErrorMemoryAllocation)
+        return set_error(ctx, PICO_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    return set_error(ctx, PICO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cudaError_t DeviceBuffer::reserve(size_t bytes)
+{
+    if (bytes <= cap) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&ptr, bytes);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+}
+
+void DeviceBuffer::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+}
+
+// Reads and clears the latched device status; returns a PICO status.
+int take_device_status(pico_gpu_ctx* ctx, cudaStream_t stream)
+{
+    int err = 0;
+    cudaError_t e = cudaMemcpyAsync(&err, &ctx->status->trace_error, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "status read");
+    if (err) {
+        cudaMemsetAsync(&ctx->status->trace_error, 0, sizeof(int), stream);
+        cudaStreamSynchronize(stream);
+        if (err & kTraceStackOverflow)
+            return set_error(ctx, PICO_ERR_STACK_OVERFLOW, "a ray exceeded the traversal stack");
+        return set_error(ctx, PICO_ERR_TIMEOUT, "a traversal exceeded its iteration bound");
+    }
+    return PICO_OK;
+}
+
+}  // namespace pico
+
+extern "C" {
+
+int pico_gpu_init(int device, pico_gpu_ctx** out)
+{
+    if (!out) return PICO_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return PICO_ERR_NO_DEVICE;
+    if (device < 0 || device >= count) return PICO_ERR_INVALID_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return PICO_ERR_CUDA;
+    auto* ctx = new (std::nothrow) pico_gpu_ctx();
+    if (!ctx) return PICO_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->status, 2 * sizeof(DeviceStatus));
+    if (e == cudaSuccess) e = cudaMemset(ctx->status, 0, 2 * sizeof(DeviceStatus));
+    if (e != cudaSuccess) {
+        pico_gpu_shutdown(ctx);
+        return e == cudaErrorMemoryAllocation ? PICO_ERR_OUT_OF_MEMORY : PICO_ERR_CUDA;
+    }
+    *out = ctx;
+    return PICO_OK;
+}
+
+void pico_gpu_shutdown(pico_gpu_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    for (DeviceBuffer* b : {&ctx->buf_a, &ctx->buf_b, &ctx->buf_c, &ctx->buf_d, &ctx->buf_e}) b->release();
+    if (ctx->status) cudaFree(ctx->status);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+    delete ctx;
+}
+
+const char* pico_gpu_status_string(int status)
+{
+    switch (status) {
+    case PICO_OK: return "ok";
+    case PICO_ERR_INVALID_ARG: return "invalid argument";
+    case PICO_ERR_CUDA: return "CUDA error";
+    case PICO_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PICO_ERR_STACK_OVERFLOW: return "traversal stack overflow";
+    case PICO_ERR_TIMEOUT: return "device loop bound reached";
+    case PICO_ERR_CANCELLED: return "cancelled";
+    case PICO_ERR_NO_DEVICE: return "no CUDA device";
+    case PICO_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+const char* pico_gpu_last_error(const pico_gpu_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out)
+{
+    if (!ctx || !desc || !out) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    *out = nullptr;
+    cudaSetDevice(ctx->device);
+    FlatScene fs;
+    const std::string why = build_flat_scene(*desc, fs);
+    if (!why.empty()) {
+        const bool unsupported = why.find("not supported") != std::string::npos;
+        return set_error(ctx, unsupported ? PICO_ERR_UNSUPPORTED : PICO_ERR_INVALID_ARG, why);
+    }
+    auto* s = new (std::nothrow) pico_gpu_scene();
+    if (!s) return set_error(ctx, PICO_ERR_OUT_OF_MEMORY, "host allocation");
+    s->ctx = ctx;
+    s->nlights = (uint32_t)fs.lights.size();
+    s->ninstances = (uint32_t)fs.inst_shade.size();
+    s->inst_rank_host = fs.inst_rank;
+    s->light_inst_host.reserve(fs.lights.size());
+    for (const GpuLight& l : fs.lights) s->light_inst_host.push_back(l.inst);
+
+    size_t total = 0;
+    auto upload = [&](const auto& vec, auto*& dst) -> cudaError_t {
+        using T = typename std::decay_t<decltype(vec)>::value_type;
+        dst = nullptr;
+        const size_t bytes = vec.size() * sizeof(T);
+        if (bytes == 0) return cudaSuccess;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) return e;
+        s->allocations.push_back(p);
+        total += bytes;
+        e = cudaMemcpy(p, vec.data(), bytes, cudaMemcpyHostToDevice);
+        dst = static_cast<std::remove_reference_t<decltype(dst)>>(p);
+        return e;
+    };
+    SceneView& v = s->view;
+    std::memset(&v, 0, sizeof v);
+    cudaError_t e = cudaSuccess;
+    const GpuNode* nodes; const GpuTri* tris; const GpuTriShade* tshade; const GpuInstance* insts;
+    const GpuInstanceShade* ishade; const uint32_t* irank; const GpuMaterial* mats; const GpuLight* lights;
+    const float* law; const uint32_t* lai; const float* lpos;
+    if (e == cudaSuccess) e = upload(fs.nodes, nodes);
+    if (e == cudaSuccess) e = upload(fs.tris, tris);
+    if (e == cudaSuccess) e = upload(fs.tri_shade, tshade);
+    if (e == cudaSuccess) e = upload(fs.insts, insts);
+    if (e == cudaSuccess) e = upload(fs.inst_shade, ishade);
+    if (e == cudaSuccess) e = upload(fs.inst_rank, irank);
+    if (e == cudaSuccess) e = upload(fs.materials, mats);
+    if (e == cudaSuccess) e = upload(fs.lights, lights);
+    if (e == cudaSuccess) e = upload(fs.light_alias_weight, law);
+    if (e == cudaSuccess) e = upload(fs.light_alias_index, lai);
+    if (e == cudaSuccess) e = upload(fs.light_positions, lpos);
+    if (e != cudaSuccess) {
+        pico_gpu_scene_free(s);
+        return cuda_error(ctx, e, "scene upload");
+    }
+    v.nodes = nodes; v.tris = tris; v.tri_shade = tshade; v.insts = insts; v.inst_shade = ishade;
+    v.inst_rank = irank; v.materials = mats; v.lights = lights; v.light_alias_weight = law;
+    v.light_alias_index = lai; v.light_positions = lpos;
+    v.nlights = (uint32_t)fs.lights.size();
+    v.tlas_root_ref = fs.tlas_root_ref;
+    for (int a = 0; a < 3; ++a) {
+        v.tlas_lo[a] = fs.tlas_lo[a]; v.tlas_hi[a] = fs.tlas_hi[a]; v.sky[a] = fs.sky[a];
+    }
+    v.ninstances = (uint32_t)fs.inst_shade.size();
+    s->info[0] = fs.tlas_nodes; s->info[1] = fs.blas_nodes; s->info[2] = fs.tris.size();
+    s->info[3] = fs.insts.size(); s->info[4] = total; s->info[5] = fs.lights.size();
+    *out = s;
+    return PICO_OK;
+}
+
+void pico_gpu_scene_free(pico_gpu_scene* s)
+{
+    if (!s) return;
+    if (s->ctx) cudaSetDevice(s->ctx->device);
+    for (void* p : s->allocations) cudaFree(p);
+    delete s;
+}
+
+int pico_gpu_scene_info(const pico_gpu_scene* s, uint64_t* out6)
+{
+    if (!s || !out6) return PICO_ERR_INVALID_ARG;
+    std::memcpy(out6, s->info, sizeof(s->info));
+    return PICO_OK;
+}
+
+int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_ray* d_rays,
+                                  uint64_t n, pico_hit* d_hits, void* stream)
+{
+    if (!ctx || !scene || (n && (!d_rays || !d_hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return set_error(ctx, PICO_ERR_INVALID_ARG, "rays not 16-byte aligned");
+    const cudaError_t e = launch_trace(scene->view, d_rays, n, d_hits, ctx->status, false,
+                                       static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "trace launch");
+    return PICO_OK;
+}
+
+int pico_gpu_check(pico_gpu_ctx* ctx, void* stream)
+{
+    if (!ctx) return PICO_ERR_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "stream");
+    return take_device_status(ctx, static_cast<cudaStream_t>(stream));
+}
+
+int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_ray* d_rays, uint64_t n,
+                         uint64_t* out3, void* stream)
+{
+    if (!ctx || !scene || !out3 || (n && !d_rays)) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = ctx->buf_e.reserve(sizeof(pico_hit) * (n ? n : 1));
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->counters, 0, sizeof(ctx->status->counters), st);
+    if (e == cudaSuccess)
+        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, st);
+    unsigned long long c[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c, ctx->status->counters, sizeof c, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "trace stats");
+    out3[0] = c[0]; out3[1] = c[1]; out3[2] = c[2];
+    return take_device_status(ctx, st);
+}
+
+// Host-buffer closest hit: the batch is cut into chunks that alternate between
+// two streams, so the copy of one chunk overlaps the traversal of the other.
+int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_ray* rays, uint64_t n,
+                           pico_hit* hits)
+{
+    if (!ctx || !scene || (n && (!rays || !hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    if (n == 0) return PICO_OK;
+    const uint64_t chunk = n < (1ull << 22) ? n : (1ull << 22);
+    cudaError_t e = ctx->buf_a.reserve(chunk * sizeof(pico_ray));
+    if (e == cudaSuccess) e = ctx->buf_b.reserve(chunk * sizeof(pico_ray));
+    if (e == cudaSuccess) e = ctx->buf_c.reserve(chunk * sizeof(pico_hit));
+    if (e == cudaSuccess) e = ctx->buf_d.reserve(chunk * sizeof(pico_hit));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "staging allocation");
+    cudaStream_t streams[2] = {ctx->stream, ctx->stream2};
+    DeviceBuffer* rbuf[2] = {&ctx->buf_a, &ctx->buf_b};
+    DeviceBuffer* hbuf[2] = {&ctx->buf_c, &ctx->buf_d};
+    for (uint64_t off = 0, k = 0; off < n && e == cudaSuccess; off += chunk, ++k) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        const int s = (int)(k & 1);
+        pico_ray* dr = static_cast<pico_ray*>(rbuf[s]->ptr);
+        pico_hit* dh = static_cast<pico_hit*>(hbuf[s]->ptr);
+        e = cudaMemcpyAsync(dr, rays + off, m * sizeof(pico_ray), cudaMemcpyHostToDevice, streams[s]);
+        if (e == cudaSuccess)
+            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, streams[s]);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(hits + off, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, streams[s]);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(streams[0]);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(streams[1]);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
+    int st = take_device_status(ctx, ctx->stream);
+    if (st == PICO_OK) {
+        int err2 = 0;
+        e = cudaMemcpy(&err2, &ctx->status2()->trace_error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "status read");
+        if (err2) {
+            cudaMemset(&ctx->status2()->trace_error, 0, sizeof(int));
+            st = set_error(ctx, (err2 & kTraceStackOverflow) ? PICO_ERR_STACK_OVERFLOW : PICO_ERR_TIMEOUT,
+                           "traversal error");
+        }
+    }
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,50 @@
+// Internal definitions behind the C ABI.
+#pragma once
+
+#include "kernels.h"
+#include "pico_gpu.h"
+#include "scene_build.h"
+#include "traverse_status.h"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace pico {
+
+// A device allocation reused across calls, grown on demand.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t cap = 0;
+    cudaError_t reserve(size_t bytes);
+    void release();
+};
+
+}  // namespace pico
+
+struct pico_gpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;
+    pico::DeviceStatus* status = nullptr;   // two status blocks, one per stream
+    std::string last_error;
+    pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
+    pico::DeviceStatus* status2() { return status + 1; }
+};
+
+struct pico_gpu_scene {
+    pico_gpu_ctx* ctx = nullptr;
+    SceneView view{};
+    std::vector<void*> allocations;
+    std::vector<uint32_t> inst_rank_host;
+    std::vector<uint32_t> light_inst_host;
+    uint32_t nlights = 0, ninstances = 0;
+    uint64_t info[6] = {0, 0, 0, 0, 0, 0};
+};
+
+namespace pico {
+int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg);
+int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what);
+int take_device_status(pico_gpu_ctx* ctx, cudaStream_t stream);
+}  // namespace pico

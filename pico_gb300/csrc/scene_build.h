@@ -1,0 +1,38 @@
+// Host-side scene construction: the reference's SAH builder and the
+// flattening of its binary BVHs into the device layout of layout.h.
+#pragma once
+
+#include "layout.h"
+#include "pico_gpu.h"
+
+#include <string>
+#include <vector>
+
+namespace pico {
+
+// Host image of everything pico_gpu_scene_upload copies to the device.
+struct FlatScene {
+    std::vector<GpuNode> nodes;           // TLAS nodes first, then every BLAS
+    std::vector<GpuTri> tris;
+    std::vector<GpuTriShade> tri_shade;
+    std::vector<GpuInstance> insts;       // TLAS rank order
+    std::vector<GpuInstanceShade> inst_shade;
+    std::vector<uint32_t> inst_rank;      // original index -> rank
+    std::vector<GpuMaterial> materials;
+    std::vector<GpuLight> lights;
+    std::vector<float> light_alias_weight;
+    std::vector<uint32_t> light_alias_index;
+    std::vector<float> light_positions;
+    uint32_t tlas_root_ref = PICO_REF_EMPTY;
+    float tlas_lo[3] = {0, 0, 0}, tlas_hi[3] = {0, 0, 0};
+    float sky[3] = {0, 0, 0};
+    uint32_t tlas_nodes = 0, blas_nodes = 0;
+};
+
+// Builds the flat scene; returns an empty string on success, else the reason.
+std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& out);
+
+// glm::inverse of a column-major 4x4 in glm's operation order.
+void mat4_inverse(const float* m, float* out);
+
+}  // namespace pico

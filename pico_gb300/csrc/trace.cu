@@ -1,0 +1,95 @@
+// Closest-hit kernel for ray batches (UpperLevelBVH::get_closest_intersection
+// over many rays, Core/UpperLevelBVH.cpp:12-20).
+//
+// Persistent: the grid is a whole number of CTAs per SM and every warp pulls
+// 32 rays at a time from a global counter, so long rays do not leave SMs idle
+// at the tail of the batch.  Rays are 32 B (two 16-byte loads), hits 20 B.
+#include "kernels.h"
+#include "traverse.cuh"
+
+namespace pico {
+
+constexpr int kTraceThreads = 128;
+
+template <bool kCount>
+__global__ void __launch_bounds__(kTraceThreads) trace_kernel(SceneView sc, const float4* __restrict__ rays,
+                                                              uint64_t n, pico_hit* __restrict__ hits,
+                                                              DeviceStatus* status)
+{
+    TraceCounters cnt{0, 0, 0};
+    const unsigned lane = threadIdx.x & 31u;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&status->work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const unsigned long long i = base + lane;
+        if (i < n) {
+            const float4 o = __ldg(rays + 2 * i), d = __ldg(rays + 2 * i + 1);
+            TraceHit h;
+            const int s = trace_closest<kCount>(sc, o, d, h, &cnt);
+            if (s != kTraceOk) atomicOr(&status->trace_error, s);
+            pico_hit out;
+            if (h.rank != kNoHit && s == kTraceOk) {
+                out.inst = sc.insts[h.rank].inst_id;
+                out.prim = sc.tris[h.tri].prim;
+                out.t = h.t; out.u = h.u; out.v = h.v;
+            } else {
+                out.inst = kNoHit; out.prim = kNoHit;
+                out.t = __int_as_float(0x7f800000); out.u = 0.0f; out.v = 0.0f;
+            }
+            hits[i] = out;
+        }
+    }
+    if (kCount) {
+        // one atomic per warp per counter
+        for (int off = 16; off > 0; off >>= 1) {
+            cnt.nodes += __shfl_down_sync(0xffffffffu, cnt.nodes, off);
+            cnt.tris += __shfl_down_sync(0xffffffffu, cnt.tris, off);
+            cnt.insts += __shfl_down_sync(0xffffffffu, cnt.insts, off);
+        }
+        if (lane == 0) {
+            atomicAdd(&status->counters[0], cnt.nodes);
+            atomicAdd(&status->counters[1], cnt.tris);
+            atomicAdd(&status->counters[2], cnt.insts);
+        }
+    }
+}
+
+int sm_count()
+{
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, pico_hit* hits,
+                         DeviceStatus* status, bool count, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    int per_sm = 0;
+    if (count)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<true>, kTraceThreads, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<false>, kTraceThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    uint64_t blocks = (uint64_t)sm_count() * (uint64_t)per_sm;
+    const uint64_t needed = (n + kTraceThreads - 1) / kTraceThreads;
+    if (blocks > needed) blocks = needed;
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    if (count)
+        trace_kernel<true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(sc, r, n, hits, status);
+    else
+        trace_kernel<false><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(sc, r, n, hits, status);
+    return cudaGetLastError();
+}
+
+}  // namespace pico
