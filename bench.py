@@ -1,0 +1,310 @@
+"""Benchmark: closest-hit traversal throughput (Mrays/s) on the instance-field workload.
+
+Workload: 4096 instances of a level-4 icosphere (5120 triangles each, 21M
+triangles instanced) under random translation in [-50, 50]^3, log-uniform
+scale in [0.5, 4] and random rotation, as a two-level SAH BVH; 16,777,216 rays,
+half coherent primary rays of a 4096 x 4096 pinhole and half cosine-distributed
+rays leaving random surface points.  One step = one closest-hit pass
+(UpperLevelBVH::get_closest_intersection semantics) over the whole batch.
+
+  value   rays/s with rays and hits resident in HBM (device-pointer entry point),
+          timed with CUDA events on the launching stream.
+  e2e     rays/s through the host-buffer entry point from pinned host memory:
+          every step copies the rays in and the hits out.
+  cpu_baseline / --impl reference
+          the reference algorithm on this machine's host cores: the reference's own
+          code when its harness is built here (oracle/_ref), else the oracle port.
+
+With --gpus N under torchrun each rank traces the full batch on its own GPU
+(replicas: the path does not shard) and value is the sum over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from pico_gb300 import scenes  # noqa: E402
+from pico_gb300.types import HIT_DTYPE, RAY_DTYPE  # noqa: E402
+
+RAY_BYTES, HIT_BYTES = RAY_DTYPE.itemsize, HIT_DTYPE.itemsize
+NODE_BYTES, TRI_BYTES, INST_BYTES = 64, 48, 144
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--rays", type=int, default=1 << 24)
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--level", type=int, default=4)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 22)
+    return ap.parse_args()
+
+
+def workload(args):
+    scene = scenes.instance_field(n_instances=args.instances, level=args.level, seed=12345)
+    rays = scenes.field_rays(scene, n_total=args.rays, resolution=4096, seed=7)
+    return scene, rays
+
+
+def config_of(args, n_gpus):
+    return {"workload": f"instance field: {args.instances} x level-{args.level} icosphere "
+                        f"({20 * 4 ** args.level} tris each), {args.rays} rays (50% primary 4096^2 pinhole, "
+                        f"50% cosine bounce from surface points)",
+            "instances": args.instances, "triangles_per_mesh": 20 * 4 ** args.level, "rays": args.rays,
+            "l2": "inputs larger than L2 (rays 512 MiB + hits 320 MiB per step)",
+            "parallelism": f"replicas x{n_gpus}"}
+
+
+def cpu_sample(rays, k):
+    step = max(1, len(rays) // k)
+    return np.ascontiguousarray(rays[::step][:k])
+
+
+def cpu_trace(scene, rays, nthreads=0):
+    """Times the reference algorithm on host cores; returns (kind, seconds, threads)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pico_oracle
+    cores = os.cpu_count() or 1
+    try:
+        ref = pico_oracle.Reference()
+        rs = ref.scene(scene)
+        _, secs = rs.trace_timed(rays, nthreads)
+        return "reference", secs, nthreads or cores
+    except (FileNotFoundError, OSError):
+        pass
+    o = pico_oracle.Oracle()
+    os_ = o.scene(scene)
+    t0 = time.perf_counter()
+    os_.trace(rays, nthreads)
+    return "port", time.perf_counter() - t0, nthreads or cores
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "50"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.reader.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "0x1") or val.startswith("Active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        busy = [s for s in sm if s > 0.5 * max(sm)]
+        return {"sm_mhz": float(np.median(busy)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dram_traffic_per_ray():
+    """DRAM bytes per ray from the committed ncu summary of the trace kernel, if any."""
+    p = ROOT / "profiles" / "trace_kernel_dram.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["dram_bytes_per_ray"])
+        except (KeyError, ValueError):
+            return None
+    return None
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    scene, rays = workload(args)
+    sample = cpu_sample(rays, args.cpu_sample)
+    times = []
+    kind = cores = None
+    for i in range(args.warmup + args.steps):
+        kind, secs, cores = cpu_trace(scene, sample)
+        if i >= args.warmup:
+            times.append(secs)
+    t = float(np.mean(times))
+    v = len(sample) / t / 1e6
+    line = {"metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+            "config": config_of(args, args.gpus),
+            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": kind,
+                             "sample": f"{len(sample)} rays, every {len(rays) // len(sample)}th ray of the batch"},
+            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import pico_gb300
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    scene, rays = workload(args)
+    n = len(rays)
+    ctx = pico_gb300.Context(local)
+    gs = ctx.upload(scene)
+    info = gs.info()
+
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_rays = torch.from_numpy(rays.view(np.uint8)).to(f"cuda:{local}")
+    d_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step():
+        gs.trace_closest_device(d_rays.data_ptr(), n, d_hits.data_ptr(), sh)
+
+    for _ in range(args.warmup):
+        step()
+    gs.check(sh)
+    counts = gs.trace_stats(d_rays.data_ptr(), n, sh)
+
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        evs[0].record(stream)
+        for k in range(args.steps):
+            step()
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    gs.check(sh)
+    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = evs[0].elapsed_time(evs[-1])
+    if dist:
+        t = torch.tensor([total_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    ms = total_ms / args.steps
+    value = world * n / (ms / 1e3) / 1e6
+
+    # end to end from pinned host memory through the host-buffer entry point
+    e2e = None
+    if not args.no_e2e:
+        h_rays = torch.from_numpy(rays.view(np.uint8)).pin_memory()
+        h_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8).pin_memory()
+        for _ in range(max(1, min(args.warmup, 2))):
+            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
+        e2e_s = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([e2e_s], device=f"cuda:{local}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {"value": world * n / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+               "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    algo_bytes = (counts["nodes"] * NODE_BYTES + counts["tris"] * TRI_BYTES + counts["instances"] * INST_BYTES
+                  + n * (RAY_BYTES + HIT_BYTES))
+    launch_s = float(np.mean(per_step)) / 1e3
+    achieved = algo_bytes / launch_s / 1e9
+    peak, peak_src = measured_peaks()
+    dpr = dram_traffic_per_ray()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": dpr * n if dpr else None, "peak_source": peak_src,
+                "kernel": "trace_kernel<false>", "algorithmic_bytes_per_launch": algo_bytes,
+                "visits_per_ray": {k: v / n for k, v in counts.items()},
+                "note": "scene (~1.3 MB) is L2-resident; algorithmic bytes count every node/triangle/instance "
+                        "fetch (64/48/144 B) plus ray in/hit out, so frac vs HBM can exceed 1"}
+
+    cpu = None
+    if not args.no_cpu:
+        sample = cpu_sample(rays, args.cpu_sample)
+        kind, secs, cores = cpu_trace(scene, sample)
+        cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
+               "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
+
+    line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
+            "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clocks.summary(), "scene": info}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

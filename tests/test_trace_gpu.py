@@ -1,0 +1,169 @@
+"""Closest-hit parity: the sm_103a traversal against the oracle, bit for bit.
+
+UpperLevelBVH::get_closest_intersection (Core/UpperLevelBVH.cpp:12-20) returns,
+for every ray, the instance and triangle hit first and the world distance.
+Here the GPU result must equal the oracle's exactly: same instance, same
+triangle, same float bits for t, u and v.  Ties (equal distances) must resolve
+like the reference's depth-first first-found rule, which the tie scenes check.
+"""
+import numpy as np
+import pytest
+
+import pico_gb300
+from pico_gb300 import scenes
+from pico_gb300.types import DIFFUSE, HIT_DTYPE, RAY_DTYPE, Instance, Material, Mesh, SceneData
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_same_hits(got, want, label=""):
+    for k in ("inst", "prim"):
+        bad = np.nonzero(got[k] != want[k])[0]
+        assert len(bad) == 0, f"{label}: {k} differs on {len(bad)} of {len(want)} rays (first {bad[:5]})"
+    for k in ("t", "u", "v"):
+        bad = np.nonzero(got[k].view(np.uint32) != want[k].view(np.uint32))[0]
+        assert len(bad) == 0, f"{label}: {k} bits differ on {len(bad)} rays (first {bad[:5]})"
+
+
+def random_rays(rng, n, lo, hi, normalize=True):
+    r = np.zeros(n, RAY_DTYPE)
+    r["org"][:, :3] = rng.uniform(lo, hi, size=(n, 3))
+    r["org"][:, 3] = 1.0
+    d = rng.normal(size=(n, 3))
+    if normalize:
+        d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r["dir"][:, :3] = d
+    r["dir"][:, 3] = 10000.0
+    return r
+
+
+def check(ctx, oracle, scene, rays, label):
+    gs = ctx.upload(scene)
+    got = gs.trace_closest(rays)
+    want = oracle.scene(scene).trace(rays)
+    assert_same_hits(got, want, label)
+    return got, want
+
+
+def test_cornell_primary_and_bounce(ctx, oracle):
+    scene = scenes.cornell_box()
+    rays = np.concatenate([scenes.primary_rays(scenes.cornell_camera(128, 128), seed=3),
+                           scenes.surface_rays(scene, 20000, seed=4)])
+    got, want = check(ctx, oracle, scene, rays, "cornell")
+    assert (want["inst"] != pico_gb300.MISS).mean() > 0.5
+
+
+def test_instance_field(ctx, oracle):
+    scene = scenes.instance_field(n_instances=512, level=3, seed=21, extent=30.0)
+    cam = scenes.field_camera(256)
+    cam.position = (0.0, 0.0, -80.0)
+    rays = np.concatenate([scenes.primary_rays(cam, seed=5), scenes.surface_rays(scene, 60000, seed=6)])
+    got, want = check(ctx, oracle, scene, rays, "field")
+    assert (want["inst"] != pico_gb300.MISS).mean() > 0.3
+
+
+def test_random_origins_inside_and_outside(ctx, oracle):
+    scene = scenes.instance_field(n_instances=128, level=2, seed=8, extent=6.0)
+    rng = np.random.default_rng(9)
+    rays = np.concatenate([random_rays(rng, 30000, -8, 8), random_rays(rng, 5000, -8, 8, normalize=False)])
+    check(ctx, oracle, scene, rays, "random")
+
+
+def test_axis_aligned_rays_and_slab_planes(ctx, oracle):
+    """Zero direction components give infinite inverse directions and, with an
+    origin on a slab plane, NaN slab distances; the reference's selects decide."""
+    scene = scenes.cornell_box()
+    rng = np.random.default_rng(10)
+    n = 6000
+    r = np.zeros(n, RAY_DTYPE)
+    grid = np.array([0.0, 0.25, 0.3, 0.375, 0.5, 0.625, 0.7, 1.0], np.float32)
+    r["org"][:, :3] = rng.choice(grid, size=(n, 3))
+    r["org"][:, 3] = 1.0
+    axes = np.eye(3, dtype=np.float32)
+    d = axes[rng.integers(0, 3, n)] * rng.choice(np.array([-1.0, 1.0], np.float32), size=(n, 1))
+    r["dir"][:, :3] = d
+    r["dir"][:, 3] = 10000.0
+    check(ctx, oracle, scene, r, "axis")
+
+
+def test_ties_between_instances(ctx, oracle):
+    """Two instances with one transform: every hit is a tie at equal world t."""
+    s = scenes.instance_field(n_instances=16, level=2, seed=2, extent=4.0)
+    dup = list(s.instances)
+    for inst in s.instances[:8]:
+        dup.append(Instance(inst.mesh, inst.transform.copy(), DIFFUSE, 0))
+    s.instances = dup
+    rng = np.random.default_rng(12)
+    rays = random_rays(rng, 20000, -6, 6)
+    got, want = check(ctx, oracle, s, rays, "instance ties")
+    assert np.isin(want["inst"], np.arange(8)).any()
+
+
+def test_ties_within_mesh_and_large_leaves(ctx, oracle):
+    """40 copies of one triangle share a centroid, so the SAH leaves them in one
+    leaf (split into node chains on the GPU) and every hit is a 40-way tie."""
+    p = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    k = 40
+    pos = np.tile(p, (k, 1))
+    nrm = np.tile(np.array([[0, 0, 1]], np.float32), (3 * k, 1))
+    idx = np.arange(3 * k, dtype=np.uint32).reshape(k, 3)
+    s = SceneData(meshes=[Mesh(pos, nrm, idx), scenes.quad_mesh([[0, 0, 2], [1, 0, 2], [1, 1, 2], [0, 1, 2]], [0, 0, -1])],
+                  materials=[Material()])
+    eye = scenes.glm_storage(np.eye(4))
+    s.instances = [Instance(0, eye), Instance(1, eye), Instance(0, scenes.glm_storage(scenes.translate([0, 0, 1])))]
+    rng = np.random.default_rng(13)
+    r = np.zeros(5000, RAY_DTYPE)
+    r["org"][:, :3] = np.c_[rng.uniform(-0.2, 1.2, (5000, 2)), np.full(5000, -1.0)]
+    r["org"][:, 3] = 1.0
+    r["dir"][:, :3] = [0, 0, 1]
+    r["dir"][:, 3] = 100.0
+    got, want = check(ctx, oracle, s, r, "mesh ties")
+    assert (want["prim"][want["inst"] == 0] == 0).all()   # the reference keeps the first-found copy
+
+
+def test_single_instance_and_misses(ctx, oracle):
+    s = SceneData(meshes=[scenes.quad_mesh([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0]], [0, 0, 1])],
+                  instances=[Instance(0, scenes.glm_storage(np.eye(4)))], materials=[Material()])
+    rng = np.random.default_rng(14)
+    rays = random_rays(rng, 4000, -2, 2)
+    got, want = check(ctx, oracle, s, rays, "single")
+    miss = want["inst"] == pico_gb300.MISS
+    assert miss.any() and (~miss).any()
+    assert np.isinf(got["t"][miss]).all()
+
+
+def test_empty_batch(ctx):
+    gs = ctx.upload(scenes.cornell_box())
+    out = gs.trace_closest(np.zeros(0, RAY_DTYPE))
+    assert out.shape == (0,)
+
+
+def test_device_pointer_path_matches_host_path(ctx, oracle):
+    torch = pytest.importorskip("torch")
+    scene = scenes.instance_field(n_instances=256, level=3, seed=31, extent=20.0)
+    rays = np.concatenate([scenes.primary_rays(scenes.field_camera(128), seed=1),
+                           scenes.surface_rays(scene, 30000, seed=2)])
+    gs = ctx.upload(scene)
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.empty(len(rays) * HIT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    gs.trace_closest_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), stream)
+    gs.check(stream)
+    got = d_hits.cpu().numpy().view(HIT_DTYPE)
+    assert_same_hits(got, oracle.scene(scene).trace(rays), "device path")
+    stats = gs.trace_stats(d_rays.data_ptr(), len(rays), stream)
+    assert stats["nodes"] > 0 and stats["tris"] > 0 and stats["instances"] > 0
+
+
+def test_scene_info(ctx):
+    gs = ctx.upload(scenes.instance_field(n_instances=64, level=2, seed=1))
+    info = gs.info()
+    assert info["instances"] == 64 and info["triangles"] == 320 and info["tlas_nodes"] > 0
+
+
+def test_unsupported_bsdf_is_rejected(ctx):
+    s = scenes.cornell_box()
+    s.instances[0].bsdf = 3   # BTDF
+    with pytest.raises(pico_gb300.PicoError) as e:
+        ctx.upload(s)
+    assert e.value.status == -8
