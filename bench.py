@@ -161,13 +161,13 @@ def measured_peaks():
 
 
 def dram_traffic_per_ray():
-    """DRAM bytes per ray from the committed ncu summary of the trace kernel, if any."""
-    p = ROOT / "profiles" / "trace_kernel_dram.json"
+    """DRAM bytes per ray measured by ncu for the closest-hit kernel (profiles/trace_kernel_dram.txt)."""
+    p = ROOT / "profiles" / "trace_kernel_dram.txt"
     if p.exists():
-        try:
-            return float(json.loads(p.read_text())["dram_bytes_per_ray"])
-        except (KeyError, ValueError):
-            return None
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == "dram_bytes_per_ray":
+                return float(parts[1])
     return None
 
 

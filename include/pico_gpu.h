@@ -157,6 +157,16 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
                            const float* d_positions, const float* d_diffuse, uint32_t width,
                            uint32_t height, float* d_out, void* stream);
 
+/* ---- shading routines on caller inputs ---------------------------------------
+ * BSRDF::pdf and BSRDF::sample (Render/BSRDF.hpp:50-52) and direct_lighting_pdf
+ * (Render/Integrators.cpp:13-22) as the device integrator evaluates them, for n
+ * tuples: kinds[n], mats[n], V/N/H[n*3], xi[n*4] (the Hammersley points the lobe
+ * consumes, in order).  Outputs: pdf(V, H) [n], L [n*3], P [n], energy [n*3] and
+ * the direct-lighting pdf towards L [n]. */
+int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, const pico_material* mats,
+                       const float* V, const float* N, const float* H, const float* xi, float* pdf,
+                       float* L, float* P, float* energy, float* direct_pdf);
+
 #ifdef __cplusplus
 }
 #endif

@@ -48,6 +48,7 @@ SIGNATURES = {
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
+    "pico_gpu_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
@@ -116,6 +117,25 @@ class Context:
         out = np.empty(width * height * 3, np.float32)
         self.check(self.lib.pico_gpu_atrous(self.handle, *map(_f32, arrs), width, height, _f32(out)), "atrous")
         return out.reshape(height, width, 3)
+
+    def bsdf_eval(self, kinds, materials, V, N, H, xi):
+        """Device BSRDF routines on given inputs: (pdf, L, P, energy, direct_pdf)."""
+        from .types import CMaterial
+        n = len(kinds)
+        k = np.ascontiguousarray(kinds, np.uint32)
+        mats = (CMaterial * max(n, 1))()
+        for i, m in enumerate(materials):
+            mats[i].diffuse[:] = list(m.diffuse)
+            mats[i].specular[:] = list(m.specular)
+            mats[i].roughness = m.roughness
+            mats[i].emissive[:] = list(m.emissive)
+        arr = [np.ascontiguousarray(a, np.float32) for a in (V, N, H, xi)]
+        pdf, P, dl = (np.empty(n, np.float32) for _ in range(3))
+        L, E = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+        self.check(self.lib.pico_gpu_bsdf_eval(self.handle, n, k.ctypes.data, mats, *[a.ctypes.data for a in arr],
+                                               pdf.ctypes.data, L.ctypes.data, P.ctypes.data, E.ctypes.data,
+                                               dl.ctypes.data), "bsdf_eval")
+        return pdf, L, P, E, dl
 
     def atrous_device(self, d_pixels: int, d_normals: int, d_positions: int, d_diffuse: int, width: int,
                       height: int, d_out: int, stream: int = 0):

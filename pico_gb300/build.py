@@ -24,7 +24,8 @@ BUILD = ROOT / "_build"
 LIB = BUILD / "libpico_gpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["scene_build.cpp", "capi.cpp", "render_stub.cpp", "trace.cu"]
+SOURCES = ["scene_build.cpp", "capi.cpp", "render.cpp", "trace.cu", "integrator.cu", "atrous.cu",
+           "bsdf_eval.cu"]
 
 
 def nvcc_path() -> str:

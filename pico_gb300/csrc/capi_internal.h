@@ -8,8 +8,12 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
+
+struct RenderBuffers;
 
 namespace pico {
 
@@ -30,6 +34,7 @@ struct pico_gpu_ctx {
     pico::DeviceStatus* status = nullptr;   // two status blocks, one per stream
     std::string last_error;
     pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
+    RenderBuffers* render = nullptr;            // wavefront path state and image buffers
     pico::DeviceStatus* status2() { return status + 1; }
 };
 
@@ -47,4 +52,6 @@ namespace pico {
 int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg);
 int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what);
 int take_device_status(pico_gpu_ctx* ctx, cudaStream_t stream);
+RenderBuffers* render_buffers(pico_gpu_ctx* ctx);
+void free_render_buffers(pico_gpu_ctx* ctx);
 }  // namespace pico

@@ -1,0 +1,355 @@
+// Wavefront path tracer reproducing Monte_Carlo_Integrator (Render/Integrators.cpp:46-209)
+// and the per-pixel sample loop of Scene::render_scene_to_memory (Core/Scene.cpp:164-198).
+//
+// A batch holds `npix` pixels x `spb` samples, one path per thread slot, with
+// the path state in structure-of-arrays form in HBM.  Per bounce depth:
+//   extend   closest hit for every queued path (traverse.cuh)
+//   shade    BSRDF sample, emission, NEE setup, Russian roulette, next ray;
+//            survivors and shadow rays are appended to queues with one
+//            atomic per warp (ballot + popc + shuffle)
+//   shadow   closest hit for the NEE rays; a light hit adds its radiance
+// then `finish` turns payloads into sample values (NaN/Inf -> pink, as
+// Integrators.cpp:145-146) and `accumulate` applies the reference's running
+// mean / variance and early-exit rule per pixel, samples in order.
+//
+// The estimator is the reference's, including its non-physical choices: the
+// NEE term is throughput * bsdf_pdf(L) * Le * albedo with no light pdf, any
+// light hit by the shadow ray counts, Russian roulette runs from depth 0 with
+// survival max(throughput), throughput is multiplied by the sample pdf, and
+// rays leave surfaces 0.01 along the normal (or the light direction).
+#include "kernels_render.h"
+#include "shade.cuh"
+#include "traverse.cuh"
+
+namespace pico {
+
+constexpr int kRenderThreads = 256;
+
+__device__ __forceinline__ uint32_t warp_append(bool take, uint32_t* counter)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = __ballot_sync(0xffffffffu, take);
+    uint32_t base = 0;
+    if (lane == (unsigned)(__ffs(mask) - 1) && mask) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, mask ? __ffs(mask) - 1 : 0);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, CameraView cam, unsigned long long seed)
+{
+    // whole warps iterate together so the queue append can use warp collectives
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (b.n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool live = false;
+        if (i < b.n) {
+            const uint32_t slot = i % b.npix, s = i / b.npix;
+            const uint32_t pixel = b.pix_list[slot];
+            live = b.done[pixel] == 0;
+            Pcg32 rng = path_rng(seed, pixel, b.count[pixel] + s);
+            float x0, x1;
+            hammersley(rng, x0, x1);
+            float4 o, d;
+            camera_ray(cam, x0, x1, pixel % b.width, pixel / b.width, o, d);
+            b.org[i] = o;
+            b.dir[i] = d;
+            b.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            b.pay[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b.rng[i] = rng.state;
+            b.depth[i] = 0;
+        }
+        const uint32_t at = warp_append(live, &b.counters[0]);
+        if (live) b.queue[0][at] = i;
+    }
+}
+
+// Closest hit for the paths in `q` (count in *count); persistent, 32 rays per fetch.
+__global__ void __launch_bounds__(128) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
+                                                    const uint32_t* count, unsigned long long* work, int* err,
+                                                    bool shadow)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    const uint32_t n = *count;
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const unsigned long long k = base + lane;
+        if (k < n) {
+            const uint32_t i = q[k];
+            const float4 o = shadow ? b.sorg[i] : b.org[i];
+            const float4 d = shadow ? b.sdir[i] : b.dir[i];
+            TraceHit h;
+            const int s = trace_closest<false>(sc, o, d, h, nullptr);
+            if (s != kTraceOk) atomicOr(err, s);
+            const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
+            if (shadow) {
+                // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176)
+                if (rank != kNoHit) {
+                    const uint32_t inst = sc.insts[rank].inst_id;
+                    const GpuInstanceShade is = sc.inst_shade[inst];
+                    if (is.bsdf == PICO_BSDF_LIGHT) {
+                        const GpuMaterial& m = sc.materials[is.material];
+                        const float4 c = b.scontrib[i], e = b.senergy[i];
+                        float4 p = b.pay[i];
+                        p.x = p.x + (c.x * m.emissive[0]) * e.x;
+                        p.y = p.y + (c.y * m.emissive[1]) * e.y;
+                        p.z = p.z + (c.z * m.emissive[2]) * e.z;
+                        b.pay[i] = p;
+                    }
+                }
+            } else {
+                b.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(rank));
+                b.hit_tri[i] = h.tri;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, PathBatch b, int cur, uint32_t depth,
+                                                              uint32_t max_depth, bool trace_last)
+{
+    const uint32_t n = b.counters[cur];
+    const uint32_t nxt = cur ^ 1;
+    // whole warps iterate together so the queue appends can use warp collectives
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t k = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool cont = false, shadow = false;
+        uint32_t i = 0;
+        if (k < n) {
+            i = b.queue[cur][k];
+            const float4 hit = b.hit[i];
+            const uint32_t rank = __float_as_uint(hit.w);
+            float4 thr = b.thr[i], pay = b.pay[i];
+            const float4 dir = b.dir[i];
+            if (rank == kNoHit) {
+                // sky on a miss (Integrators.cpp:152, 208)
+                pay.x = pay.x + thr.x * sc.sky[0];
+                pay.y = pay.y + thr.y * sc.sky[1];
+                pay.z = pay.z + thr.z * sc.sky[2];
+                b.pay[i] = pay;
+            } else if (depth < max_depth) {
+                Pcg32 rng{b.rng[i]};
+                const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z);
+                const GpuInstanceShade is = sc.inst_shade[f.inst];
+                const GpuMaterial m = sc.materials[is.material];
+                const ex::V3 V = ex::v3(-dir.x, -dir.y, -dir.z);
+                auto next_xi = [&](float& a, float& c) { hammersley(rng, a, c); };
+                const BsdfSample smp = sample_bsdf(is.bsdf, m, V, f.n, next_xi);
+                if (is.bsdf == PICO_BSDF_LIGHT) {
+                    pay.x = pay.x + thr.x * smp.energy.x;
+                    pay.y = pay.y + thr.y * smp.energy.y;
+                    pay.z = pay.z + thr.z * smp.energy.z;
+                }
+                // next-event estimation towards one uniformly chosen light
+                if (is.bsdf != PICO_BSDF_LIGHT && sc.nlights > 0) {
+                    uint32_t li = (uint32_t)(rng.uniform() * (float)sc.nlights);
+                    if (li >= sc.nlights) li = sc.nlights - 1;
+                    const GpuLight L = sc.lights[li];
+                    const uint32_t bucket = rng.next() % L.ntris;
+                    const float coin = (float)rng.next() / 4294967296.0f;
+                    const uint32_t t = coin <= sc.light_alias_weight[L.tri_base + bucket]
+                                           ? bucket
+                                           : sc.light_alias_index[L.tri_base + bucket];
+                    float x0, x1;
+                    hammersley(rng, x0, x1);
+                    const float su0 = ex::sqrt_(x0);
+                    const float bx = 1.0f - su0, by = x1 * su0;
+                    const float* lp = sc.light_positions + 9 * (size_t)(L.tri_base + t);
+                    const float w0 = (1.0f - bx) - by;
+                    const float sx = (w0 * lp[0] + bx * lp[3]) + by * lp[6];
+                    const float sy = (w0 * lp[1] + bx * lp[4]) + by * lp[7];
+                    const float sz = (w0 * lp[2] + bx * lp[5]) + by * lp[8];
+                    const float4* lip = reinterpret_cast<const float4*>(sc.insts + sc.inst_rank[L.inst]);
+                    const float4 r0 = __ldg(lip + 3), r1 = __ldg(lip + 4), r2 = __ldg(lip + 5);
+                    const ex::V3 spw = ex::v3(ex::row4(r0, sx, sy, sz, 1.0f), ex::row4(r1, sx, sy, sz, 1.0f),
+                                              ex::row4(r2, sx, sy, sz, 1.0f));
+                    const ex::V3 tl = ex::normalize(ex::v3(spw.x - f.px, spw.y - f.py, spw.z - f.pz));
+                    if (!(ex::dot(tl, f.n) < 0.0f)) {
+                        const float pdf = direct_lighting_pdf(is.bsdf, m, f.n, V, tl);
+                        b.sorg[i] = make_float4(f.px + 0.01f * tl.x, f.py + 0.01f * tl.y, f.pz + 0.01f * tl.z,
+                                                f.pw + 0.0f);
+                        b.sdir[i] = make_float4(tl.x, tl.y, tl.z, 10000.0f);
+                        b.scontrib[i] = make_float4(thr.x * pdf, thr.y * pdf, thr.z * pdf, 0.0f);
+                        b.senergy[i] = make_float4(smp.energy.x, smp.energy.y, smp.energy.z, 0.0f);
+                        shadow = true;
+                    }
+                }
+                b.pay[i] = pay;
+                if (smp.P != 0.0f) {
+                    // Russian roulette with survival max(throughput) (Integrators.cpp:185-193)
+                    const float q = ex::smax(ex::smax(thr.x, thr.y), thr.z);
+                    if (!(rng.uniform() > q)) {
+                        const float iq = 1.0f / q;
+                        thr.x = (thr.x * iq) * (smp.P * smp.energy.x);
+                        thr.y = (thr.y * iq) * (smp.P * smp.energy.y);
+                        thr.z = (thr.z * iq) * (smp.P * smp.energy.z);
+                        b.thr[i] = thr;
+                        b.org[i] = make_float4(f.px + 0.01f * f.n.x, f.py + 0.01f * f.n.y, f.pz + 0.01f * f.n.z,
+                                               f.pw + 0.0f);
+                        b.dir[i] = make_float4(smp.L.x, smp.L.y, smp.L.z, dir.w);
+                        b.depth[i] = depth + 1;
+                        // the ray after the last shaded vertex can only add sky radiance
+                        const bool finite = isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z);
+                        cont = depth + 1 < max_depth || trace_last || !finite;
+                    }
+                }
+                b.rng[i] = rng.state;
+            }
+        }
+        const uint32_t at = warp_append(cont, &b.counters[nxt]);
+        if (cont) b.queue[nxt][at] = i;
+        const uint32_t sat = warp_append(shadow, &b.counters[2]);
+        if (shadow) b.shadow_queue[sat] = i;
+    }
+}
+
+__global__ void __launch_bounds__(kRenderThreads) finish_kernel(PathBatch b)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < b.n; i += gridDim.x * blockDim.x) {
+        float4 p = b.pay[i];
+        if (!isfinite(p.x) || !isfinite(p.y) || !isfinite(p.z)) p = make_float4(1.0f, 0.4f, 0.7f, 0.0f);
+        b.samples[i] = p;
+    }
+}
+
+// Scene.cpp:173-198 for each pixel of the batch, samples in order, exact float ops.
+__global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b, uint32_t spb, uint32_t max_samples,
+                                                                   float max_variance)
+{
+    using namespace ex;
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < b.npix; slot += gridDim.x * blockDim.x) {
+        const uint32_t pixel = b.pix_list[slot];
+        if (b.done[pixel]) continue;
+        float* px = b.pixels + 3 * (size_t)pixel;
+        float* var = b.variance + 3 * (size_t)pixel;
+        uint32_t cnt = b.count[pixel];
+        uint32_t taken = b.taken[pixel];
+        for (uint32_t s = 0; s < spb && taken < max_samples; ++s) {
+            const float4 x4 = b.samples[(size_t)s * b.npix + slot];
+            float x[3] = {x4.x, x4.y, x4.z};
+            const uint32_t prev = cnt;
+            ++taken;
+            if (prev < 1) {
+                cnt = 1;
+                var[0] = var[1] = var[2] = 0.0f;
+            } else {
+                const float f = div(1.0f, (float)prev), g = div(1.0f, (float)(prev + 1));
+                for (int c = 0; c < 3; ++c) {
+                    const float pp = px[c];
+                    const float np = add(pp, mul(sub(x[c], pp), f));
+                    var[c] = mul(add(mul(var[c], (float)prev), mul(sub(x[c], pp), sub(x[c], np))), g);
+                    x[c] = np;
+                }
+                cnt = prev + 1;
+            }
+            px[0] = x[0]; px[1] = x[1]; px[2] = x[2];
+            if (prev > 4 && var[0] <= max_variance && var[1] <= max_variance && var[2] <= max_variance) {
+                b.done[pixel] = 1;
+                break;
+            }
+        }
+        if (taken >= max_samples) b.done[pixel] = 1;
+        b.count[pixel] = cnt;
+        b.taken[pixel] = taken;
+    }
+}
+
+// Scene::generate_denoiser_inputs: one primary ray per pixel with xi = (0, 0).
+__global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView cam, uint32_t W, uint32_t H,
+                                                     float* normals, float* positions, float* diffuse, int* err)
+{
+    using namespace ex;
+    const uint32_t npx = W * H;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+        float4 o, d;
+        camera_ray(cam, 0.0f, 0.0f, p % W, p / W, o, d);
+        TraceHit h;
+        const int s = trace_closest<false>(sc, o, d, h, nullptr);
+        if (s != kTraceOk) atomicOr(err, s);
+        float n[3], pos[3], alb[3];
+        if (s == kTraceOk && h.rank != kNoHit) {
+            const Fragment f = make_fragment(sc, h.rank, h.tri, h.u, h.v);
+            n[0] = f.n.x; n[1] = f.n.y; n[2] = f.n.z;
+            const float* V = cam.view;
+            for (int r = 0; r < 3; ++r)
+                pos[r] = add(add(mul(V[0 * 4 + r], f.px), mul(V[1 * 4 + r], f.py)),
+                             add(mul(V[2 * 4 + r], f.pz), mul(V[3 * 4 + r], f.pw)));
+            const GpuMaterial& m = sc.materials[sc.inst_shade[f.inst].material];
+            alb[0] = m.diffuse[0]; alb[1] = m.diffuse[1]; alb[2] = m.diffuse[2];
+        } else {
+            n[0] = -d.x; n[1] = -d.y; n[2] = -d.z;
+            pos[0] = mul(d.x, d.w); pos[1] = mul(d.y, d.w); pos[2] = mul(d.z, d.w);
+            alb[0] = sc.sky[0]; alb[1] = sc.sky[1]; alb[2] = sc.sky[2];
+        }
+        for (int c = 0; c < 3; ++c) {
+            normals[3 * (size_t)p + c] = n[c];
+            positions[3 * (size_t)p + c] = pos[c];
+            diffuse[3 * (size_t)p + c] = alb[c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------- launchers
+static unsigned grid_for(uint32_t n, int threads)
+{
+    const uint64_t want = ((uint64_t)n + threads - 1) / threads;
+    const uint64_t cap = (uint64_t)sm_count() * 8;
+    return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
+}
+
+static unsigned extend_grid()
+{
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel, 128, 0);
+        if (per_sm < 1) per_sm = 1;
+    }
+    return (unsigned)(sm_count() * per_sm);
+}
+
+cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
+                                uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
+                                DeviceStatus* status, cudaStream_t st)
+{
+    cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed);
+    const bool trace_last = sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
+    int cur = 0;
+    for (uint32_t depth = 0; depth <= max_depth; ++depth) {
+        e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
+        if (e != cudaSuccess) return e;
+        extend_kernel<<<extend_grid(), 128, 0, st>>>(sc, b, b.queue[cur], &b.counters[cur], &status->work,
+                                                      &status->trace_error, false);
+        e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
+                                                                                trace_last);
+        if (depth < max_depth) {
+            e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
+            if (e != cudaSuccess) return e;
+            extend_kernel<<<extend_grid(), 128, 0, st>>>(sc, b, b.shadow_queue, &b.counters[2], &status->work,
+                                                          &status->trace_error, true);
+        }
+        cur ^= 1;
+    }
+    finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
+    accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
+                           float* positions, float* diffuse, DeviceStatus* status, cudaStream_t st)
+{
+    gbuffer_kernel<<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions, diffuse,
+                                                          &status->trace_error);
+    return cudaGetLastError();
+}
+
+}  // namespace pico

@@ -1,0 +1,290 @@
+// Scene::render_scene_to_memory (Core/Scene.cpp:143-235) on the device, plus the
+// denoiser entry points.
+//
+// The caller's progressive buffers (mean, sample count, variance per pixel) are
+// copied in, advanced by up to max_samples samples per pixel with the
+// reference's running mean / variance and early-exit rule, and copied back.
+// Pixels whose count already reaches max_samples are skipped, as the
+// reference's tile loop skips them.  Samples run as batches of at most 4M
+// paths (pixels x samples), each pixel's samples in order across batches; the
+// cancel flag is polled between batches.  When requested, the a-trous pass
+// then runs on the result and replaces it (Scene.cpp:212-234).
+#include "capi_internal.h"
+#include "kernels_render.h"
+
+#include <cmath>
+#include <cstring>
+
+using namespace pico;
+
+namespace {
+
+constexpr uint32_t kMaxPaths = 1u << 22;
+
+// glm-order float helpers for the host-side camera quantities.
+float dot3(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+void cross3(const float* a, const float* b, float* o)
+{
+    o[0] = a[1] * b[2] - b[1] * a[2];
+    o[1] = a[2] * b[0] - b[2] * a[0];
+    o[2] = a[0] * b[1] - b[0] * a[1];
+}
+void normalize3(const float* a, float* o)
+{
+    const float s = 1.0f / std::sqrt(dot3(a, a));
+    o[0] = a[0] * s; o[1] = a[1] * s; o[2] = a[2] * s;
+}
+
+// Camera::getRight (Core/Camera.hpp:64-65) and Camera::getViewMatrix (glm::lookAtRH).
+CameraView make_camera_view(const pico_camera& c)
+{
+    CameraView v{};
+    for (int a = 0; a < 3; ++a) { v.pos[a] = c.position[a]; v.dir[a] = c.direction[a]; v.up[a] = c.up[a]; }
+    v.res_x = (float)c.resolution[0];
+    v.res_y = (float)c.resolution[1];
+    v.aspect = c.aspect;
+    v.far_plane = c.far_plane;
+    float nd[3];
+    normalize3(c.direction, nd);
+    cross3(nd, c.up, v.right);
+    const float center[3] = {c.position[0] + c.direction[0], c.position[1] + c.direction[1],
+                             c.position[2] + c.direction[2]};
+    const float fd[3] = {center[0] - c.position[0], center[1] - c.position[1], center[2] - c.position[2]};
+    float f[3], s[3], u[3], sc[3];
+    normalize3(fd, f);
+    cross3(f, c.up, sc);
+    normalize3(sc, s);
+    cross3(s, f, u);
+    float m[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+    m[0][0] = s[0]; m[1][0] = s[1]; m[2][0] = s[2];
+    m[0][1] = u[0]; m[1][1] = u[1]; m[2][1] = u[2];
+    m[0][2] = -f[0]; m[1][2] = -f[1]; m[2][2] = -f[2];
+    m[3][0] = -dot3(s, c.position); m[3][1] = -dot3(u, c.position); m[3][2] = dot3(f, c.position);
+    std::memcpy(v.view, m, sizeof m);
+    return v;
+}
+
+template <class T>
+T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }
+
+}  // namespace
+
+// Path state and image buffers owned by the context, grown on demand.
+struct RenderBuffers {
+    DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, sorg, sdir, scontrib, senergy, q0, q1, sq,
+        counters, samples;
+    DeviceBuffer pixels, variance, count, taken, done, pix_list;
+    DeviceBuffer gn, gp, gd, ga, gb, stats, out;
+    ~RenderBuffers()
+    {
+        for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &sorg, &sdir, &scontrib,
+                                &senergy, &q0, &q1, &sq, &counters, &samples, &pixels, &variance, &count, &taken,
+                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out})
+            b->release();
+    }
+};
+
+namespace pico {
+RenderBuffers* render_buffers(pico_gpu_ctx* ctx)
+{
+    if (!ctx->render) ctx->render = new RenderBuffers();
+    return ctx->render;
+}
+void free_render_buffers(pico_gpu_ctx* ctx)
+{
+    delete ctx->render;
+    ctx->render = nullptr;
+}
+}  // namespace pico
+
+namespace {
+
+cudaError_t reserve_paths(RenderBuffers& r, size_t n)
+{
+    cudaError_t e = cudaSuccess;
+    for (DeviceBuffer* b : {&r.org, &r.dir, &r.thr, &r.pay, &r.hit, &r.sorg, &r.sdir, &r.scontrib, &r.senergy,
+                            &r.samples})
+        if (e == cudaSuccess) e = b->reserve(n * sizeof(float4));
+    for (DeviceBuffer* b : {&r.hit_tri, &r.depth, &r.q0, &r.q1, &r.sq})
+        if (e == cudaSuccess) e = b->reserve(n * sizeof(uint32_t));
+    if (e == cudaSuccess) e = r.rng.reserve(n * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = r.counters.reserve(4 * sizeof(uint32_t));
+    return e;
+}
+
+int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const float* d_n, const float* d_p,
+               const float* d_d, uint32_t W, uint32_t H, float* d_out, cudaStream_t st)
+{
+    const size_t n = (size_t)W * H * 3;
+    const size_t tiles = (size_t)((W + 63) / 64) * ((H + 63) / 64);
+    cudaError_t e = r.ga.reserve(n * sizeof(float));
+    if (e == cudaSuccess) e = r.gb.reserve(n * sizeof(float));
+    if (e == cudaSuccess) e = r.stats.reserve(tiles * 2 * sizeof(float));
+    if (e == cudaSuccess)
+        e = launch_atrous(d_pix, d_n, d_p, d_d, W, H, as<float>(r.ga), as<float>(r.gb), as<float>(r.stats), d_out, st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous");
+    return PICO_OK;
+}
+
+bool valid_camera(const pico_camera* c) { return c && c->resolution[0] > 0 && c->resolution[1] > 0; }
+
+}  // namespace
+
+extern "C" {
+
+int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                    const pico_render_config* cfg, float* pixels, uint32_t* sample_count, float* variance,
+                    const volatile int32_t* should_quit)
+{
+    if (!ctx || !scene || !cfg || !valid_camera(camera) || !pixels || !sample_count || !variance)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (cfg->width != camera->resolution[0] || cfg->height != camera->resolution[1])
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "render size differs from the camera resolution");
+    if (cfg->tonemap) return set_error(ctx, PICO_ERR_UNSUPPORTED, "tone mapping is not implemented");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& r = *render_buffers(ctx);
+    const uint32_t W = cfg->width, H = cfg->height;
+    const size_t npx = (size_t)W * H;
+
+    cudaError_t e = r.pixels.reserve(npx * 3 * sizeof(float));
+    if (e == cudaSuccess) e = r.variance.reserve(npx * 3 * sizeof(float));
+    for (DeviceBuffer* b : {&r.count, &r.taken, &r.done, &r.pix_list})
+        if (e == cudaSuccess) e = b->reserve(npx * sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "image buffers");
+
+    std::vector<uint32_t> active, done(npx, 0u);
+    active.reserve(npx);
+    for (size_t p = 0; p < npx; ++p) {
+        if (sample_count[p] >= cfg->max_samples) done[p] = 1;
+        else active.push_back((uint32_t)p);
+    }
+    e = cudaMemcpyAsync(r.pixels.ptr, pixels, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.variance.ptr, variance, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.count.ptr, sample_count, npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.done.ptr, done.data(), npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(r.taken.ptr, 0, npx * sizeof(uint32_t), st);
+    if (e == cudaSuccess && !active.empty())
+        e = cudaMemcpyAsync(r.pix_list.ptr, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render upload");
+
+    const CameraView cam = make_camera_view(*camera);
+    bool cancelled = false;
+    if (!active.empty() && cfg->max_samples > 0) {
+        const uint32_t chunk_pix = (uint32_t)std::min<size_t>(active.size(), kMaxPaths);
+        const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, kMaxPaths / chunk_pix));
+        e = reserve_paths(r, (size_t)chunk_pix * spb_max);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
+        for (size_t p0 = 0; p0 < active.size() && !cancelled; p0 += chunk_pix) {
+            const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, active.size() - p0);
+            for (uint32_t s0 = 0; s0 < cfg->max_samples; s0 += spb_max) {
+                if (should_quit && *should_quit) { cancelled = true; break; }
+                const uint32_t spb = std::min(spb_max, cfg->max_samples - s0);
+                PathBatch b{};
+                b.n = npix * spb; b.npix = npix; b.width = W;
+                b.pix_list = as<uint32_t>(r.pix_list) + p0;
+                b.org = as<float4>(r.org); b.dir = as<float4>(r.dir); b.thr = as<float4>(r.thr);
+                b.pay = as<float4>(r.pay); b.hit = as<float4>(r.hit); b.hit_tri = as<uint32_t>(r.hit_tri);
+                b.rng = as<unsigned long long>(r.rng); b.depth = as<uint32_t>(r.depth);
+                b.sorg = as<float4>(r.sorg); b.sdir = as<float4>(r.sdir); b.scontrib = as<float4>(r.scontrib);
+                b.senergy = as<float4>(r.senergy); b.queue[0] = as<uint32_t>(r.q0); b.queue[1] = as<uint32_t>(r.q1);
+                b.shadow_queue = as<uint32_t>(r.sq); b.counters = as<uint32_t>(r.counters);
+                b.samples = as<float4>(r.samples);
+                b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
+                b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
+                e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
+                                        cfg->max_variance, ctx->status, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
+            }
+        }
+    }
+    int status = take_device_status(ctx, st);
+    if (status != PICO_OK) return status;
+
+    if (cfg->denoise) {
+        const size_t n3 = npx * 3;
+        for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
+            if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
+        if (e == cudaSuccess)
+            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
+        status = run_atrous(ctx, r, as<float>(r.pixels), as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
+                            as<float>(r.out), st);
+        if (status != PICO_OK) return status;
+        e = cudaMemcpyAsync(r.pixels.ptr, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "denoise copy");
+    }
+    e = cudaMemcpyAsync(pixels, r.pixels.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(variance, r.variance.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(sample_count, r.count.ptr, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render download");
+    status = take_device_status(ctx, st);
+    if (status != PICO_OK) return status;
+    return cancelled ? set_error(ctx, PICO_ERR_CANCELLED, "render cancelled") : PICO_OK;
+}
+
+int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                             float* normals, float* positions, float* diffuse)
+{
+    if (!ctx || !scene || !valid_camera(camera) || !normals || !positions || !diffuse)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& r = *render_buffers(ctx);
+    const uint32_t W = camera->resolution[0], H = camera->resolution[1];
+    const size_t n3 = (size_t)W * H * 3;
+    cudaError_t e = cudaSuccess;
+    for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd})
+        if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
+    if (e == cudaSuccess)
+        e = launch_gbuffer(scene->view, make_camera_view(*camera), W, H, as<float>(r.gn), as<float>(r.gp),
+                           as<float>(r.gd), ctx->status, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(normals, r.gn.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(positions, r.gp.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(diffuse, r.gd.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
+    return take_device_status(ctx, st);
+}
+
+int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float* d_normals, const float* d_positions,
+                           const float* d_diffuse, uint32_t width, uint32_t height, float* d_out, void* stream)
+{
+    if (!ctx || !d_pixels || !d_normals || !d_positions || !d_diffuse || !d_out)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (d_out == d_pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "output must not alias the input");
+    cudaSetDevice(ctx->device);
+    return run_atrous(ctx, *render_buffers(ctx), d_pixels, d_normals, d_positions, d_diffuse, width, height, d_out,
+                      static_cast<cudaStream_t>(stream));
+}
+
+int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals, const float* positions,
+                    const float* diffuse, uint32_t W, uint32_t H, float* out)
+{
+    if (!ctx || !pixels || !normals || !positions || !diffuse || !out)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& r = *render_buffers(ctx);
+    const size_t n3 = (size_t)W * H * 3;
+    cudaError_t e = cudaSuccess;
+    for (DeviceBuffer* b : {&r.pixels, &r.gn, &r.gp, &r.gd, &r.out})
+        if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.pixels.ptr, pixels, n3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.gn.ptr, normals, n3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.gp.ptr, positions, n3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.gd.ptr, diffuse, n3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous upload");
+    int status = run_atrous(ctx, r, as<float>(r.pixels), as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
+                            as<float>(r.out), st);
+    if (status != PICO_OK) return status;
+    e = cudaMemcpyAsync(out, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous download");
+    return PICO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,319 @@
+// Device sampling and shading: the reference's camera, tangent frame, lobes,
+// BSRDF sample / pdf and direct-lighting pdf.
+//
+//   Camera::generate_ray            Core/Camera.cpp:11-28 (exact operation order)
+//   construct_world_to_tangent      Core/vectorUtils.cpp:9-35
+//   glm::inverse(mat3)              glm/detail/func_matrix.inl:272-294
+//   cosine lobe                     Render/Distributions.cpp:14-29
+//   Beckmann lobe                   Render/Distributions.cpp:31-78
+//   BSRDF sample / pdf              Render/BSRDF.cpp:11-214
+//   direct_lighting_pdf             Render/Integrators.cpp:13-22
+//   hammersley(i, 2^32-1)           Core/RandUtils.cpp:13-27, 87-90
+//
+// The geometric parts (camera ray, frame, inverse, reflection) keep glm's
+// operation order through the exact helpers; the transcendental functions use
+// CUDA's IEEE-accurate cosf/sinf/logf/expf (not the fast intrinsics), which
+// agree with the host libm to a few ulp.  Random numbers come from a PCG32
+// stream per path (O'Neill 2014) instead of the reference's xorshift and
+// mt19937_64 draws: the estimator's distribution is the same, its stream is not.
+#pragma once
+
+#include "exact_math.cuh"
+#include "kernels_render.h"
+#include "layout.h"
+
+namespace pico {
+
+// ---------------------------------------------------------------- random numbers
+struct Pcg32 {
+    unsigned long long state;
+    __device__ __forceinline__ uint32_t next()
+    {
+        const unsigned long long old = state;
+        state = old * 6364136223846793005ull + 1442695040888963407ull;
+        const uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+        const uint32_t rot = (uint32_t)(old >> 59u);
+        return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+    }
+    // uniform_real_distribution<float>(0, 1) stand-in: 24 random bits in [0, 1)
+    __device__ __forceinline__ float uniform() { return (float)(next() >> 8) * (1.0f / 16777216.0f); }
+};
+
+// splitmix64 finaliser, used to derive independent PCG states from (seed, pixel, sample)
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z)
+{
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ Pcg32 path_rng(unsigned long long seed, uint32_t pixel, uint32_t sample)
+{
+    Pcg32 r;
+    r.state = mix64(seed ^ mix64(((unsigned long long)pixel << 32) | sample));
+    r.next();
+    return r;
+}
+
+__device__ __forceinline__ float radical_inverse(uint32_t bits)
+{
+    return (float)__brev(bits) * 2.3283064365386963e-10f;
+}
+
+// Hammersley_Generator::next(): one 32-bit draw -> (i / 2^32, radical inverse of i).
+__device__ __forceinline__ void hammersley(Pcg32& r, float& x, float& y)
+{
+    const uint32_t i = r.next();
+    x = ex::div((float)i, 4294967296.0f);
+    y = radical_inverse(i);
+}
+
+// ---------------------------------------------------------------- camera
+__device__ __forceinline__ void camera_ray(const CameraView& c, float xi_x, float xi_y, uint32_t px, uint32_t py,
+                                           float4& org, float4& dir)
+{
+    using namespace ex;
+    const float rx = div(xi_x, 2.0f), ry = div(xi_y, 2.0f);
+    const float dx = mul(sub(div(add((float)px, rx), c.res_x), 0.5f), c.aspect);
+    const float dy = sub(div(add((float)py, ry), c.res_y), 0.5f);
+    const V3 D = v3(c.dir[0], c.dir[1], c.dir[2]), U = v3(c.up[0], c.up[1], c.up[2]);
+    const V3 R = v3(c.right[0], c.right[1], c.right[2]);
+    const V3 d = normalize(vadd(vadd(vscale(D, 1.0f), vscale(U, dy)), vscale(R, dx)));
+    org = make_float4(c.pos[0], c.pos[1], c.pos[2], 1.0f);
+    dir = make_float4(d.x, d.y, d.z, c.far_plane);
+}
+
+// ---------------------------------------------------------------- tangent space
+struct M3 { float m[3][3]; };   // column-major like glm: m[c][r]
+
+__device__ __forceinline__ M3 tangent_frame(ex::V3 V, ex::V3 N)
+{
+    using namespace ex;
+    V3 t;
+    if (fabsf(dot(V, N)) > 0.95f) {
+        const V3 vv = fabsf(N.z) > 0.99f ? v3(1, 0, 0) : v3(0, 0, 1);
+        t = normalize(cross(N, vv));
+    } else {
+        t = normalize(cross(V, N));
+    }
+    const V3 b = normalize(cross(t, N));
+    M3 m;   // transpose(mat3(t, b, N))
+    m.m[0][0] = t.x; m.m[1][0] = t.y; m.m[2][0] = t.z;
+    m.m[0][1] = b.x; m.m[1][1] = b.y; m.m[2][1] = b.z;
+    m.m[0][2] = N.x; m.m[1][2] = N.y; m.m[2][2] = N.z;
+    return m;
+}
+
+__device__ __forceinline__ ex::V3 m3_mul(const M3& m, ex::V3 v)
+{
+    using namespace ex;
+    return v3(add(add(mul(m.m[0][0], v.x), mul(m.m[1][0], v.y)), mul(m.m[2][0], v.z)),
+              add(add(mul(m.m[0][1], v.x), mul(m.m[1][1], v.y)), mul(m.m[2][1], v.z)),
+              add(add(mul(m.m[0][2], v.x), mul(m.m[1][2], v.y)), mul(m.m[2][2], v.z)));
+}
+
+__device__ __forceinline__ M3 m3_inverse(const M3& a)
+{
+    using namespace ex;
+    const float(*m)[3] = a.m;
+    const float det = add(sub(mul(m[0][0], sub(mul(m[1][1], m[2][2]), mul(m[2][1], m[1][2]))),
+                              mul(m[1][0], sub(mul(m[0][1], m[2][2]), mul(m[2][1], m[0][2])))),
+                          mul(m[2][0], sub(mul(m[0][1], m[1][2]), mul(m[1][1], m[0][2]))));
+    const float o = div(1.0f, det);
+    M3 r;
+    r.m[0][0] = mul(sub(mul(m[1][1], m[2][2]), mul(m[2][1], m[1][2])), o);
+    r.m[1][0] = mul(-sub(mul(m[1][0], m[2][2]), mul(m[2][0], m[1][2])), o);
+    r.m[2][0] = mul(sub(mul(m[1][0], m[2][1]), mul(m[2][0], m[1][1])), o);
+    r.m[0][1] = mul(-sub(mul(m[0][1], m[2][2]), mul(m[2][1], m[0][2])), o);
+    r.m[1][1] = mul(sub(mul(m[0][0], m[2][2]), mul(m[2][0], m[0][2])), o);
+    r.m[2][1] = mul(-sub(mul(m[0][0], m[2][1]), mul(m[2][0], m[0][1])), o);
+    r.m[0][2] = mul(sub(mul(m[0][1], m[1][2]), mul(m[1][1], m[0][2])), o);
+    r.m[1][2] = mul(-sub(mul(m[0][0], m[1][2]), mul(m[1][0], m[0][2])), o);
+    r.m[2][2] = mul(sub(mul(m[0][0], m[1][1]), mul(m[1][0], m[0][1])), o);
+    return r;
+}
+
+// ---------------------------------------------------------------- lobes
+constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ ex::V3 cos_sample(float u1, float u2)
+{
+    using namespace ex;
+    const float r = sqrt_(u1);
+    const float phi = (float)((double)u2 * kPi * 2.0);
+    const float om = sub(1.0f, u1);
+    const float z = (float)sqrt((double)((0.0f < om) ? om : 0.0f));
+    const double c = cos((double)phi), s = sin((double)phi);
+    return normalize(v3((float)((double)r * c), (float)((double)r * s), z));
+}
+
+__device__ __forceinline__ float cos_pdf(ex::V3 H)
+{
+    const float c = ex::div(H.z, (float)kPi);
+    return (0.0f < c) ? c : 0.0f;
+}
+
+__device__ __forceinline__ ex::V3 beckmann_sample(float x0, float x1, ex::V3 V, float R)
+{
+    using namespace ex;
+    const float alpha = mul(R, R);
+    float log_sample = logf(sub(1.0f, x0));
+    if (isinf(log_sample)) log_sample = 0.0f;
+    const float tan2 = mul(mul(-alpha, alpha), log_sample);
+    const float phi = (float)((double)mul(x1, 2.0f) * kPi);
+    const float cos_t = div(1.0f, sqrt_(add(1.0f, tan2)));
+    const float s2 = sub(1.0f, mul(cos_t, cos_t));
+    const float sin_t = sqrt_((0.0f < s2) ? s2 : 0.0f);
+    V3 H = v3(mul(sin_t, cosf(phi)), mul(sin_t, sinf(phi)), cos_t);
+    if (!(mul(V.z, H.z) > 0.0f)) H = vneg(H);
+    return normalize(H);
+}
+
+__device__ __forceinline__ float roughness_to_alpha(float r)
+{
+    using namespace ex;
+    r = (r < 1e-3f) ? 1e-3f : r;
+    const float x = logf(r);
+    return add(add(add(add(1.62142f, mul(0.819955f, x)), mul(mul(0.1734f, x), x)), mul(mul(mul(0.0171201f, x), x), x)),
+               mul(mul(mul(mul(0.000640711f, x), x), x), x));
+}
+
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return (v < lo) ? lo : ((hi < v) ? hi : v); }
+
+__device__ __forceinline__ float beckmann_D(ex::V3 w, float R)
+{
+    using namespace ex;
+    const float ax = roughness_to_alpha(R);
+    const float cos2 = mul(w.z, w.z);
+    const float s2 = sub(1.0f, cos2);
+    const float sin2 = (0.0f < s2) ? s2 : 0.0f;
+    const float tan2 = div(sin2, cos2);
+    if (isinf(tan2)) return 0.0f;
+    const float cos4 = mul(cos2, cos2);
+    const float sin_t = sqrt_(sin2);
+    const float cphi = (sin_t == 0.0f) ? 1.0f : clampf(div(w.x, sin_t), -1.0f, 1.0f);
+    const float sphi = (sin_t == 0.0f) ? 0.0f : clampf(div(w.y, sin_t), -1.0f, 1.0f);
+    const float a2 = mul(ax, ax);
+    const float e = expf(mul(-tan2, add(div(mul(cphi, cphi), a2), div(mul(sphi, sphi), a2))));
+    return (float)((double)e / (kPi * (double)ax * (double)ax * (double)cos4));
+}
+
+__device__ __forceinline__ float beckmann_pdf(ex::V3 H, float R)
+{
+    const float d = clampf(beckmann_D(H, R), 0.0f, 1.0f);
+    return ex::mul(d, fabsf(H.z));
+}
+
+__device__ __forceinline__ float bsdf_pdf(uint32_t kind, ex::V3 wo, ex::V3 H, float roughness, float refl)
+{
+    using namespace ex;
+    switch (kind) {
+    case PICO_BSDF_DIFFUSE:
+    case PICO_BSDF_LIGHT: return cos_pdf(H);
+    case PICO_BSDF_SPECULAR: return div(beckmann_pdf(H, roughness), mul(2.0f, dot(wo, H)));
+    case PICO_BSDF_DIELECTRIC:
+        return add(mul(cos_pdf(H), sub(1.0f, refl)), mul(div(beckmann_pdf(H, roughness), mul(2.0f, dot(wo, H))), refl));
+    default: return 0.0f;
+    }
+}
+
+__device__ __forceinline__ ex::V3 reflect3(ex::V3 I, ex::V3 N)
+{
+    using namespace ex;
+    const float d = dot(N, I);
+    return v3(sub(I.x, mul(mul(N.x, d), 2.0f)), sub(I.y, mul(mul(N.y, d), 2.0f)), sub(I.z, mul(mul(N.z, d), 2.0f)));
+}
+
+struct BsdfSample {
+    ex::V3 L;
+    float P;
+    ex::V3 energy;
+};
+
+// BSRDF::sample; `xi` yields the Hammersley points the lobe consumes in the reference's order.
+template <class NextXi>
+__device__ __forceinline__ BsdfSample sample_bsdf(uint32_t kind, const GpuMaterial& m, ex::V3 V, ex::V3 N, NextXi&& next_xi)
+{
+    using namespace ex;
+    const M3 w2t = tangent_frame(V, N);
+    const M3 t2w = m3_inverse(w2t);
+    const V3 vt = normalize(m3_mul(w2t, V));
+    BsdfSample s;
+    float x0, x1;
+    if (kind == PICO_BSDF_DIFFUSE || kind == PICO_BSDF_LIGHT) {
+        next_xi(x0, x1);
+        const V3 H = cos_sample(x0, x1);
+        s.P = cos_pdf(H);
+        s.L = normalize(m3_mul(t2w, H));
+        s.energy = kind == PICO_BSDF_DIFFUSE ? v3(m.diffuse[0], m.diffuse[1], m.diffuse[2])
+                                             : v3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    } else if (kind == PICO_BSDF_SPECULAR) {
+        next_xi(x0, x1);
+        const V3 H = beckmann_sample(x0, x1, vt, m.roughness);
+        const V3 L = normalize(reflect3(vneg(vt), H));
+        s.L = normalize(m3_mul(t2w, L));
+        s.P = bsdf_pdf(PICO_BSDF_SPECULAR, vt, H, m.roughness, m.reflectance);
+        s.energy = v3(m.specular[0], m.specular[1], m.specular[2]);
+    } else {
+        next_xi(x0, x1);
+        if (x1 >= m.reflectance) {
+            next_xi(x0, x1);
+            const V3 H = cos_sample(x0, x1);
+            s.L = normalize(m3_mul(t2w, H));
+            s.P = cos_pdf(H);
+            s.energy = v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+        } else {
+            next_xi(x0, x1);
+            const V3 H = beckmann_sample(x0, x1, vt, m.roughness);
+            const V3 L = normalize(reflect3(vneg(vt), H));
+            s.L = normalize(m3_mul(t2w, L));
+            s.P = div(beckmann_pdf(H, m.roughness), mul(2.0f, dot(vt, H)));
+            s.energy = v3(m.specular[0], m.specular[1], m.specular[2]);
+        }
+    }
+    return s;
+}
+
+__device__ __forceinline__ float direct_lighting_pdf(uint32_t kind, const GpuMaterial& m, ex::V3 N, ex::V3 wi, ex::V3 wo)
+{
+    using namespace ex;
+    const M3 t = tangent_frame(wi, N);
+    const V3 two = m3_mul(t, wo);
+    const V3 H = m3_mul(t, normalize(vadd(wi, wo)));
+    return bsdf_pdf(kind, two, H, m.roughness, m.reflectance);
+}
+
+// ---------------------------------------------------------------- hit fragments
+struct Fragment {
+    float px, py, pz, pw;   // world position (vec4)
+    ex::V3 n;               // world normal
+    uint32_t inst;          // original instance index
+};
+
+// interpolate_fragment + lower_level_intersector's world transform for a hit.
+__device__ __forceinline__ Fragment make_fragment(const SceneView& sc, uint32_t rank, uint32_t tri, float u, float v)
+{
+    using namespace ex;
+    const float4* tp = reinterpret_cast<const float4*>(sc.tris + tri);
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    const float4* np = reinterpret_cast<const float4*>(sc.tri_shade + tri);
+    const float4 na = __ldg(np), nb = __ldg(np + 1), nc = __ldg(np + 2);
+    const float w = sub(sub(1.0f, v), u);
+    const float px = add(add(mul(w, a.x), mul(u, b.x)), mul(v, c.x));
+    const float py = add(add(mul(w, a.y), mul(u, b.y)), mul(v, c.y));
+    const float pz = add(add(mul(w, a.z), mul(u, b.z)), mul(v, c.z));
+    const V3 nobj = normalize(v3(add(add(mul(w, na.x), mul(u, nb.x)), mul(v, nc.x)),
+                                 add(add(mul(w, na.y), mul(u, nb.y)), mul(v, nc.y)),
+                                 add(add(mul(w, na.z), mul(u, nb.z)), mul(v, nc.z))));
+    const float4* ip = reinterpret_cast<const float4*>(sc.insts + rank);
+    const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
+    Fragment f;
+    f.px = row4(f0, px, py, pz, 1.0f); f.py = row4(f1, px, py, pz, 1.0f);
+    f.pz = row4(f2, px, py, pz, 1.0f); f.pw = row4(f3, px, py, pz, 1.0f);
+    f.n = normalize(v3(row3(f0, nobj.x, nobj.y, nobj.z), row3(f1, nobj.x, nobj.y, nobj.z),
+                       row3(f2, nobj.x, nobj.y, nobj.z)));
+    f.inst = sc.insts[rank].inst_id;
+    return f;
+}
+
+}  // namespace pico

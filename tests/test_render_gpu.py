@@ -1,0 +1,187 @@
+"""Rendering, shading and denoising on the GPU against the oracle.
+
+* BSRDF pdf / sample and the direct-lighting pdf on the reference's own golden
+  inputs: within 1e-5 (the only differences come from CUDA's cosf/sinf/logf/expf
+  against the host libm).
+* Denoiser inputs (one primary ray per pixel): bit-exact.
+* A-trous on identical G-buffers: within 1e-4 relative, NaN where the reference
+  produces NaN.
+* The Monte Carlo render: statistically, per pixel, against the oracle's
+  restatement of the reference integrator run with the reference's own random
+  streams (the GPU draws different random numbers, so the test compares means
+  within a few standard errors).
+* The progressive-buffer contract of Scene::render_scene_to_memory: counts,
+  resume, early exit, cancellation.
+"""
+import ctypes as C
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import pico_gb300
+from pico_gb300 import scenes
+from pico_gb300.types import Material
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE / "golden"))
+from scene_io import load_camera, load_scene  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLDEN = HERE / "golden"
+
+
+def test_bsdf_routines_match_reference(ctx, oracle):
+    z = np.load(GOLDEN / "sampling.npz")
+    mats = [Material(tuple(r[0:3]), tuple(r[3:6]), float(r[6]), tuple(r[7:10])) for r in z["mats"]]
+    n = len(z["samp_kind"])
+    kinds = z["samp_kind"]
+    mat_list = [mats[int(i)] for i in z["samp_mat"]]
+    xi = np.stack([oracle.hammersley(int(s), 2).reshape(-1) for s in z["samp_seed"]])
+    H = z["beckmann_sample"]
+    pdf, L, P, E, dl = ctx.bsdf_eval(kinds, mat_list, z["dir_V"], z["dir_N"], H, xi)
+    # BSRDF::pdf(wo = V, H) for each lobe kind, against the reference value
+    refl = np.array([np.linalg.norm(m.specular) / (np.linalg.norm(m.specular) + np.linalg.norm(m.diffuse))
+                     for m in mat_list], np.float32)
+    want_pdf = np.array([oracle.bsdf_pdf(int(kinds[i]), z["dir_V"][i], H[i], mat_list[i].roughness, float(refl[i]))
+                         for i in range(n)], np.float32)
+    np.testing.assert_allclose(pdf, want_pdf, rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(L, z["samp_L"], rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(P, z["samp_P"], rtol=1e-5, atol=1e-6)
+    np.testing.assert_array_equal(E, z["samp_E"])
+    np.testing.assert_allclose(dl, z["direct_pdf"], rtol=1e-5, atol=1e-5)
+
+
+def test_denoiser_inputs_bit_exact(ctx, oracle):
+    z = np.load(GOLDEN / "atrous.npz")
+    scene, cam = load_scene(z, "cornell"), load_camera(z["cam"])
+    gs = ctx.upload(scene)
+    n, p, d = gs.denoiser_inputs(cam)
+    for got, key in ((n, "normals"), (p, "positions"), (d, "diffuse")):
+        np.testing.assert_array_equal(got.view(np.uint32), z[key].view(np.uint32), err_msg=key)
+
+
+def atrous_close(got, want, rtol=1e-4):
+    nan_g, nan_w = np.isnan(got), np.isnan(want)
+    np.testing.assert_array_equal(nan_g, nan_w)
+    ok = ~nan_w
+    np.testing.assert_allclose(got[ok], want[ok], rtol=rtol, atol=1e-6)
+
+
+def test_atrous_matches_reference(ctx):
+    z = np.load(GOLDEN / "atrous.npz")
+    W, H = load_camera(z["cam"]).resolution
+    got = ctx.atrous(z["pixels"], z["normals"], z["positions"], z["diffuse"], W, H)
+    atrous_close(got, z["denoised"])
+
+
+@pytest.mark.parametrize("W,H", [(64, 64), (130, 70), (17, 200)])
+def test_atrous_ragged_sizes(ctx, oracle, W, H):
+    """Partial tiles at the right and bottom edges and tiles narrower than the tap span."""
+    rng = np.random.default_rng(W * 1000 + H)
+    pix = rng.gamma(1.0, 1.0, (H, W, 3)).astype(np.float32)
+    nrm = rng.normal(size=(H, W, 3)).astype(np.float32)
+    pos = rng.normal(size=(H, W, 3)).astype(np.float32) * 3
+    dif = rng.random((H, W, 3)).astype(np.float32)
+    got = ctx.atrous(pix, nrm, pos, dif, W, H)
+    atrous_close(got, oracle.atrous(pix, nrm, pos, dif, W, H))
+
+
+def test_atrous_device_path(ctx, oracle):
+    torch = pytest.importorskip("torch")
+    z = np.load(GOLDEN / "atrous.npz")
+    W, H = load_camera(z["cam"]).resolution
+    d = [torch.from_numpy(np.ascontiguousarray(z[k])).cuda() for k in ("pixels", "normals", "positions", "diffuse")]
+    out = torch.empty_like(d[0])
+    stream = torch.cuda.current_stream().cuda_stream
+    ctx.atrous_device(*[t.data_ptr() for t in d], W, H, out.data_ptr(), stream)
+    torch.cuda.synchronize()
+    atrous_close(out.cpu().numpy(), z["denoised"])
+
+
+def reference_render(oracle, scene, cam, spp, depth, seed=1):
+    W, H = cam.resolution
+    idx = np.arange(W * H, dtype=np.uint32)
+    seeds = (np.arange(W * H, dtype=np.uint64) * np.uint64(2654435761) + np.uint64(seed)) % np.uint64(2 ** 32)
+    return oracle.scene(scene).render_pixels(cam, depth, spp, idx, seeds)
+
+
+def test_render_statistically_matches_reference(ctx, oracle):
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(48, 48)
+    spp, depth = 512, 5
+    gs = ctx.upload(scene)
+    g_pix, g_cnt, g_var = gs.render(cam, depth, spp, seed=7)
+    r_pix, r_cnt, r_var = reference_render(oracle, scene, cam, spp, depth)
+    # both means average samples 2..N (Scene.cpp:185-191); the variance buffer is
+    # the running population variance, so SE^2 = var / (count - 1)
+    se = np.sqrt(g_var / np.maximum(g_cnt - 1, 1)[..., None] + r_var / np.maximum(r_cnt - 1, 1)[..., None])
+    z = np.abs(g_pix - r_pix) / np.maximum(se, 1e-6)
+    frac = (z <= 4.0).mean()
+    assert frac >= 0.995, f"only {frac:.4f} of pixel channels within 4 standard errors"
+    # pixels that only see the black sky stop after 6 samples in both
+    # (variance exactly 0 after more than 4 samples, Scene.cpp:196-197)
+    sky = sky_pixels(oracle, scene, cam)
+    assert sky.any() and (g_cnt[sky] == 6).all() and (r_cnt[sky] == 6).all()
+    assert abs(g_pix.mean() - r_pix.mean()) < 0.02 * r_pix.mean()
+
+
+def sky_pixels(oracle, scene, cam):
+    """Pixels whose primary rays miss everything for every jitter (xi in [0, 1)^2 -> [0, 0.5) px)."""
+    W, H = cam.resolution
+    os_ = oracle.scene(scene)
+    miss = np.ones((H, W), bool)
+    for xi in ((0.0, 0.0), (0.9999, 0.0), (0.0, 0.9999), (0.9999, 0.9999)):
+        rays = np.stack([oracle.generate_ray(cam, xi, x, y) for y in range(H) for x in range(W)])
+        miss &= (os_.trace(rays)["inst"] == pico_gb300.MISS).reshape(H, W)
+    return miss
+
+
+def test_render_counts_resume_and_cancel(ctx):
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(32, 32)
+    gs = ctx.upload(scene)
+    pix, cnt, var = gs.render(cam, 5, 8, seed=3)
+    # a pixel with a non-zero mean has a positive variance, so it never stops early
+    inside = (pix > 0).any(axis=2)
+    assert inside.mean() > 0.5 and (cnt[inside] == 8).all()
+    before = cnt.copy()
+    # a second call runs max_samples more samples on every pixel below max_samples
+    pix, cnt, var = gs.render(cam, 5, 16, seed=4, pixels=pix, sample_count=cnt, variance=var)
+    assert (cnt[inside] == before[inside] + 16).all()
+    # pixels at or above max_samples are skipped
+    pix2, cnt2, var2 = gs.render(cam, 5, 8, seed=5, pixels=pix.copy(), sample_count=cnt.copy(), variance=var.copy())
+    np.testing.assert_array_equal(cnt2[inside], cnt[inside])
+    # cancellation before the first batch leaves the buffers untouched
+    flag = C.c_int32(1)
+    with pytest.raises(pico_gb300.PicoError) as e:
+        gs.render(cam, 5, 64, seed=6, pixels=pix.copy(), sample_count=cnt.copy(), variance=var.copy(),
+                  should_quit=flag)
+    assert e.value.status == -6
+
+
+def test_render_with_denoise_matches_atrous_of_render(ctx, oracle):
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(64, 64)
+    gs = ctx.upload(scene)
+    raw, cnt, var = gs.render(cam, 5, 8, seed=11)
+    den, cnt2, var2 = gs.render(cam, 5, 8, seed=11, denoise=True)
+    np.testing.assert_array_equal(cnt, cnt2)
+    n, p, d = oracle.scene(scene).denoiser_inputs(cam)
+    atrous_close(den, oracle.atrous(raw, n, p, d, 64, 64))
+
+
+def test_render_instance_field_runs(ctx):
+    """Many instances, a Lambert field lit by two quad lights; checks finite, non-trivial output."""
+    s = scenes.instance_field(n_instances=128, level=2, seed=17, extent=8.0)
+    s.materials.append(Material(diffuse=(0.8, 0.8, 0.8), emissive=(20.0, 20.0, 20.0)))
+    for k, y in enumerate((12.0, -12.0)):
+        s.meshes.append(scenes.quad_mesh([[-4, y, -4], [4, y, -4], [4, y, 4], [-4, y, 4]], [0, -np.sign(y), 0]))
+        s.instances.append(pico_gb300.Instance(len(s.meshes) - 1, scenes.glm_storage(np.eye(4)), pico_gb300.LIGHT, 1))
+    cam = scenes.field_camera(64)
+    cam.position = (0.0, 0.0, -25.0)
+    gs = ctx.upload(s)
+    assert gs.info()["lights"] == 2
+    pix, cnt, var = gs.render(cam, 5, 16, seed=2)
+    assert np.isfinite(pix).all() and pix.mean() > 0.0

@@ -26,12 +26,17 @@ def assert_same_hits(got, want, label=""):
 
 
 def random_rays(rng, n, lo, hi, normalize=True):
+    """Unnormalized directions are scaled to length >= 1: the reference prunes
+    TLAS nodes by comparing a parametric slab distance with a Euclidean hit
+    distance, which is conservative only for |D| >= 1; below that its answer
+    depends on its own visit order (every reference caller normalizes)."""
     r = np.zeros(n, RAY_DTYPE)
     r["org"][:, :3] = rng.uniform(lo, hi, size=(n, 3))
     r["org"][:, 3] = 1.0
     d = rng.normal(size=(n, 3))
-    if normalize:
-        d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    if not normalize:
+        d *= rng.uniform(1.0, 4.0, size=(n, 1))
     r["dir"][:, :3] = d
     r["dir"][:, 3] = 10000.0
     return r
