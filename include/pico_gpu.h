@@ -120,6 +120,16 @@ void pico_gpu_shutdown(pico_gpu_ctx* ctx);
 const char* pico_gpu_status_string(int status);
 const char* pico_gpu_last_error(const pico_gpu_ctx* ctx);
 
+/* Traversal order of every closest-hit query in a context.  NEAR_FIRST (the
+ * default) enters the nearer child first and breaks equal distances by the
+ * reference's depth-first rank; REFERENCE walks children 0 then 1 with strict
+ * comparisons exactly like BVH::get_closest_intersections (Core/BVH.cpp:27-63).
+ * They differ only where the reference's float slab test prunes a box whose
+ * triangle is a few ulp nearer than the best so far (near-ties at shared
+ * edges); REFERENCE reproduces the reference's choice there too. */
+enum pico_traversal_order { PICO_ORDER_NEAR_FIRST = 0, PICO_ORDER_REFERENCE = 1 };
+int pico_gpu_set_traversal_order(pico_gpu_ctx* ctx, int order);
+
 /* ---- scene -------------------------------------------------------------- */
 int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out);
 void pico_gpu_scene_free(pico_gpu_scene* scene);

@@ -36,6 +36,7 @@ SIGNATURES = {
     "pico_gpu_shutdown": (None, [_vp]),
     "pico_gpu_status_string": (C.c_char_p, [C.c_int]),
     "pico_gpu_last_error": (C.c_char_p, [_vp]),
+    "pico_gpu_set_traversal_order": (C.c_int, [_vp, C.c_int]),
     "pico_gpu_scene_upload": (C.c_int, [_vp, C.POINTER(CSceneDesc), C.POINTER(_vp)]),
     "pico_gpu_scene_free": (None, [_vp]),
     "pico_gpu_scene_info": (C.c_int, [_vp, C.POINTER(_u64)]),
@@ -108,6 +109,10 @@ class Context:
             self.close()
         except Exception:
             pass
+
+    def set_traversal_order(self, order: int):
+        """0: near-first (default), 1: the reference's child order (exact in near-tie cases)."""
+        self.check(self.lib.pico_gpu_set_traversal_order(self.handle, order), "set_traversal_order")
 
     def upload(self, scene: SceneData) -> "GpuScene":
         return GpuScene(self, scene)

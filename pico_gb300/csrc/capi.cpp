@@ -114,6 +114,14 @@ const char* pico_gpu_status_string(int status)
 
 const char* pico_gpu_last_error(const pico_gpu_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
 
+int pico_gpu_set_traversal_order(pico_gpu_ctx* ctx, int order)
+{
+    if (!ctx || (order != PICO_ORDER_NEAR_FIRST && order != PICO_ORDER_REFERENCE))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "unknown traversal order");
+    ctx->order = order;
+    return PICO_OK;
+}
+
 int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out)
 {
     if (!ctx || !desc || !out) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
@@ -206,7 +214,7 @@ int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene
     if (!ctx || !scene || (n && (!d_rays || !d_hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return set_error(ctx, PICO_ERR_INVALID_ARG, "rays not 16-byte aligned");
     const cudaError_t e = launch_trace(scene->view, d_rays, n, d_hits, ctx->status, false,
-                                       static_cast<cudaStream_t>(stream));
+                                       ctx->order, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_error(ctx, e, "trace launch");
     return PICO_OK;
 }
@@ -228,7 +236,7 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
     cudaError_t e = ctx->buf_e.reserve(sizeof(pico_hit) * (n ? n : 1));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->counters, 0, sizeof(ctx->status->counters), st);
     if (e == cudaSuccess)
-        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, st);
+        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, ctx->order, st);
     unsigned long long c[4] = {0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(c, ctx->status->counters, sizeof c, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -261,7 +269,7 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
         pico_hit* dh = static_cast<pico_hit*>(hbuf[s]->ptr);
         e = cudaMemcpyAsync(dr, rays + off, m * sizeof(pico_ray), cudaMemcpyHostToDevice, streams[s]);
         if (e == cudaSuccess)
-            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, streams[s]);
+            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, ctx->order, streams[s]);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(hits + off, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, streams[s]);
     }

@@ -35,6 +35,7 @@ struct pico_gpu_ctx {
     std::string last_error;
     pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
     RenderBuffers* render = nullptr;            // wavefront path state and image buffers
+    int order = PICO_ORDER_NEAR_FIRST;          // traversal order of every trace in this context
     pico::DeviceStatus* status2() { return status + 1; }
 };
 

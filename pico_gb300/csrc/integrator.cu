@@ -65,6 +65,7 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
 }
 
 // Closest hit for the paths in `q` (count in *count); persistent, 32 rays per fetch.
+template <int kOrder>
 __global__ void __launch_bounds__(128) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                     const uint32_t* count, unsigned long long* work, int* err,
                                                     bool shadow)
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(128) extend_kernel(SceneView sc, PathBatch b, 
             const float4 o = shadow ? b.sorg[i] : b.org[i];
             const float4 d = shadow ? b.sdir[i] : b.dir[i];
             TraceHit h;
-            const int s = trace_closest<false>(sc, o, d, h, nullptr);
+            const int s = trace_closest<false, kOrder>(sc, o, d, h, nullptr);
             if (s != kTraceOk) atomicOr(err, s);
             const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
             if (shadow) {
@@ -260,6 +261,7 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
 }
 
 // Scene::generate_denoiser_inputs: one primary ray per pixel with xi = (0, 0).
+template <int kOrder>
 __global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView cam, uint32_t W, uint32_t H,
                                                      float* normals, float* positions, float* diffuse, int* err)
 {
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView c
         float4 o, d;
         camera_ray(cam, 0.0f, 0.0f, p % W, p / W, o, d);
         TraceHit h;
-        const int s = trace_closest<false>(sc, o, d, h, nullptr);
+        const int s = trace_closest<false, kOrder>(sc, o, d, h, nullptr);
         if (s != kTraceOk) atomicOr(err, s);
         float n[3], pos[3], alb[3];
         if (s == kTraceOk && h.rank != kNoHit) {
@@ -302,19 +304,28 @@ static unsigned grid_for(uint32_t n, int threads)
     return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
+template <int kOrder>
 static unsigned extend_grid()
 {
     static int per_sm = 0;
     if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder>, 128, 0);
         if (per_sm < 1) per_sm = 1;
     }
     return (unsigned)(sm_count() * per_sm);
 }
 
+template <int kOrder>
+static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
+                          DeviceStatus* status, bool shadow, cudaStream_t st)
+{
+    extend_kernel<kOrder><<<extend_grid<kOrder>(), 128, 0, st>>>(sc, b, q, count, &status->work,
+                                                                  &status->trace_error, shadow);
+}
+
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                DeviceStatus* status, cudaStream_t st)
+                                DeviceStatus* status, int order, cudaStream_t st)
 {
     cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
@@ -324,8 +335,10 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     for (uint32_t depth = 0; depth <= max_depth; ++depth) {
         e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
-        extend_kernel<<<extend_grid(), 128, 0, st>>>(sc, b, b.queue[cur], &b.counters[cur], &status->work,
-                                                      &status->trace_error, false);
+        if (order == kReferenceOrder)
+            launch_extend<kReferenceOrder>(sc, b, b.queue[cur], &b.counters[cur], status, false, st);
+        else
+            launch_extend<kNearFirst>(sc, b, b.queue[cur], &b.counters[cur], status, false, st);
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
@@ -334,8 +347,10 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         if (depth < max_depth) {
             e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
             if (e != cudaSuccess) return e;
-            extend_kernel<<<extend_grid(), 128, 0, st>>>(sc, b, b.shadow_queue, &b.counters[2], &status->work,
-                                                          &status->trace_error, true);
+            if (order == kReferenceOrder)
+                launch_extend<kReferenceOrder>(sc, b, b.shadow_queue, &b.counters[2], status, true, st);
+            else
+                launch_extend<kNearFirst>(sc, b, b.shadow_queue, &b.counters[2], status, true, st);
         }
         cur ^= 1;
     }
@@ -345,10 +360,14 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
 }
 
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
-                           float* positions, float* diffuse, DeviceStatus* status, cudaStream_t st)
+                           float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st)
 {
-    gbuffer_kernel<<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions, diffuse,
-                                                          &status->trace_error);
+    if (order == kReferenceOrder)
+        gbuffer_kernel<kReferenceOrder><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions,
+                                                                             diffuse, &status->trace_error);
+    else
+        gbuffer_kernel<kNearFirst><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions, diffuse,
+                                                                        &status->trace_error);
     return cudaGetLastError();
 }
 

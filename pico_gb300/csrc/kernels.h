@@ -20,6 +20,6 @@ struct DeviceStatus {
 int sm_count();
 
 cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, pico_hit* hits,
-                         DeviceStatus* status, bool count, cudaStream_t stream);
+                         DeviceStatus* status, bool count, int order, cudaStream_t stream);
 
 }  // namespace pico

@@ -37,9 +37,9 @@ struct PathBatch {
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                DeviceStatus* status, cudaStream_t st);
+                                DeviceStatus* status, int order, cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
-                           float* positions, float* diffuse, DeviceStatus* status, cudaStream_t st);
+                           float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
 cudaError_t launch_atrous(const float* pixels, const float* normals, const float* positions, const float* diffuse,
                           uint32_t W, uint32_t H, float* scratch_a, float* scratch_b, float* tile_stats, float* out,
                           cudaStream_t st);

@@ -194,7 +194,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
                 b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
                 b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
                 e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
-                                        cfg->max_variance, ctx->status, st);
+                                        cfg->max_variance, ctx->status, ctx->order, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
             }
@@ -208,7 +208,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
             if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
         if (e == cudaSuccess)
-            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, st);
+            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, ctx->order, st);
         if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
         status = run_atrous(ctx, r, as<float>(r.pixels), as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
                             as<float>(r.out), st);
@@ -241,7 +241,7 @@ int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, con
         if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
     if (e == cudaSuccess)
         e = launch_gbuffer(scene->view, make_camera_view(*camera), W, H, as<float>(r.gn), as<float>(r.gp),
-                           as<float>(r.gd), ctx->status, st);
+                           as<float>(r.gd), ctx->status, ctx->order, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(normals, r.gn.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(positions, r.gp.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(diffuse, r.gd.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);

@@ -11,7 +11,7 @@ namespace pico {
 
 constexpr int kTraceThreads = 128;
 
-template <bool kCount>
+template <bool kCount, int kOrder>
 __global__ void __launch_bounds__(kTraceThreads) trace_kernel(SceneView sc, const float4* __restrict__ rays,
                                                               uint64_t n, pico_hit* __restrict__ hits,
                                                               DeviceStatus* status)
@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(kTraceThreads) trace_kernel(SceneView sc, cons
         if (i < n) {
             const float4 o = __ldg(rays + 2 * i), d = __ldg(rays + 2 * i + 1);
             TraceHit h;
-            const int s = trace_closest<kCount>(sc, o, d, h, &cnt);
+            const int s = trace_closest<kCount, kOrder>(sc, o, d, h, &cnt);
             if (s != kTraceOk) atomicOr(&status->trace_error, s);
             pico_hit out;
             if (h.rank != kNoHit && s == kTraceOk) {
@@ -68,28 +68,35 @@ int sm_count()
     return sms;
 }
 
-cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, pico_hit* hits,
-                         DeviceStatus* status, bool count, cudaStream_t stream)
+template <bool kCount, int kOrder>
+static cudaError_t launch_trace_t(const SceneView& sc, const float4* r, uint64_t n, pico_hit* hits,
+                                  DeviceStatus* status, cudaStream_t stream)
 {
-    cudaError_t e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), stream);
-    if (e != cudaSuccess) return e;
-    if (n == 0) return cudaSuccess;
-    int per_sm = 0;
-    if (count)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<true>, kTraceThreads, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<false>, kTraceThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
+    static int per_sm = 0;
+    if (!per_sm) {
+        const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trace_kernel<kCount, kOrder>,
+                                                                            kTraceThreads, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
     uint64_t blocks = (uint64_t)sm_count() * (uint64_t)per_sm;
     const uint64_t needed = (n + kTraceThreads - 1) / kTraceThreads;
     if (blocks > needed) blocks = needed;
-    const float4* r = reinterpret_cast<const float4*>(rays);
-    if (count)
-        trace_kernel<true><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(sc, r, n, hits, status);
-    else
-        trace_kernel<false><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(sc, r, n, hits, status);
+    trace_kernel<kCount, kOrder><<<(unsigned)blocks, kTraceThreads, 0, stream>>>(sc, r, n, hits, status);
     return cudaGetLastError();
+}
+
+cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, pico_hit* hits,
+                         DeviceStatus* status, bool count, int order, cudaStream_t stream)
+{
+    cudaError_t e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), stream);
+    if (e != cudaSuccess || n == 0) return e;
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    if (order == kReferenceOrder)
+        return count ? launch_trace_t<true, kReferenceOrder>(sc, r, n, hits, status, stream)
+                     : launch_trace_t<false, kReferenceOrder>(sc, r, n, hits, status, stream);
+    return count ? launch_trace_t<true, kNearFirst>(sc, r, n, hits, status, stream)
+                 : launch_trace_t<false, kNearFirst>(sc, r, n, hits, status, stream);
 }
 
 }  // namespace pico

@@ -86,13 +86,28 @@ __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, 
     return false;
 }
 
-template <bool kCount>
+// Traversal orders.  kNearFirst enters the nearer child first and breaks
+// equal distances by rank; kReferenceOrder walks children 0 then 1 and keeps the
+// first of equal distances, re-testing a deferred child against the best
+// distance at the moment it is reached, exactly like the reference's recursion
+// (Core/BVH.cpp:27-63).  Both return the reference's answer except where the
+// reference's own float slab test rejects a box whose triangle lies a few ulp
+// nearer than the current best (triangles on box faces meeting at an edge):
+// there only the reference order reproduces its choice.
+enum TraversalOrder : int { kNearFirst = 0, kReferenceOrder = 1 };
+
+// A stack entry: a reference and the slab distance of its box (NaN = box
+// missed; -inf = no box to test).
+struct StackEntry { uint32_t ref; float tmin; };
+
+template <bool kCount, int kOrder>
 __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
                                              TraceCounters* cnt)
 {
     using namespace ex;
     const float kInf = __int_as_float(0x7f800000);
-    uint32_t stack[kTraceStack];
+    const float kNan = __int_as_float(0x7fffffff);
+    StackEntry stack[kTraceStack];
     int sp = 0;
 
     best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
@@ -104,6 +119,11 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
     uint32_t ltri = kNoHit, cur = 0;
     bool in_blas = false;
 
+    // `visit` decides whether a box at slab distance t is entered against the current best.
+    auto visit = [&](float t, float limit) -> bool {
+        return kOrder == kReferenceOrder ? (t < limit) : (t <= limit && t < kInf);
+    };
+
     uint32_t ref = PICO_REF_DONE;
     {
         bool h;
@@ -114,7 +134,19 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
 
     for (uint32_t iter = 0;; ++iter) {
         if (iter >= kTraceMaxIter) return kTraceIterLimit;
-        if (ref == PICO_REF_DONE) break;
+        if (ref == PICO_REF_DONE) {
+            // pop the next entry whose box still qualifies
+            bool found = false;
+            while (sp > 0) {
+                const StackEntry e = stack[--sp];
+                if (e.tmin == -kInf || visit(e.tmin, in_blas ? lt : best.t)) {
+                    ref = e.ref;
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) break;
+        }
         if (!pico_is_leaf(ref)) {
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
@@ -124,21 +156,31 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
             const float rix = in_blas ? qix : wix, riy = in_blas ? qiy : wiy, riz = in_blas ? qiz : wiz;
             const float limit = in_blas ? lt : best.t;
             bool h0, h1;
-            const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-            const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
-            const bool v0 = h0 && t0 <= limit && t0 < kInf;
-            const bool v1 = h1 && t1 <= limit && t1 < kInf;
-            if (v0 && v1) {
-                const bool swap = t1 < t0;
-                if (sp >= kTraceStack) return kTraceStackOverflow;
-                stack[sp++] = swap ? n3.x : n3.y;
-                ref = swap ? n3.y : n3.x;
-            } else if (v0) {
-                ref = n3.x;
-            } else if (v1) {
-                ref = n3.y;
+            float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
+            float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            t0 = h0 ? t0 : kNan;
+            t1 = h1 ? t1 : kNan;
+            if (kOrder == kReferenceOrder) {
+                // child 1 waits on the stack and is tested when reached
+                if (n3.y != PICO_REF_EMPTY) {
+                    if (sp >= kTraceStack) return kTraceStackOverflow;
+                    stack[sp++] = StackEntry{n3.y, t1};
+                }
+                ref = (n3.x != PICO_REF_EMPTY && visit(t0, limit)) ? n3.x : PICO_REF_DONE;
             } else {
-                ref = sp ? stack[--sp] : PICO_REF_DONE;
+                const bool v0 = visit(t0, limit), v1 = visit(t1, limit);
+                if (v0 && v1) {
+                    const bool swap = t1 < t0;
+                    if (sp >= kTraceStack) return kTraceStackOverflow;
+                    stack[sp++] = swap ? StackEntry{n3.x, t0} : StackEntry{n3.y, t1};
+                    ref = swap ? n3.y : n3.x;
+                } else if (v0) {
+                    ref = n3.x;
+                } else if (v1) {
+                    ref = n3.y;
+                } else {
+                    ref = PICO_REF_DONE;
+                }
             }
             continue;
         }
@@ -157,17 +199,19 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                 const float wz = row4(f2, px, py, pz, 1.0f), ww = row4(f3, px, py, pz, 1.0f);
                 const float ex_ = sub(wx, o.x), ey = sub(wy, o.y), ez = sub(wz, o.z), ew = sub(ww, o.w);
                 const float tw = sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
-                if (tw < best.t || (tw == best.t && cur < best.rank)) {
+                const bool better = kOrder == kReferenceOrder ? tw < best.t
+                                                              : (tw < best.t || (tw == best.t && cur < best.rank));
+                if (better) {
                     best.t = tw; best.rank = cur; best.tri = ltri; best.u = lu; best.v = lv;
                 }
             }
             in_blas = false;
-            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            ref = PICO_REF_DONE;
             continue;
         }
         const uint32_t first = pico_leaf_first(ref), count = pico_leaf_count(ref);
         if (count == 0) {
-            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            ref = PICO_REF_DONE;
             continue;
         }
         if (in_blas) {
@@ -175,18 +219,20 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                 const uint32_t tri = first + k;
                 float t, u, v;
                 if (kCount) cnt->tris++;
-                if (intersect_triangle(sc.tris + tri, qox, qoy, qoz, qdx, qdy, qdz, t, u, v) &&
-                    (t < lt || (t == lt && tri < ltri))) {
-                    lt = t; ltri = tri; lu = u; lv = v;
+                if (intersect_triangle(sc.tris + tri, qox, qoy, qoz, qdx, qdy, qdz, t, u, v)) {
+                    const bool better = kOrder == kReferenceOrder ? t < lt : (t < lt || (t == lt && tri < ltri));
+                    if (better) {
+                        lt = t; ltri = tri; lu = u; lv = v;
+                    }
                 }
             }
-            ref = stack[--sp];   // the END_BLAS sentinel is below, so sp > 0 here
+            ref = PICO_REF_DONE;
             continue;
         }
         // TLAS leaf: search instance `first`; the rest of the leaf waits on the stack.
         if (count > 1) {
             if (sp >= kTraceStack) return kTraceStackOverflow;
-            stack[sp++] = pico_leaf_ref(first + 1, count - 1);
+            stack[sp++] = StackEntry{pico_leaf_ref(first + 1, count - 1), -kInf};
         }
         if (kCount) cnt->insts++;
         const float4* ip = reinterpret_cast<const float4*>(sc.insts + first);
@@ -198,11 +244,11 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
         bool h;
         const float tm = slab(rl.x, rh.x, rl.y, rh.y, rl.z, rh.z, qox, qoy, qoz, qix, qiy, qiz, h);
         if (!(h && tm < kInf)) {
-            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            ref = PICO_REF_DONE;
             continue;
         }
         if (sp >= kTraceStack) return kTraceStackOverflow;
-        stack[sp++] = PICO_REF_END_BLAS;
+        stack[sp++] = StackEntry{PICO_REF_END_BLAS, -kInf};
         in_blas = true;
         cur = first;
         lt = kInf; ltri = kNoHit;

@@ -54,12 +54,24 @@ def test_bsdf_routines_match_reference(ctx, oracle):
 
 
 def test_denoiser_inputs_bit_exact(ctx, oracle):
+    """In the reference's traversal order the G-buffer is bit-exact; near-first
+    differs only on pixels whose primary ray grazes the edge where two box-aligned
+    walls meet, where the reference's own slab test decides between near-equal hits."""
     z = np.load(GOLDEN / "atrous.npz")
     scene, cam = load_scene(z, "cornell"), load_camera(z["cam"])
     gs = ctx.upload(scene)
-    n, p, d = gs.denoiser_inputs(cam)
+    try:
+        ctx.set_traversal_order(1)
+        n, p, d = gs.denoiser_inputs(cam)
+    finally:
+        ctx.set_traversal_order(0)
     for got, key in ((n, "normals"), (p, "positions"), (d, "diffuse")):
         np.testing.assert_array_equal(got.view(np.uint32), z[key].view(np.uint32), err_msg=key)
+    n2, p2, d2 = gs.denoiser_inputs(cam)
+    differ = (p2 != z["positions"]).any(axis=2)
+    assert differ.mean() < 1e-3
+    # the near-first choice is an equally near hit: positions agree to float precision
+    np.testing.assert_allclose(p2[differ], z["positions"][differ], rtol=1e-5, atol=1e-5)
 
 
 def atrous_close(got, want, rtol=1e-4):
@@ -100,31 +112,49 @@ def test_atrous_device_path(ctx, oracle):
     atrous_close(out.cpu().numpy(), z["denoised"])
 
 
-def reference_render(oracle, scene, cam, spp, depth, seed=1):
-    W, H = cam.resolution
-    idx = np.arange(W * H, dtype=np.uint32)
-    seeds = (np.arange(W * H, dtype=np.uint64) * np.uint64(2654435761) + np.uint64(seed)) % np.uint64(2 ** 32)
-    return oracle.scene(scene).render_pixels(cam, depth, spp, idx, seeds)
+def batch_means(render_batch, K):
+    """K independent renders (fresh progressive buffers each): mean and standard
+    error per pixel channel from the spread of the batch means.  The estimator has
+    rare high-value paths, so one render's own variance buffer underestimates the
+    error of some pixels; batch means do not."""
+    imgs, counts = [], []
+    for k in range(K):
+        pix, cnt = render_batch(k)
+        imgs.append(pix)
+        counts.append(cnt)
+    imgs = np.stack(imgs)
+    return imgs.mean(0), imgs.std(0, ddof=1) / np.sqrt(K), np.stack(counts)
 
 
 def test_render_statistically_matches_reference(ctx, oracle):
     scene = scenes.cornell_box()
     cam = scenes.cornell_camera(48, 48)
-    spp, depth = 512, 5
+    W, H = cam.resolution
+    K, spp, depth = 16, 32, 5
     gs = ctx.upload(scene)
-    g_pix, g_cnt, g_var = gs.render(cam, depth, spp, seed=7)
-    r_pix, r_cnt, r_var = reference_render(oracle, scene, cam, spp, depth)
-    # both means average samples 2..N (Scene.cpp:185-191); the variance buffer is
-    # the running population variance, so SE^2 = var / (count - 1)
-    se = np.sqrt(g_var / np.maximum(g_cnt - 1, 1)[..., None] + r_var / np.maximum(r_cnt - 1, 1)[..., None])
-    z = np.abs(g_pix - r_pix) / np.maximum(se, 1e-6)
+    os_ = oracle.scene(scene)
+    idx = np.arange(W * H, dtype=np.uint32)
+    rng = np.random.default_rng(77)
+
+    def gpu_batch(k):
+        pix, cnt, _ = gs.render(cam, depth, spp, seed=1000 + k)
+        return pix, cnt
+
+    def ref_batch(k):
+        pix, cnt, _ = os_.render_pixels(cam, depth, spp, idx, rng.integers(0, 2 ** 32, W * H, dtype=np.uint64))
+        return pix, cnt
+
+    g_mean, g_se, g_cnt = batch_means(gpu_batch, K)
+    r_mean, r_se, r_cnt = batch_means(ref_batch, K)
+    z = np.abs(g_mean - r_mean) / np.maximum(np.sqrt(g_se ** 2 + r_se ** 2), 1e-6)
     frac = (z <= 4.0).mean()
     assert frac >= 0.995, f"only {frac:.4f} of pixel channels within 4 standard errors"
+    assert z.mean() < 1.0, f"mean |z| {z.mean():.3f}"
     # pixels that only see the black sky stop after 6 samples in both
     # (variance exactly 0 after more than 4 samples, Scene.cpp:196-197)
     sky = sky_pixels(oracle, scene, cam)
-    assert sky.any() and (g_cnt[sky] == 6).all() and (r_cnt[sky] == 6).all()
-    assert abs(g_pix.mean() - r_pix.mean()) < 0.02 * r_pix.mean()
+    assert sky.any() and (g_cnt[:, sky] == 6).all() and (r_cnt[:, sky] == 6).all()
+    assert abs(g_mean.mean() - r_mean.mean()) < 0.01 * r_mean.mean()
 
 
 def sky_pixels(oracle, scene, cam):
@@ -168,7 +198,7 @@ def test_render_with_denoise_matches_atrous_of_render(ctx, oracle):
     raw, cnt, var = gs.render(cam, 5, 8, seed=11)
     den, cnt2, var2 = gs.render(cam, 5, 8, seed=11, denoise=True)
     np.testing.assert_array_equal(cnt, cnt2)
-    n, p, d = oracle.scene(scene).denoiser_inputs(cam)
+    n, p, d = gs.denoiser_inputs(cam)   # the same traversal order the render used
     atrous_close(den, oracle.atrous(raw, n, p, d, 64, 64))
 
 

@@ -43,10 +43,16 @@ def random_rays(rng, n, lo, hi, normalize=True):
 
 
 def check(ctx, oracle, scene, rays, label):
+    """Both traversal orders must reproduce the oracle exactly on these batches."""
     gs = ctx.upload(scene)
-    got = gs.trace_closest(rays)
     want = oracle.scene(scene).trace(rays)
-    assert_same_hits(got, want, label)
+    try:
+        for order in (1, 0):
+            ctx.set_traversal_order(order)
+            got = gs.trace_closest(rays)
+            assert_same_hits(got, want, f"{label} (order {order})")
+    finally:
+        ctx.set_traversal_order(0)
     return got, want
 
 
