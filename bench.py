@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
+    ap.add_argument("--order", type=int, default=0, choices=[0, 1],
+                    help="traversal order: 0 near-first (default), 1 the reference's child order")
     return ap.parse_args()
 
 
@@ -214,6 +216,7 @@ def main():
     scene, rays = workload(args)
     n = len(rays)
     ctx = pico_gb300.Context(local)
+    ctx.set_traversal_order(args.order)
     gs = ctx.upload(scene)
     info = gs.info()
 
@@ -284,7 +287,8 @@ def main():
     dpr = dram_traffic_per_ray()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": dpr * n if dpr else None, "peak_source": peak_src,
-                "kernel": "trace_kernel<false>", "algorithmic_bytes_per_launch": algo_bytes,
+                "kernel": f"trace_kernel<false, {'near-first' if args.order == 0 else 'reference order'}>",
+                "algorithmic_bytes_per_launch": algo_bytes,
                 "visits_per_ray": {k: v / n for k, v in counts.items()},
                 "note": "scene (~1.3 MB) is L2-resident; algorithmic bytes count every node/triangle/instance "
                         "fetch (64/48/144 B) plus ray in/hit out, so frac vs HBM can exceed 1"}

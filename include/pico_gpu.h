@@ -18,6 +18,7 @@
  *                              (Render/Integrators.hpp:33-57)
  *   pico_gpu_denoiser_inputs   Scene::generate_denoiser_inputs (Core/Scene.cpp:248-294)
  *   pico_gpu_atrous            Util::atrous_denoise (Util/Denoisers.hpp:9)
+ *   pico_gpu_tonemap           Util::reinhard_tone_mapping (Util/ToneMappers.hpp, ToneMappers.cpp:12-44)
  *
  * Conventions: every function returns PICO_OK (0) or a negative PICO_ERR_*
  * code; host buffers are caller-owned and the call returns when they hold
@@ -166,6 +167,10 @@ int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals
 int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float* d_normals,
                            const float* d_positions, const float* d_diffuse, uint32_t width,
                            uint32_t height, float* d_out, void* stream);
+
+/* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44) in place on W*H*3 floats. */
+int pico_gpu_tonemap(pico_gpu_ctx* ctx, float* pixels, uint32_t width, uint32_t height);
+int pico_gpu_tonemap_device(pico_gpu_ctx* ctx, float* d_pixels, uint32_t width, uint32_t height, void* stream);
 
 /* ---- shading routines on caller inputs ---------------------------------------
  * BSRDF::pdf and BSRDF::sample (Render/BSRDF.hpp:50-52) and direct_lighting_pdf

@@ -138,6 +138,8 @@ void po_denoiser_inputs(const po_scene* s, const po_camera* cam, uint32_t W, uin
 void po_view_matrix(const po_camera* cam, float* m4);          /* Camera::getViewMatrix */
 void po_atrous_denoise(const float* pixels, const float* normals, const float* positions,
                        const float* diffuse, uint32_t W, uint32_t H, float* out);
+/* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44), in place. */
+void po_reinhard(float* pixels, uint32_t W, uint32_t H);
 
 #ifdef __cplusplus
 }

@@ -115,6 +115,7 @@ class Oracle(_SceneLib):
             "po_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "po_view_matrix": (None, [C.POINTER(CCamera), _fp]),
             "po_atrous_denoise": (None, [_fp, _fp, _fp, _fp, _u32, _u32, _fp]),
+            "po_reinhard": (None, [_fp, _u32, _u32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -225,11 +226,20 @@ class Oracle(_SceneLib):
                                cnt.ctypes.data_as(_up), var.ctypes.data_as(_fp))
         return px, int(cnt[0]), var
 
+    def reinhard(self, pixels, W, H) -> np.ndarray:
+        return _reinhard(self.lib.po_reinhard, pixels, W, H)
+
     def atrous(self, pixels, normals, positions, diffuse, W, H) -> np.ndarray:
         out = np.empty(W * H * 3, np.float32)
         self.lib.po_atrous_denoise(_f(pixels), _f(normals), _f(positions), _f(diffuse), W, H,
                                    out.ctypes.data_as(_fp))
         return out.reshape(H, W, 3)
+
+
+def _reinhard(fn, pixels, W, H):
+    out = np.ascontiguousarray(pixels, np.float32).copy()
+    fn(out.ctypes.data_as(_fp), W, H)
+    return out
 
 
 class OracleScene:
@@ -354,6 +364,7 @@ class Reference(_SceneLib):
                                                C.POINTER(_u64), _u32, _fp, _up, _fp, _i32]),
             "ref_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "ref_atrous": (C.c_double, [_fp, _fp, _fp, _fp, _u32, _u32, _fp, _i32]),
+            "ref_reinhard": (None, [_fp, _u32, _u32]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -362,6 +373,9 @@ class Reference(_SceneLib):
 
     def scene(self, scene: SceneData) -> "ReferenceScene":
         return ReferenceScene(self, scene)
+
+    def reinhard(self, pixels, W, H) -> np.ndarray:
+        return _reinhard(self.lib.ref_reinhard, pixels, W, H)
 
 
 class ReferenceScene:

@@ -7,6 +7,7 @@
  *   Util::atrous_denoise              Util/Denoisers.cpp:107-126
  *   blend_pixel (per 64x64 tile)      Util/Denoisers.cpp:18-101
  *   Tiler tile walk                   Util/Tiler.hpp:20-49
+ *   Util::reinhard_tone_mapping       Util/ToneMappers.cpp:12-44
  *
  * The 5x5 kernel table keeps the reference's 0.09563 entry at index 17.
  * std::min(std::exp(x), 1.0f) is restated as `(1 < e) ? 1 : e`, which keeps
@@ -146,4 +147,20 @@ void po_atrous_denoise(const float* pixels, const float* normals, const float* p
             }
     }
     free(buf[0]);
+}
+
+/* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44): global white point
+ * = max luminance (std::max from 0, so NaN luminances are skipped), then
+ * p * (1 + p / w^2) / (1 + p) per channel, in place. */
+void po_reinhard(float* pixels, uint32_t W, uint32_t H)
+{
+    const size_t n = (size_t)W * H;
+    float white = 0.0f;
+    for (size_t i = 0; i < n; ++i) white = f_max(white, lum(pixels + 3 * i));
+    const float w2 = white * white;
+    for (size_t i = 0; i < 3 * n; ++i) {
+        const float p = pixels[i];
+        const float num = p * (1.0f + (p / w2));
+        pixels[i] = num / (1.0f + p);
+    }
 }

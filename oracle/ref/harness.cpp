@@ -33,6 +33,7 @@
 #include "Util/AliasTable.hpp"
 #include "Util/Denoisers.hpp"
 #include "Util/Tiler.hpp"
+#include "Util/ToneMappers.hpp"
 
 #include "assimp/mesh.h"
 #include "glm/ext.hpp"   // as Core/Scene.cpp:24 (brings gtx/scalar_multiplication)
@@ -602,6 +603,15 @@ double ref_atrous(const float* pixels, const float* normals, const float* positi
     std::memcpy(out, r, sizeof(float) * 3 * (size_t)W * H);
     delete[] r;
     return std::chrono::duration<double>(t1 - t0).count();
+}
+
+// Util::reinhard_tone_mapping in place, on a one-worker pool.
+void ref_reinhard(float* pixels, uint32_t W, uint32_t H)
+{
+    ThreadPool pool(1u);
+    Core::Rand::xorshift_random rng(99u);
+    Util::Tiler tiler(pool, rng, glm::uvec2(W, H), glm::uvec2(64, 64));
+    Util::reinhard_tone_mapping(reinterpret_cast<glm::vec3*>(pixels), glm::uvec2(W, H), tiler);
 }
 
 } // extern "C"

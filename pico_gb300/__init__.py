@@ -49,6 +49,8 @@ SIGNATURES = {
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
+    "pico_gpu_tonemap": (C.c_int, [_vp, _fp, _u32, _u32]),
+    "pico_gpu_tonemap_device": (C.c_int, [_vp, _vp, _u32, _u32, _vp]),
     "pico_gpu_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
@@ -122,6 +124,12 @@ class Context:
         out = np.empty(width * height * 3, np.float32)
         self.check(self.lib.pico_gpu_atrous(self.handle, *map(_f32, arrs), width, height, _f32(out)), "atrous")
         return out.reshape(height, width, 3)
+
+    def tonemap(self, pixels, width: int, height: int) -> np.ndarray:
+        """Util::reinhard_tone_mapping on a copy of `pixels`."""
+        out = np.ascontiguousarray(pixels, dtype=np.float32).copy()
+        self.check(self.lib.pico_gpu_tonemap(self.handle, _f32(out), width, height), "tonemap")
+        return out
 
     def bsdf_eval(self, kinds, materials, V, N, H, xi):
         """Device BSRDF routines on given inputs: (pdf, L, P, energy, direct_pdf)."""

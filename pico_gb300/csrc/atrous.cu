@@ -20,6 +20,8 @@
 #include "exact_math.cuh"
 #include "kernels_render.h"
 
+#include <algorithm>
+
 namespace pico {
 
 __constant__ float kAtrousWeights[25] = {
@@ -167,6 +169,56 @@ cudaError_t launch_atrous(const float* pixels, const float* normals, const float
         atrous_blend_kernel<<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats, dst);
         src = dst;
     }
+    return cudaGetLastError();
+}
+
+}  // namespace pico
+
+// ---------------------------------------------------------------------------
+// Reinhard tone mapping (Util::reinhard_tone_mapping, Util/ToneMappers.cpp:12-44):
+// a global white point = the largest luminance (from 0; NaN luminances are
+// skipped, as std::max(white, lum) skips them), then per channel
+// p * (1 + p / white^2) / (1 + p), in place.  Non-negative floats order like
+// their bit patterns, so the maximum is an atomicMax on the bits.
+namespace pico {
+
+__global__ void __launch_bounds__(256) white_point_kernel(const float* __restrict__ pix, size_t npx,
+                                                          unsigned* __restrict__ white_bits)
+{
+    float w = 0.0f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npx; i += (size_t)gridDim.x * blockDim.x) {
+        const float l = luminance(pix[3 * i], pix[3 * i + 1], pix[3 * i + 2]);
+        w = (w < l) ? l : w;
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        const float o = __shfl_down_sync(0xffffffffu, w, off);
+        w = (w < o) ? o : w;
+    }
+    if ((threadIdx.x & 31u) == 0) atomicMax(white_bits, __float_as_uint(w));
+}
+
+__global__ void __launch_bounds__(256) reinhard_kernel(float* __restrict__ pix, size_t n,
+                                                       const unsigned* __restrict__ white_bits)
+{
+    using namespace ex;
+    const float w = __uint_as_float(*white_bits);
+    const float w2 = mul(w, w);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float p = pix[i];
+        const float num = mul(p, add(1.0f, div(p, w2)));
+        pix[i] = div(num, add(1.0f, p));
+    }
+}
+
+cudaError_t launch_reinhard(float* pixels, uint32_t W, uint32_t H, unsigned* scratch, cudaStream_t st)
+{
+    const size_t npx = (size_t)W * H;
+    if (npx == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    const unsigned blocks = (unsigned)std::min<size_t>((npx + 255) / 256, (size_t)sm_count() * 8);
+    white_point_kernel<<<blocks, 256, 0, st>>>(pixels, npx, scratch);
+    reinhard_kernel<<<blocks, 256, 0, st>>>(pixels, 3 * npx, scratch);
     return cudaGetLastError();
 }
 

@@ -64,47 +64,77 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
     }
 }
 
-// Closest hit for the paths in `q` (count in *count); persistent, 32 rays per fetch.
+// Closest hit for the paths in `q` (count in *count).  Persistent with the
+// same lane refill as the batch trace kernel: a warp tops up its finished
+// lanes from the queue whenever a quarter of them are idle.
+__device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b, uint32_t i, const TraceHit& h,
+                                              int s, bool shadow)
+{
+    const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
+    if (shadow) {
+        // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176)
+        if (rank != kNoHit) {
+            const uint32_t inst = sc.insts[rank].inst_id;
+            const GpuInstanceShade is = sc.inst_shade[inst];
+            if (is.bsdf == PICO_BSDF_LIGHT) {
+                const GpuMaterial& m = sc.materials[is.material];
+                const float4 c = b.scontrib[i], e = b.senergy[i];
+                float4 p = b.pay[i];
+                p.x = p.x + (c.x * m.emissive[0]) * e.x;
+                p.y = p.y + (c.y * m.emissive[1]) * e.y;
+                p.z = p.z + (c.z * m.emissive[2]) * e.z;
+                b.pay[i] = p;
+            }
+        }
+    } else {
+        b.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(rank));
+        b.hit_tri[i] = h.tri;
+    }
+}
+
 template <int kOrder>
 __global__ void __launch_bounds__(128) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                     const uint32_t* count, unsigned long long* work, int* err,
                                                     bool shadow)
 {
+    constexpr unsigned kFull = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t n = *count;
+    Traversal<false, kOrder> tr;
+    StackEntry stack[kTraceStack];
+    uint32_t i = 0, steps = 0;
+    bool active = false, exhausted = false;
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(work, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const unsigned long long k = base + lane;
-        if (k < n) {
-            const uint32_t i = q[k];
-            const float4 o = shadow ? b.sorg[i] : b.org[i];
-            const float4 d = shadow ? b.sdir[i] : b.dir[i];
-            TraceHit h;
-            const int s = trace_closest<false, kOrder>(sc, o, d, h, nullptr);
-            if (s != kTraceOk) atomicOr(err, s);
-            const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
-            if (shadow) {
-                // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176)
-                if (rank != kNoHit) {
-                    const uint32_t inst = sc.insts[rank].inst_id;
-                    const GpuInstanceShade is = sc.inst_shade[inst];
-                    if (is.bsdf == PICO_BSDF_LIGHT) {
-                        const GpuMaterial& m = sc.materials[is.material];
-                        const float4 c = b.scontrib[i], e = b.senergy[i];
-                        float4 p = b.pay[i];
-                        p.x = p.x + (c.x * m.emissive[0]) * e.x;
-                        p.y = p.y + (c.y * m.emissive[1]) * e.y;
-                        p.z = p.z + (c.z * m.emissive[2]) * e.z;
-                        b.pay[i] = p;
-                    }
+        if (!exhausted) {
+            const unsigned idle = __ballot_sync(kFull, !active);
+            const int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == (unsigned)leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
+            base = __shfl_sync(kFull, base, leader);
+            if (base + __popc(idle) >= n) exhausted = true;
+            if (!active) {
+                const unsigned long long k = base + __popc(idle & ((1u << lane) - 1u));
+                if (k < n) {
+                    i = q[k];
+                    tr.start(sc, shadow ? b.sorg[i] : b.org[i], shadow ? b.sdir[i] : b.dir[i]);
+                    active = true;
+                    steps = 0;
                 }
-            } else {
-                b.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(rank));
-                b.hit_tri[i] = h.tri;
             }
+        }
+        if (!__any_sync(kFull, active)) break;
+        const int refill_at = exhausted ? 32 : 8;
+        for (;;) {
+            if (active) {
+                int s = tr.step(sc, stack, nullptr);
+                if (s == kTraceOk && ++steps >= kTraceMaxIter) s = kTraceIterLimit;
+                if (s != kTraceOk) {
+                    if (s != kTraceDone) atomicOr(err, s);
+                    extend_finish(sc, b, i, tr.best, s == kTraceDone ? kTraceOk : s, shadow);
+                    active = false;
+                }
+            }
+            if (__popc(__ballot_sync(kFull, !active)) >= refill_at) break;
         }
     }
 }

@@ -43,5 +43,6 @@ cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t 
 cudaError_t launch_atrous(const float* pixels, const float* normals, const float* positions, const float* diffuse,
                           uint32_t W, uint32_t H, float* scratch_a, float* scratch_b, float* tile_stats, float* out,
                           cudaStream_t st);
+cudaError_t launch_reinhard(float* pixels, uint32_t W, uint32_t H, unsigned* scratch, cudaStream_t st);
 
 }  // namespace pico

@@ -74,12 +74,12 @@ struct RenderBuffers {
     DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, sorg, sdir, scontrib, senergy, q0, q1, sq,
         counters, samples;
     DeviceBuffer pixels, variance, count, taken, done, pix_list;
-    DeviceBuffer gn, gp, gd, ga, gb, stats, out;
+    DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
     ~RenderBuffers()
     {
         for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &sorg, &sdir, &scontrib,
                                 &senergy, &q0, &q1, &sq, &counters, &samples, &pixels, &variance, &count, &taken,
-                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out})
+                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out, &tonemap})
             b->release();
     }
 };
@@ -140,7 +140,6 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (cfg->width != camera->resolution[0] || cfg->height != camera->resolution[1])
         return set_error(ctx, PICO_ERR_INVALID_ARG, "render size differs from the camera resolution");
-    if (cfg->tonemap) return set_error(ctx, PICO_ERR_UNSUPPORTED, "tone mapping is not implemented");
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
@@ -216,6 +215,12 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         e = cudaMemcpyAsync(r.pixels.ptr, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
         if (e != cudaSuccess) return cuda_error(ctx, e, "denoise copy");
     }
+    if (cfg->tonemap) {
+        // in place on the (denoised) buffer, which then replaces the caller's pixels (Scene.cpp:225-234)
+        e = r.tonemap.reserve(sizeof(unsigned));
+        if (e == cudaSuccess) e = launch_reinhard(as<float>(r.pixels), W, H, as<unsigned>(r.tonemap), st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "tone mapping");
+    }
     e = cudaMemcpyAsync(pixels, r.pixels.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(variance, r.variance.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sample_count, r.count.ptr, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -284,6 +289,35 @@ int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals
     e = cudaMemcpyAsync(out, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous download");
+    return PICO_OK;
+}
+
+int pico_gpu_tonemap_device(pico_gpu_ctx* ctx, float* d_pixels, uint32_t width, uint32_t height, void* stream)
+{
+    if (!ctx || !d_pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    RenderBuffers& r = *render_buffers(ctx);
+    cudaError_t e = r.tonemap.reserve(sizeof(unsigned));
+    if (e == cudaSuccess)
+        e = launch_reinhard(d_pixels, width, height, as<unsigned>(r.tonemap), static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "tone mapping");
+    return PICO_OK;
+}
+
+int pico_gpu_tonemap(pico_gpu_ctx* ctx, float* pixels, uint32_t width, uint32_t height)
+{
+    if (!ctx || !pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = ctx->stream;
+    RenderBuffers& r = *render_buffers(ctx);
+    const size_t n3 = (size_t)width * height * 3;
+    cudaError_t e = r.out.reserve(n3 * sizeof(float));
+    if (e == cudaSuccess) e = r.tonemap.reserve(sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.out.ptr, pixels, n3 * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = launch_reinhard(as<float>(r.out), width, height, as<unsigned>(r.tonemap), st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(pixels, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "tone mapping");
     return PICO_OK;
 }
 

@@ -100,61 +100,83 @@ enum TraversalOrder : int { kNearFirst = 0, kReferenceOrder = 1 };
 // missed; -inf = no box to test).
 struct StackEntry { uint32_t ref; float tmin; };
 
+// One ray's traversal as a resumable state machine: start() loads the ray,
+// step() advances by one unit of work (an inner node, a leaf, entering or
+// leaving an instance) and reports when the ray is finished, so a persistent
+// kernel can refill finished lanes while the others keep going.
 template <bool kCount, int kOrder>
-__device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
-                                             TraceCounters* cnt)
-{
-    using namespace ex;
-    const float kInf = __int_as_float(0x7f800000);
-    const float kNan = __int_as_float(0x7fffffff);
-    StackEntry stack[kTraceStack];
-    int sp = 0;
-
-    best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
-    const float wix = div(1.0f, d.x), wiy = div(1.0f, d.y), wiz = div(1.0f, d.z);
-
+struct Traversal {
+    // world ray
+    float ox, oy, oz, ow, dx, dy, dz;
+    float wix, wiy, wiz;
     // object-space ray of the instance being searched
-    float qox = 0, qoy = 0, qoz = 0, qdx = 0, qdy = 0, qdz = 0, qix = 0, qiy = 0, qiz = 0;
-    float lt = kInf, lu = 0.0f, lv = 0.0f;
-    uint32_t ltri = kNoHit, cur = 0;
-    bool in_blas = false;
+    float qox, qoy, qoz, qdx, qdy, qdz, qix, qiy, qiz;
+    float lt, lu, lv;     // closest triangle of the current instance (object-space t)
+    float gl;             // near-first only: object-space bound implied by the best world distance
+    float inv_len;        // 1 / |D|
+    float omag;           // 1e-4 (max |O_i| + 1): absolute slack of the instance bound
+    uint32_t ltri, cur, ref;
+    int sp;
+    bool in_blas;
+    TraceHit best;
 
-    // `visit` decides whether a box at slab distance t is entered against the current best.
-    auto visit = [&](float t, float limit) -> bool {
-        return kOrder == kReferenceOrder ? (t < limit) : (t <= limit && t < kInf);
-    };
-
-    uint32_t ref = PICO_REF_DONE;
+    __device__ __forceinline__ bool visit(float t, float limit) const
     {
-        bool h;
-        const float tm = slab(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2], sc.tlas_hi[2],
-                              o.x, o.y, o.z, wix, wiy, wiz, h);
-        if (h && tm < kInf) ref = sc.tlas_root_ref;
+        const float kInf = __int_as_float(0x7f800000);
+        return kOrder == kReferenceOrder ? (t < limit) : (t <= limit && t < kInf);
     }
 
-    for (uint32_t iter = 0;; ++iter) {
-        if (iter >= kTraceMaxIter) return kTraceIterLimit;
+    __device__ __forceinline__ void start(const SceneView& sc, const float4 o, const float4 d)
+    {
+        using namespace ex;
+        const float kInf = __int_as_float(0x7f800000);
+        ox = o.x; oy = o.y; oz = o.z; ow = o.w; dx = d.x; dy = d.y; dz = d.z;
+        wix = div(1.0f, d.x); wiy = div(1.0f, d.y); wiz = div(1.0f, d.z);
+        inv_len = kOrder == kNearFirst ? rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z) : 0.0f;
+        omag = 1e-4f * (fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) + 1.0f);
+        best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
+        lt = kInf; lu = lv = 0.0f; gl = kInf; ltri = kNoHit; cur = 0;
+        sp = 0;
+        in_blas = false;
+        bool h;
+        const float tm = slab(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2], sc.tlas_hi[2],
+                              ox, oy, oz, wix, wiy, wiz, h);
+        ref = (h && tm < kInf) ? sc.tlas_root_ref : PICO_REF_DONE;
+    }
+
+    __device__ __forceinline__ float limit() const
+    {
+        if (!in_blas) return best.t;
+        return kOrder == kNearFirst ? fminf(lt, gl) : lt;
+    }
+
+    // Returns kTraceOk while the ray continues, kTraceDone when finished, or an error.
+    // `stack` is the lane's traversal stack, kept outside the struct so the
+    // scalar state stays in registers.
+    __device__ __forceinline__ int step(const SceneView& sc, StackEntry* stack, TraceCounters* cnt)
+    {
+        using namespace ex;
+        const float kInf = __int_as_float(0x7f800000);
+        const float kNan = __int_as_float(0x7fffffff);
         if (ref == PICO_REF_DONE) {
-            // pop the next entry whose box still qualifies
-            bool found = false;
+            // pop the next entry whose box still qualifies against the current best
             while (sp > 0) {
                 const StackEntry e = stack[--sp];
-                if (e.tmin == -kInf || visit(e.tmin, in_blas ? lt : best.t)) {
+                if (e.tmin == -kInf || visit(e.tmin, e.ref == PICO_REF_END_BLAS ? kInf : limit())) {
                     ref = e.ref;
-                    found = true;
                     break;
                 }
             }
-            if (!found) break;
+            if (ref == PICO_REF_DONE) return kTraceDone;
         }
         if (!pico_is_leaf(ref)) {
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
             const uint4 n3 = __ldg(reinterpret_cast<const uint4*>(np) + 3);
             if (kCount) cnt->nodes++;
-            const float rx = in_blas ? qox : o.x, ry = in_blas ? qoy : o.y, rz = in_blas ? qoz : o.z;
+            const float rx = in_blas ? qox : ox, ry = in_blas ? qoy : oy, rz = in_blas ? qoz : oz;
             const float rix = in_blas ? qix : wix, riy = in_blas ? qiy : wiy, riz = in_blas ? qiz : wiz;
-            const float limit = in_blas ? lt : best.t;
+            const float lim = limit();
             bool h0, h1;
             float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
             float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
@@ -166,23 +188,19 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                     if (sp >= kTraceStack) return kTraceStackOverflow;
                     stack[sp++] = StackEntry{n3.y, t1};
                 }
-                ref = (n3.x != PICO_REF_EMPTY && visit(t0, limit)) ? n3.x : PICO_REF_DONE;
+                ref = (n3.x != PICO_REF_EMPTY && visit(t0, lim)) ? n3.x : PICO_REF_DONE;
             } else {
-                const bool v0 = visit(t0, limit), v1 = visit(t1, limit);
+                const bool v0 = visit(t0, lim), v1 = visit(t1, lim);
                 if (v0 && v1) {
                     const bool swap = t1 < t0;
                     if (sp >= kTraceStack) return kTraceStackOverflow;
                     stack[sp++] = swap ? StackEntry{n3.x, t0} : StackEntry{n3.y, t1};
                     ref = swap ? n3.y : n3.x;
-                } else if (v0) {
-                    ref = n3.x;
-                } else if (v1) {
-                    ref = n3.y;
                 } else {
-                    ref = PICO_REF_DONE;
+                    ref = v0 ? n3.x : (v1 ? n3.y : PICO_REF_DONE);
                 }
             }
-            continue;
+            return kTraceOk;
         }
         if (ref == PICO_REF_END_BLAS) {
             // leave the instance: its candidate is the closest triangle by object-space t
@@ -197,7 +215,7 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                 const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
                 const float wx = row4(f0, px, py, pz, 1.0f), wy = row4(f1, px, py, pz, 1.0f);
                 const float wz = row4(f2, px, py, pz, 1.0f), ww = row4(f3, px, py, pz, 1.0f);
-                const float ex_ = sub(wx, o.x), ey = sub(wy, o.y), ez = sub(wz, o.z), ew = sub(ww, o.w);
+                const float ex_ = sub(wx, ox), ey = sub(wy, oy), ez = sub(wz, oz), ew = sub(ww, ow);
                 const float tw = sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
                 const bool better = kOrder == kReferenceOrder ? tw < best.t
                                                               : (tw < best.t || (tw == best.t && cur < best.rank));
@@ -207,13 +225,11 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
             }
             in_blas = false;
             ref = PICO_REF_DONE;
-            continue;
+            return kTraceOk;
         }
         const uint32_t first = pico_leaf_first(ref), count = pico_leaf_count(ref);
-        if (count == 0) {
-            ref = PICO_REF_DONE;
-            continue;
-        }
+        ref = PICO_REF_DONE;
+        if (count == 0) return kTraceOk;
         if (in_blas) {
             for (uint32_t k = 0; k < count; ++k) {
                 const uint32_t tri = first + k;
@@ -226,8 +242,7 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                     }
                 }
             }
-            ref = PICO_REF_DONE;
-            continue;
+            return kTraceOk;
         }
         // TLAS leaf: search instance `first`; the rest of the leaf waits on the stack.
         if (count > 1) {
@@ -238,23 +253,48 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
         const float4* ip = reinterpret_cast<const float4*>(sc.insts + first);
         const float4 i0 = __ldg(ip), i1 = __ldg(ip + 1), i2 = __ldg(ip + 2);
         const float4 rl = __ldg(ip + 7), rh = __ldg(ip + 8);
-        qox = row4(i0, o.x, o.y, o.z, o.w); qoy = row4(i1, o.x, o.y, o.z, o.w); qoz = row4(i2, o.x, o.y, o.z, o.w);
-        qdx = row3(i0, d.x, d.y, d.z); qdy = row3(i1, d.x, d.y, d.z); qdz = row3(i2, d.x, d.y, d.z);
+        qox = row4(i0, ox, oy, oz, ow); qoy = row4(i1, ox, oy, oz, ow); qoz = row4(i2, ox, oy, oz, ow);
+        qdx = row3(i0, dx, dy, dz); qdy = row3(i1, dx, dy, dz); qdz = row3(i2, dx, dy, dz);
         qix = div(1.0f, qdx); qiy = div(1.0f, qdy); qiz = div(1.0f, qdz);
+        // A triangle of this instance at object-space t lies at world distance
+        // t * |D| up to float error (relative ~1e-6, absolute ~1e-7 |O|); the bound
+        // adds 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a
+        // triangle that could beat or tie the best world distance.
+        gl = kOrder == kNearFirst ? (best.t * 1.001f + omag) * inv_len : kInf;
         bool h;
         const float tm = slab(rl.x, rh.x, rl.y, rh.y, rl.z, rh.z, qox, qoy, qoz, qix, qiy, qiz, h);
-        if (!(h && tm < kInf)) {
-            ref = PICO_REF_DONE;
-            continue;
-        }
+        if (!(h && tm < kInf) || (kOrder == kNearFirst && !(tm <= gl))) return kTraceOk;
         if (sp >= kTraceStack) return kTraceStackOverflow;
         stack[sp++] = StackEntry{PICO_REF_END_BLAS, -kInf};
         in_blas = true;
         cur = first;
         lt = kInf; ltri = kNoHit;
         ref = __float_as_uint(rl.w);
+        return kTraceOk;
     }
-    return kTraceOk;
+};
+
+// Runs one ray to completion.
+template <bool kCount, int kOrder>
+__device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
+                                             TraceCounters* cnt)
+{
+    Traversal<kCount, kOrder> tr;
+    StackEntry stack[kTraceStack];
+    tr.start(sc, o, d);
+    for (uint32_t iter = 0; iter < kTraceMaxIter; ++iter) {
+        const int s = tr.step(sc, stack, cnt);
+        if (s == kTraceDone) {
+            best = tr.best;
+            return kTraceOk;
+        }
+        if (s != kTraceOk) {
+            best = tr.best;
+            return s;
+        }
+    }
+    best = tr.best;
+    return kTraceIterLimit;
 }
 
 }  // namespace pico

@@ -248,6 +248,7 @@ def atrous_fixtures(ref):
     args = [np.ascontiguousarray(a, np.float32) for a in (pixels, n, p, d)]
     ref.lib.ref_atrous(*[a.ctypes.data_as(fp) for a in args], W, H, res.ctypes.data_as(fp), 1)
     out["denoised"] = res.reshape(H, W, 3)
+    out["tonemapped"] = ref.reinhard(out["denoised"], W, H)   # Util::reinhard_tone_mapping
     np.savez_compressed(HERE / "atrous.npz", **out)
 
 

@@ -178,6 +178,12 @@ def test_denoiser_inputs_and_atrous_match_reference(oracle):
     assert_bits(out, z["denoised"], "a-trous output")
 
 
+def test_reinhard_matches_reference(oracle):
+    z = np.load(GOLDEN / "atrous.npz")
+    W, H = load_camera(z["cam"]).resolution
+    assert_bits(oracle.reinhard(z["denoised"], W, H), z["tonemapped"], "tone mapped")
+
+
 def test_accumulate_drops_first_sample(oracle):
     """Scene.cpp:185-191: mean += (x - mean) / prev_count, so the first sample is replaced."""
     s = np.array([[10, 10, 10], [1, 1, 1], [3, 3, 3]], np.float32)

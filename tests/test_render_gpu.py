@@ -100,6 +100,28 @@ def test_atrous_ragged_sizes(ctx, oracle, W, H):
     atrous_close(got, oracle.atrous(pix, nrm, pos, dif, W, H))
 
 
+def test_tonemap_matches_reference(ctx):
+    """Util::reinhard_tone_mapping: exact float operations, so bit-exact."""
+    z = np.load(GOLDEN / "atrous.npz")
+    W, H = load_camera(z["cam"]).resolution
+    got = ctx.tonemap(z["denoised"], W, H)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(z["tonemapped"]))
+    ok = ~np.isnan(got)
+    np.testing.assert_array_equal(got[ok].view(np.uint32), z["tonemapped"][ok].view(np.uint32))
+
+
+def test_render_denoise_and_tonemap_pipeline(ctx, oracle):
+    """render -> a-trous -> Reinhard, the post-processing order of Scene.cpp:212-234."""
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(64, 64)
+    gs = ctx.upload(scene)
+    raw, _, _ = gs.render(cam, 5, 8, seed=21)
+    final, _, _ = gs.render(cam, 5, 8, seed=21, denoise=True, tonemap=True)
+    n, p, d = gs.denoiser_inputs(cam)
+    want = oracle.reinhard(oracle.atrous(raw, n, p, d, 64, 64), 64, 64)
+    atrous_close(final, want)
+
+
 def test_atrous_device_path(ctx, oracle):
     torch = pytest.importorskip("torch")
     z = np.load(GOLDEN / "atrous.npz")
