@@ -69,7 +69,9 @@ def config_of(args, n_gpus):
                         f"({20 * 4 ** args.level} tris each), {args.rays} rays (50% primary 4096^2 pinhole, "
                         f"50% cosine bounce from surface points)",
             "instances": args.instances, "triangles_per_mesh": 20 * 4 ** args.level, "rays": args.rays,
-            "l2": "inputs larger than L2 (rays 512 MiB + hits 320 MiB per step)",
+            "l2": (f"inputs larger than L2 (rays {args.rays * 32 >> 20} MiB + hits {args.rays * 20 >> 20} MiB "
+                   f"per step)" if args.rays * 52 > 129 << 20 else
+                   f"inputs smaller than L2 (rays + hits {args.rays * 52 >> 20} MiB)"),
             "parallelism": f"replicas x{n_gpus}"}
 
 

@@ -19,6 +19,7 @@
  *   pico_gpu_denoiser_inputs   Scene::generate_denoiser_inputs (Core/Scene.cpp:248-294)
  *   pico_gpu_atrous            Util::atrous_denoise (Util/Denoisers.hpp:9)
  *   pico_gpu_tonemap           Util::reinhard_tone_mapping (Util/ToneMappers.hpp, ToneMappers.cpp:12-44)
+ *   pico_gpu_render_to_file    Scene::render_scene_to_file (Core/Scene.hpp:69, Core/Scene.cpp:238-246)
  *
  * Conventions: every function returns PICO_OK (0) or a negative PICO_ERR_*
  * code; host buffers are caller-owned and the call returns when they hold
@@ -171,6 +172,20 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
 /* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44) in place on W*H*3 floats. */
 int pico_gpu_tonemap(pico_gpu_ctx* ctx, float* pixels, uint32_t width, uint32_t height);
 int pico_gpu_tonemap_device(pico_gpu_ctx* ctx, float* d_pixels, uint32_t width, uint32_t height, void* stream);
+
+/* ---- image output --------------------------------------------------------
+ * Scene::render_scene_to_file (Core/Scene.hpp:69, Core/Scene.cpp:238-246):
+ * render, reverse the flat pixel array in the caller's buffer (a 180-degree
+ * rotation, as the reference does) and write a Radiance .hdr file with the same
+ * bytes stbi_write_hdr produces.  pico_gpu_encode_hdr is the writer alone
+ * (no reversal): it stores the file image in `out` (pico_gpu_hdr_bound bytes
+ * always suffice) and its size in *length. */
+int pico_gpu_render_to_file(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                            const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
+                            float* variance_rgb, const char* path);
+size_t pico_gpu_hdr_bound(uint32_t width, uint32_t height);
+int pico_gpu_encode_hdr(pico_gpu_ctx* ctx, const float* pixels, uint32_t width, uint32_t height,
+                        unsigned char* out, size_t capacity, size_t* length);
 
 /* ---- shading routines on caller inputs ---------------------------------------
  * BSRDF::pdf and BSRDF::sample (Render/BSRDF.hpp:50-52) and direct_lighting_pdf

@@ -14,6 +14,7 @@
 #ifndef PICO_ORACLE_H
 #define PICO_ORACLE_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -140,6 +141,11 @@ void po_atrous_denoise(const float* pixels, const float* normals, const float* p
                        const float* diffuse, uint32_t W, uint32_t H, float* out);
 /* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44), in place. */
 void po_reinhard(float* pixels, uint32_t W, uint32_t H);
+/* render_scene_to_file's output step (Core/Scene.cpp:238-246): std::reverse of
+ * the pixels, then stbi_write_hdr's Radiance RGBE file (returns its length). */
+void po_reverse_pixels(float* pixels, uint32_t n);
+void po_rgbe(const float* rgb, unsigned char* out);
+size_t po_encode_hdr(const float* pixels, uint32_t W, uint32_t H, unsigned char* out, size_t cap);
 
 #ifdef __cplusplus
 }

@@ -116,6 +116,8 @@ class Oracle(_SceneLib):
             "po_view_matrix": (None, [C.POINTER(CCamera), _fp]),
             "po_atrous_denoise": (None, [_fp, _fp, _fp, _fp, _u32, _u32, _fp]),
             "po_reinhard": (None, [_fp, _u32, _u32]),
+            "po_reverse_pixels": (None, [_fp, _u32]),
+            "po_encode_hdr": (C.c_size_t, [_fp, _u32, _u32, C.c_void_p, C.c_size_t]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -228,6 +230,15 @@ class Oracle(_SceneLib):
 
     def reinhard(self, pixels, W, H) -> np.ndarray:
         return _reinhard(self.lib.po_reinhard, pixels, W, H)
+
+    def hdr_file(self, pixels, W, H) -> bytes:
+        """render_scene_to_file's output: reversed pixels written as a Radiance .hdr."""
+        px = np.ascontiguousarray(pixels, np.float32).reshape(-1).copy()
+        self.lib.po_reverse_pixels(px.ctypes.data_as(_fp), W * H)
+        n = self.lib.po_encode_hdr(px.ctypes.data_as(_fp), W, H, None, 0)
+        out = (C.c_ubyte * n)()
+        self.lib.po_encode_hdr(px.ctypes.data_as(_fp), W, H, out, n)
+        return bytes(out)
 
     def atrous(self, pixels, normals, positions, diffuse, W, H) -> np.ndarray:
         out = np.empty(W * H * 3, np.float32)
@@ -365,6 +376,7 @@ class Reference(_SceneLib):
             "ref_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "ref_atrous": (C.c_double, [_fp, _fp, _fp, _fp, _u32, _u32, _fp, _i32]),
             "ref_reinhard": (None, [_fp, _u32, _u32]),
+            "ref_write_hdr": (_i32, [_fp, _u32, _u32, C.c_char_p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -376,6 +388,12 @@ class Reference(_SceneLib):
 
     def reinhard(self, pixels, W, H) -> np.ndarray:
         return _reinhard(self.lib.ref_reinhard, pixels, W, H)
+
+    def hdr_file(self, pixels, W, H, path) -> bytes:
+        px = np.ascontiguousarray(pixels, np.float32)
+        if not self.lib.ref_write_hdr(px.ctypes.data_as(_fp), W, H, str(path).encode()):
+            raise RuntimeError("stbi_write_hdr failed")
+        return Path(path).read_bytes()
 
 
 class ReferenceScene:

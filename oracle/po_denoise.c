@@ -16,6 +16,7 @@
 #include "po_internal.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -163,4 +164,107 @@ void po_reinhard(float* pixels, uint32_t W, uint32_t H)
         const float num = p * (1.0f + (p / w2));
         pixels[i] = num / (1.0f + p);
     }
+}
+
+/* ---------------------------------------------------------------------------
+ * Scene::render_scene_to_file's output step (Core/Scene.cpp:238-246): the flat
+ * pixel array reversed (std::reverse, a 180-degree rotation), then written by
+ * stb_image_write's stbi_write_hdr: the Radiance header, then per scanline the
+ * RGBE encoding (frexp of the largest component), run-length coded per
+ * component when 8 <= width < 32768 (runs of >= 3 equal bytes up to 127,
+ * literal dumps up to 128).  Components that are NaN or negative make the
+ * reference's float-to-byte conversion undefined; they are written as 0 here. */
+void po_reverse_pixels(float* pixels, uint32_t n)
+{
+    for (uint32_t i = 0, j = n ? n - 1 : 0; i < j; ++i, --j)
+        for (int c = 0; c < 3; ++c) {
+            const float t = pixels[3 * i + c];
+            pixels[3 * i + c] = pixels[3 * j + c];
+            pixels[3 * j + c] = t;
+        }
+}
+
+static unsigned char to_byte(float v) { return (v >= 0.0f && v < 256.0f) ? (unsigned char)v : 0; }
+
+void po_rgbe(const float* c, unsigned char* out)
+{
+    const float m12 = (c[1] < c[2]) ? c[2] : c[1];
+    const float maxcomp = (c[0] < m12) ? m12 : c[0];
+    if (maxcomp < 1e-32f) {
+        out[0] = out[1] = out[2] = out[3] = 0;
+        return;
+    }
+    int e;
+    const float normalize = (float)frexp(maxcomp, &e) * 256.0f / maxcomp;
+    out[0] = to_byte(c[0] * normalize);
+    out[1] = to_byte(c[1] * normalize);
+    out[2] = to_byte(c[2] * normalize);
+    out[3] = (unsigned char)(e + 128);
+}
+
+static size_t put(unsigned char* out, size_t at, size_t cap, const void* src, size_t n)
+{
+    if (out && at + n <= cap) memcpy(out + at, src, n);
+    return at + n;
+}
+
+/* Returns the byte length of the file; writes it into `out` when it fits `cap`. */
+size_t po_encode_hdr(const float* pixels, uint32_t W, uint32_t H, unsigned char* out, size_t cap)
+{
+    static const char header[] = "#?RADIANCE\n# Written by stb_image_write.h\nFORMAT=32-bit_rle_rgbe\n";
+    char buf[128];
+    size_t at = put(out, 0, cap, header, sizeof(header) - 1);
+    const int len = snprintf(buf, sizeof buf, "EXPOSURE=          1.0000000000000\n\n-Y %d +X %d\n", (int)H, (int)W);
+    at = put(out, at, cap, buf, (size_t)len);
+    unsigned char* scratch = (unsigned char*)malloc((size_t)W * 4 + 4);
+    for (uint32_t y = 0; y < H; ++y) {
+        const float* line = pixels + (size_t)3 * W * y;
+        if (W < 8 || W >= 32768) {
+            for (uint32_t x = 0; x < W; ++x) {
+                unsigned char rgbe[4];
+                po_rgbe(line + 3 * x, rgbe);
+                at = put(out, at, cap, rgbe, 4);
+            }
+            continue;
+        }
+        for (uint32_t x = 0; x < W; ++x) {
+            unsigned char rgbe[4];
+            po_rgbe(line + 3 * x, rgbe);
+            for (int c = 0; c < 4; ++c) scratch[x + (size_t)W * c] = rgbe[c];
+        }
+        const unsigned char sh[4] = {2, 2, (unsigned char)((W & 0xff00) >> 8), (unsigned char)(W & 0xff)};
+        at = put(out, at, cap, sh, 4);
+        for (int c = 0; c < 4; ++c) {
+            const unsigned char* comp = scratch + (size_t)W * c;
+            uint32_t x = 0;
+            while (x < W) {
+                uint32_t r = x;   /* first run of three equal bytes at or after x */
+                while (r + 2 < W) {
+                    if (comp[r] == comp[r + 1] && comp[r] == comp[r + 2]) break;
+                    ++r;
+                }
+                if (r + 2 >= W) r = W;
+                while (x < r) {   /* literals up to the run */
+                    uint32_t n = r - x;
+                    if (n > 128) n = 128;
+                    const unsigned char lb = (unsigned char)n;
+                    at = put(out, at, cap, &lb, 1);
+                    at = put(out, at, cap, comp + x, n);
+                    x += n;
+                }
+                if (r + 2 < W) {   /* the run itself */
+                    while (r < W && comp[r] == comp[x]) ++r;
+                    while (x < r) {
+                        uint32_t n = r - x;
+                        if (n > 127) n = 127;
+                        const unsigned char rb[2] = {(unsigned char)(n + 128), comp[x]};
+                        at = put(out, at, cap, rb, 2);
+                        x += n;
+                    }
+                }
+            }
+        }
+    }
+    free(scratch);
+    return at;
 }

@@ -36,6 +36,7 @@
 #include "Util/ToneMappers.hpp"
 
 #include "assimp/mesh.h"
+#include "stbi_image_write.h"
 #include "glm/ext.hpp"   // as Core/Scene.cpp:24 (brings gtx/scalar_multiplication)
 
 #include "../pico_oracle.h"
@@ -612,6 +613,16 @@ void ref_reinhard(float* pixels, uint32_t W, uint32_t H)
     Core::Rand::xorshift_random rng(99u);
     Util::Tiler tiler(pool, rng, glm::uvec2(W, H), glm::uvec2(64, 64));
     Util::reinhard_tone_mapping(reinterpret_cast<glm::vec3*>(pixels), glm::uvec2(W, H), tiler);
+}
+
+// The output step of Scene::render_scene_to_file (Core/Scene.cpp:238-246) on a
+// copy of the pixels: std::reverse, then stbi_write_hdr to `path`.
+int ref_write_hdr(const float* pixels, uint32_t W, uint32_t H, const char* path)
+{
+    std::vector<glm::vec3> px(reinterpret_cast<const glm::vec3*>(pixels),
+                              reinterpret_cast<const glm::vec3*>(pixels) + (size_t)W * H);
+    std::reverse(px.begin(), px.end());
+    return stbi_write_hdr(path, (int)W, (int)H, 3, reinterpret_cast<const float*>(px.data()));
 }
 
 } // extern "C"

@@ -51,6 +51,10 @@ SIGNATURES = {
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
     "pico_gpu_tonemap": (C.c_int, [_vp, _fp, _u32, _u32]),
     "pico_gpu_tonemap_device": (C.c_int, [_vp, _vp, _u32, _u32, _vp]),
+    "pico_gpu_render_to_file": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _fp,
+                                          C.POINTER(_u32), _fp, C.c_char_p]),
+    "pico_gpu_hdr_bound": (C.c_size_t, [_u32, _u32]),
+    "pico_gpu_encode_hdr": (C.c_int, [_vp, _fp, _u32, _u32, _vp, C.c_size_t, C.POINTER(C.c_size_t)]),
     "pico_gpu_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
@@ -130,6 +134,16 @@ class Context:
         out = np.ascontiguousarray(pixels, dtype=np.float32).copy()
         self.check(self.lib.pico_gpu_tonemap(self.handle, _f32(out), width, height), "tonemap")
         return out
+
+    def encode_hdr(self, pixels, width: int, height: int) -> bytes:
+        """stbi_write_hdr's file image of `pixels` (no reversal)."""
+        px = np.ascontiguousarray(pixels, dtype=np.float32)
+        cap = self.lib.pico_gpu_hdr_bound(width, height)
+        buf = (C.c_ubyte * cap)()
+        n = C.c_size_t(0)
+        self.check(self.lib.pico_gpu_encode_hdr(self.handle, _f32(px), width, height, buf, cap, C.byref(n)),
+                   "encode_hdr")
+        return bytes(buf[:n.value])
 
     def bsdf_eval(self, kinds, materials, V, N, H, xi):
         """Device BSRDF routines on given inputs: (pdf, L, P, energy, direct_pdf)."""
@@ -227,6 +241,20 @@ class GpuScene:
         self.ctx.check(self.lib.pico_gpu_render(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),
                                                 _f32(pixels), sample_count.ctypes.data_as(C.POINTER(C.c_uint32)),
                                                 _f32(variance), C.byref(quit_flag)), "render")
+        return pixels, sample_count, variance
+
+    def render_to_file(self, camera: Camera, max_depth: int, max_samples: int, path, seed: int = 1,
+                       pixels=None, sample_count=None, variance=None, denoise: bool = False, tonemap: bool = False):
+        """Scene::render_scene_to_file: renders, reverses `pixels` in place and writes a Radiance .hdr."""
+        W, H = int(camera.resolution[0]), int(camera.resolution[1])
+        pixels = np.zeros((H, W, 3), np.float32) if pixels is None else pixels
+        sample_count = np.zeros((H, W), np.uint32) if sample_count is None else sample_count
+        variance = np.zeros((H, W, 3), np.float32) if variance is None else variance
+        cfg = CRenderConfig(max_depth, max_samples, 0.0, H, W, int(tonemap), int(denoise), 0, seed)
+        cam = camera.to_c()
+        self.ctx.check(self.lib.pico_gpu_render_to_file(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),
+                                                        _f32(pixels), sample_count.ctypes.data_as(C.POINTER(C.c_uint32)),
+                                                        _f32(variance), str(path).encode()), "render_to_file")
         return pixels, sample_count, variance
 
     def denoiser_inputs(self, camera: Camera):

@@ -183,8 +183,10 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     v.light_alias_index = lai; v.light_positions = lpos;
     v.nlights = (uint32_t)fs.lights.size();
     v.tlas_root_ref = fs.tlas_root_ref;
+    v.tlas_fast_root_ref = fs.tlas_fast_root_ref;
     for (int a = 0; a < 3; ++a) {
         v.tlas_lo[a] = fs.tlas_lo[a]; v.tlas_hi[a] = fs.tlas_hi[a]; v.sky[a] = fs.sky[a];
+        v.tlas_fast_lo[a] = fs.tlas_fast_lo[a]; v.tlas_fast_hi[a] = fs.tlas_fast_hi[a];
     }
     v.ninstances = (uint32_t)fs.inst_shade.size();
     s->info[0] = fs.tlas_nodes; s->info[1] = fs.blas_nodes; s->info[2] = fs.tris.size();

@@ -64,9 +64,8 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
     }
 }
 
-// Closest hit for the paths in `q` (count in *count).  Persistent with the
-// same lane refill as the batch trace kernel: a warp tops up its finished
-// lanes from the queue whenever a quarter of them are idle.
+// Closest hit for the paths in `q` (count in *count): persistent, 32 queue
+// entries per warp fetch, each lane runs its ray to completion.
 __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b, uint32_t i, const TraceHit& h,
                                               int s, bool shadow)
 {
@@ -93,48 +92,25 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 }
 
 template <int kOrder>
-__global__ void __launch_bounds__(128) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
-                                                    const uint32_t* count, unsigned long long* work, int* err,
-                                                    bool shadow)
+__global__ void __launch_bounds__(128, 8) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
+                                                       const uint32_t* count, unsigned long long* work, int* err,
+                                                       bool shadow)
 {
-    constexpr unsigned kFull = 0xffffffffu;
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t n = *count;
-    Traversal<false, kOrder> tr;
-    StackEntry stack[kTraceStack];
-    uint32_t i = 0, steps = 0;
-    bool active = false, exhausted = false;
     for (;;) {
-        if (!exhausted) {
-            const unsigned idle = __ballot_sync(kFull, !active);
-            const int leader = __ffs(idle) - 1;
-            unsigned long long base = 0;
-            if (lane == (unsigned)leader) base = atomicAdd(work, (unsigned long long)__popc(idle));
-            base = __shfl_sync(kFull, base, leader);
-            if (base + __popc(idle) >= n) exhausted = true;
-            if (!active) {
-                const unsigned long long k = base + __popc(idle & ((1u << lane) - 1u));
-                if (k < n) {
-                    i = q[k];
-                    tr.start(sc, shadow ? b.sorg[i] : b.org[i], shadow ? b.sdir[i] : b.dir[i]);
-                    active = true;
-                    steps = 0;
-                }
-            }
-        }
-        if (!__any_sync(kFull, active)) break;
-        const int refill_at = exhausted ? 32 : 8;
-        for (;;) {
-            if (active) {
-                int s = tr.step(sc, stack, nullptr);
-                if (s == kTraceOk && ++steps >= kTraceMaxIter) s = kTraceIterLimit;
-                if (s != kTraceOk) {
-                    if (s != kTraceDone) atomicOr(err, s);
-                    extend_finish(sc, b, i, tr.best, s == kTraceDone ? kTraceOk : s, shadow);
-                    active = false;
-                }
-            }
-            if (__popc(__ballot_sync(kFull, !active)) >= refill_at) break;
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(work, 32ull);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        const unsigned long long k = base + lane;
+        if (k < n) {
+            const uint32_t i = q[k];
+            TraceHit h;
+            const int s = trace_closest<false, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
+                                                       shadow ? b.sdir[i] : b.dir[i], h, nullptr);
+            if (s != kTraceOk) atomicOr(err, s);
+            extend_finish(sc, b, i, h, s, shadow);
         }
     }
 }

@@ -106,8 +106,10 @@ struct SceneView {
     const uint32_t* light_alias_index;  // per light triangle (alias, local index)
     const float* light_positions;       // per light triangle: v0, v1, v2 (9 floats)
     uint32_t nlights;
-    uint32_t tlas_root_ref;
+    uint32_t tlas_root_ref;             // the reference's TLAS boxes
     float tlas_lo[3], tlas_hi[3];
+    uint32_t tlas_fast_root_ref;        // same topology, boxes refitted to the transformed vertices
+    float tlas_fast_lo[3], tlas_fast_hi[3];
     float sky[3];
     uint32_t ninstances;
 };

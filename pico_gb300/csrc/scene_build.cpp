@@ -450,6 +450,70 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
     };
     fs.tlas_root_ref = flatten(tlas, fs.nodes, place);
     fs.tlas_nodes = (uint32_t)(fs.nodes.size() - before);
+
+    // The same TLAS topology with boxes refitted to each instance's transformed
+    // vertices (for the near-first walk).  Computed in double and widened by
+    // 1e-5 of the scene's largest coordinate magnitude, far above the float error
+    // of a hit point seen from anywhere in the scene.  Falls back to the
+    // reference's box when transforming every vertex would be costly.
+    uint64_t work = 0;
+    for (uint32_t i = 0; i < desc.ninstances; ++i) work += desc.meshes[desc.instances[i].mesh].nverts;
+    std::vector<std::array<double, 6>> extent(desc.ninstances);
+    double mag = 1.0;
+    for (uint32_t i = 0; i < desc.ninstances; ++i) {
+        const pico_instance& in = desc.instances[i];
+        const pico_mesh& m = desc.meshes[in.mesh];
+        std::array<double, 6>& e = extent[i];
+        e = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+        if (work > 400000000ull || m.nverts == 0) continue;
+        const float* T = in.transform;
+        for (uint32_t v = 0; v < m.nverts; ++v) {
+            const double x = m.positions[3 * v], y = m.positions[3 * v + 1], z = m.positions[3 * v + 2];
+            for (int r = 0; r < 3; ++r) {
+                const double w = (double)T[0 * 4 + r] * x + (double)T[1 * 4 + r] * y + (double)T[2 * 4 + r] * z +
+                                 (double)T[3 * 4 + r];
+                e[r] = std::min(e[r], w);
+                e[3 + r] = std::max(e[3 + r], w);
+            }
+        }
+        for (int r = 0; r < 3; ++r) mag = std::max(mag, std::max(std::fabs(e[r]), std::fabs(e[3 + r])));
+    }
+    const double pad = 1e-5 * mag;
+    std::vector<Box> tight(desc.ninstances);
+    for (uint32_t i = 0; i < desc.ninstances; ++i) {
+        const std::array<double, 6>& e = extent[i];
+        if (!(e[0] <= e[3])) {
+            tight[i] = items[i].box;
+            continue;
+        }
+        tight[i].lo = {(float)(e[0] - pad), (float)(e[1] - pad), (float)(e[2] - pad), 1.0f};
+        tight[i].hi = {(float)(e[3] + pad), (float)(e[4] + pad), (float)(e[5] + pad), 1.0f};
+    }
+    RefBvh refit = tlas;
+    for (RefNode& n : refit.nodes) {   // post-order: children before parents
+        n.box = Box{};
+        if (!n.values.empty()) {
+            for (uint32_t v : n.values) n.box.grow(tight[v]);
+        } else {
+            for (int c = 0; c < 2; ++c)
+                if (n.child[c] != kInvalid) n.box.grow(refit.nodes[n.child[c]].box);
+        }
+    }
+    uint32_t rank_cursor = 0;   // leaves come in the same depth-first order as above
+    auto replace = [&](const std::vector<uint32_t>& values) -> uint32_t {
+        const uint32_t first = rank_cursor;
+        rank_cursor += (uint32_t)values.size();
+        return first;
+    };
+    fs.tlas_fast_root_ref = flatten(refit, fs.nodes, replace);
+    if (refit.root != kInvalid) {
+        const Box& b = refit.nodes[refit.root].box;
+        fs.tlas_fast_lo[0] = b.lo.x; fs.tlas_fast_lo[1] = b.lo.y; fs.tlas_fast_lo[2] = b.lo.z;
+        fs.tlas_fast_hi[0] = b.hi.x; fs.tlas_fast_hi[1] = b.hi.y; fs.tlas_fast_hi[2] = b.hi.z;
+    } else {
+        const float nan = std::numeric_limits<float>::quiet_NaN();
+        for (int a = 0; a < 3; ++a) fs.tlas_fast_lo[a] = fs.tlas_fast_hi[a] = nan;
+    }
     if (tlas.root != kInvalid) {
         const Box& b = tlas.nodes[tlas.root].box;
         fs.tlas_lo[0] = b.lo.x; fs.tlas_lo[1] = b.lo.y; fs.tlas_lo[2] = b.lo.z;

@@ -25,6 +25,8 @@ struct FlatScene {
     std::vector<float> light_positions;
     uint32_t tlas_root_ref = PICO_REF_EMPTY;
     float tlas_lo[3] = {0, 0, 0}, tlas_hi[3] = {0, 0, 0};
+    uint32_t tlas_fast_root_ref = PICO_REF_EMPTY;   // refitted TLAS for the near-first walk
+    float tlas_fast_lo[3] = {0, 0, 0}, tlas_fast_hi[3] = {0, 0, 0};
     float sky[3] = {0, 0, 0};
     uint32_t tlas_nodes = 0, blas_nodes = 0;
 };

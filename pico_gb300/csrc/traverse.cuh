@@ -86,215 +86,296 @@ __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, 
     return false;
 }
 
-// Traversal orders.  kNearFirst enters the nearer child first and breaks
-// equal distances by rank; kReferenceOrder walks children 0 then 1 and keeps the
-// first of equal distances, re-testing a deferred child against the best
-// distance at the moment it is reached, exactly like the reference's recursion
-// (Core/BVH.cpp:27-63).  Both return the reference's answer except where the
-// reference's own float slab test rejects a box whose triangle lies a few ulp
-// nearer than the current best (triangles on box faces meeting at an edge):
-// there only the reference order reproduces its choice.
+// Traversal orders.  kNearFirst enters the nearer child first, breaks equal
+// distances by rank, walks a refitted TLAS whose boxes bound each instance's
+// transformed vertices (tighter than the reference's transformed mesh AABB,
+// still containing every point the instance can be hit at; rays with a zero
+// direction component walk the reference's TLAS instead), and bounds each
+// BLAS walk by the best world distance so far.  kReferenceOrder walks the
+// reference's own boxes, children 0 then 1, keeps the first of equal distances
+// and re-tests a deferred child against the best distance when it is reached,
+// exactly like the reference's recursion (Core/BVH.cpp:27-63).  Both return the
+// reference's answer except where the reference's own float slab test rejects a
+// box whose triangle lies a few ulp nearer than the current best (triangles on
+// box faces meeting at an edge): there only the reference order reproduces its
+// choice.
 enum TraversalOrder : int { kNearFirst = 0, kReferenceOrder = 1 };
 
-// A stack entry: a reference and the slab distance of its box (NaN = box
-// missed; -inf = no box to test).
-struct StackEntry { uint32_t ref; float tmin; };
+// Object-space ray of an instance (transform_ray, Core/AABB.cpp:43-52) and its BLAS root.
+struct ObjectRay {
+    float ox, oy, oz, dx, dy, dz, ix, iy, iz;
+    float4 root_lo, root_hi;   // root box xyz; .w carries the root reference / instance id
+};
 
-// One ray's traversal as a resumable state machine: start() loads the ray,
-// step() advances by one unit of work (an inner node, a leaf, entering or
-// leaving an instance) and reports when the ray is finished, so a persistent
-// kernel can refill finished lanes while the others keep going.
-template <bool kCount, int kOrder>
-struct Traversal {
-    // world ray
-    float ox, oy, oz, ow, dx, dy, dz;
-    float wix, wiy, wiz;
-    // object-space ray of the instance being searched
-    float qox, qoy, qoz, qdx, qdy, qdz, qix, qiy, qiz;
-    float lt, lu, lv;     // closest triangle of the current instance (object-space t)
-    float gl;             // near-first only: object-space bound implied by the best world distance
-    float inv_len;        // 1 / |D|
-    float omag;           // 1e-4 (max |O_i| + 1): absolute slack of the instance bound
-    uint32_t ltri, cur, ref;
-    int sp;
-    bool in_blas;
-    TraceHit best;
+__device__ __forceinline__ ObjectRay to_object(const GpuInstance* inst, const float4 o, const float4 d)
+{
+    using namespace ex;
+    const float4* ip = reinterpret_cast<const float4*>(inst);
+    const float4 i0 = __ldg(ip), i1 = __ldg(ip + 1), i2 = __ldg(ip + 2);
+    ObjectRay r;
+    r.root_lo = __ldg(ip + 7);
+    r.root_hi = __ldg(ip + 8);
+    r.ox = row4(i0, o.x, o.y, o.z, o.w); r.oy = row4(i1, o.x, o.y, o.z, o.w); r.oz = row4(i2, o.x, o.y, o.z, o.w);
+    r.dx = row3(i0, d.x, d.y, d.z); r.dy = row3(i1, d.x, d.y, d.z); r.dz = row3(i2, d.x, d.y, d.z);
+    r.ix = div(1.0f, r.dx); r.iy = div(1.0f, r.dy); r.iz = div(1.0f, r.dz);
+    return r;
+}
 
-    __device__ __forceinline__ bool visit(float t, float limit) const
+// World distance of an instance's closest triangle: |T * interpolate(u, v) - O|
+// as a 4-vector (Core/LowerLevelMeshBVH.cpp:134-163, Core/UpperLevelBVH.cpp:70-73).
+__device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t rank, uint32_t tri, float u, float v,
+                                                const float4 o)
+{
+    using namespace ex;
+    const float4* tp = reinterpret_cast<const float4*>(sc.tris + tri);
+    const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+    const float w = sub(sub(1.0f, v), u);
+    const float px = add(add(mul(w, a.x), mul(u, b.x)), mul(v, c.x));
+    const float py = add(add(mul(w, a.y), mul(u, b.y)), mul(v, c.y));
+    const float pz = add(add(mul(w, a.z), mul(u, b.z)), mul(v, c.z));
+    const float4* ip = reinterpret_cast<const float4*>(sc.insts + rank);
+    const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
+    const float ex_ = sub(row4(f0, px, py, pz, 1.0f), o.x), ey = sub(row4(f1, px, py, pz, 1.0f), o.y);
+    const float ez = sub(row4(f2, px, py, pz, 1.0f), o.z), ew = sub(row4(f3, px, py, pz, 1.0f), o.w);
+    return sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
+}
+
+template <bool kCount>
+__device__ __forceinline__ int trace_near_first(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
+                                                TraceCounters* cnt)
+{
+    using namespace ex;
+    const float kInf = __int_as_float(0x7f800000);
+    uint32_t stack[kTraceStack];
+    int sp = 0;
+    best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
+    const float wix = div(1.0f, d.x), wiy = div(1.0f, d.y), wiz = div(1.0f, d.z);
+    // A triangle of an instance at object-space t lies at world distance t |D| up
+    // to float error (relative ~1e-6, absolute ~1e-7 |O|); the BLAS bound adds
+    // 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a triangle
+    // that could beat or tie the best world distance.
+    const float inv_len = rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+    const float omag = 1e-4f * (fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) + 1.0f);
+    ObjectRay q{};
+    float gl = kInf, lt = kInf, lu = 0.0f, lv = 0.0f;
+    uint32_t ltri = kNoHit, cur = 0;
+    bool in_blas = false;
+
+    // A ray with a zero direction component whose origin lies on a box plane gets
+    // a NaN slab distance there, and the reference skips that box.  Such rays walk
+    // the reference's own TLAS boxes so those decisions stay the reference's; every
+    // other ray walks the refitted TLAS (same topology, same leaf ranks), where no
+    // slab distance can be NaN.
+    uint32_t ref = PICO_REF_DONE;
     {
-        const float kInf = __int_as_float(0x7f800000);
-        return kOrder == kReferenceOrder ? (t < limit) : (t <= limit && t < kInf);
-    }
-
-    __device__ __forceinline__ void start(const SceneView& sc, const float4 o, const float4 d)
-    {
-        using namespace ex;
-        const float kInf = __int_as_float(0x7f800000);
-        ox = o.x; oy = o.y; oz = o.z; ow = o.w; dx = d.x; dy = d.y; dz = d.z;
-        wix = div(1.0f, d.x); wiy = div(1.0f, d.y); wiz = div(1.0f, d.z);
-        inv_len = kOrder == kNearFirst ? rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z) : 0.0f;
-        omag = 1e-4f * (fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) + 1.0f);
-        best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
-        lt = kInf; lu = lv = 0.0f; gl = kInf; ltri = kNoHit; cur = 0;
-        sp = 0;
-        in_blas = false;
-        bool h;
-        const float tm = slab(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2], sc.tlas_hi[2],
-                              ox, oy, oz, wix, wiy, wiz, h);
-        ref = (h && tm < kInf) ? sc.tlas_root_ref : PICO_REF_DONE;
-    }
-
-    __device__ __forceinline__ float limit() const
-    {
-        if (!in_blas) return best.t;
-        return kOrder == kNearFirst ? fminf(lt, gl) : lt;
-    }
-
-    // Returns kTraceOk while the ray continues, kTraceDone when finished, or an error.
-    // `stack` is the lane's traversal stack, kept outside the struct so the
-    // scalar state stays in registers.
-    __device__ __forceinline__ int step(const SceneView& sc, StackEntry* stack, TraceCounters* cnt)
-    {
-        using namespace ex;
-        const float kInf = __int_as_float(0x7f800000);
-        const float kNan = __int_as_float(0x7fffffff);
-        if (ref == PICO_REF_DONE) {
-            // pop the next entry whose box still qualifies against the current best
-            while (sp > 0) {
-                const StackEntry e = stack[--sp];
-                if (e.tmin == -kInf || visit(e.tmin, e.ref == PICO_REF_END_BLAS ? kInf : limit())) {
-                    ref = e.ref;
-                    break;
-                }
-            }
-            if (ref == PICO_REF_DONE) return kTraceDone;
+        const bool axis = d.x == 0.0f || d.y == 0.0f || d.z == 0.0f;
+        float lo[3], hi[3];   // selected by value: the scene view lives in kernel parameters
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = axis ? sc.tlas_lo[a] : sc.tlas_fast_lo[a];
+            hi[a] = axis ? sc.tlas_hi[a] : sc.tlas_fast_hi[a];
         }
+        bool h;
+        const float tm = slab(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], o.x, o.y, o.z, wix, wiy, wiz, h);
+        if (h && tm < kInf) ref = axis ? sc.tlas_root_ref : sc.tlas_fast_root_ref;
+    }
+    for (uint32_t iter = 0;; ++iter) {
+        if (iter >= kTraceMaxIter) return kTraceIterLimit;
+        if (ref == PICO_REF_DONE) break;
         if (!pico_is_leaf(ref)) {
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
             const uint4 n3 = __ldg(reinterpret_cast<const uint4*>(np) + 3);
             if (kCount) cnt->nodes++;
-            const float rx = in_blas ? qox : ox, ry = in_blas ? qoy : oy, rz = in_blas ? qoz : oz;
-            const float rix = in_blas ? qix : wix, riy = in_blas ? qiy : wiy, riz = in_blas ? qiz : wiz;
-            const float lim = limit();
+            const float rx = in_blas ? q.ox : o.x, ry = in_blas ? q.oy : o.y, rz = in_blas ? q.oz : o.z;
+            const float rix = in_blas ? q.ix : wix, riy = in_blas ? q.iy : wiy, riz = in_blas ? q.iz : wiz;
+            const float limit = in_blas ? fminf(lt, gl) : best.t;
             bool h0, h1;
-            float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-            float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
-            t0 = h0 ? t0 : kNan;
-            t1 = h1 ? t1 : kNan;
-            if (kOrder == kReferenceOrder) {
-                // child 1 waits on the stack and is tested when reached
-                if (n3.y != PICO_REF_EMPTY) {
-                    if (sp >= kTraceStack) return kTraceStackOverflow;
-                    stack[sp++] = StackEntry{n3.y, t1};
-                }
-                ref = (n3.x != PICO_REF_EMPTY && visit(t0, lim)) ? n3.x : PICO_REF_DONE;
+            const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
+            const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            const bool v0 = h0 && t0 <= limit && t0 < kInf;
+            const bool v1 = h1 && t1 <= limit && t1 < kInf;
+            if (v0 && v1) {
+                const bool swap = t1 < t0;
+                if (sp >= kTraceStack) return kTraceStackOverflow;
+                stack[sp++] = swap ? n3.x : n3.y;
+                ref = swap ? n3.y : n3.x;
+            } else if (v0) {
+                ref = n3.x;
+            } else if (v1) {
+                ref = n3.y;
             } else {
-                const bool v0 = visit(t0, lim), v1 = visit(t1, lim);
-                if (v0 && v1) {
-                    const bool swap = t1 < t0;
-                    if (sp >= kTraceStack) return kTraceStackOverflow;
-                    stack[sp++] = swap ? StackEntry{n3.x, t0} : StackEntry{n3.y, t1};
-                    ref = swap ? n3.y : n3.x;
-                } else {
-                    ref = v0 ? n3.x : (v1 ? n3.y : PICO_REF_DONE);
-                }
+                ref = sp ? stack[--sp] : PICO_REF_DONE;
             }
-            return kTraceOk;
+            continue;
         }
         if (ref == PICO_REF_END_BLAS) {
             // leave the instance: its candidate is the closest triangle by object-space t
             if (ltri != kNoHit) {
-                const float4* tp = reinterpret_cast<const float4*>(sc.tris + ltri);
-                const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-                const float w = sub(sub(1.0f, lv), lu);
-                const float px = add(add(mul(w, a.x), mul(lu, b.x)), mul(lv, c.x));
-                const float py = add(add(mul(w, a.y), mul(lu, b.y)), mul(lv, c.y));
-                const float pz = add(add(mul(w, a.z), mul(lu, b.z)), mul(lv, c.z));
-                const float4* ip = reinterpret_cast<const float4*>(sc.insts + cur);
-                const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
-                const float wx = row4(f0, px, py, pz, 1.0f), wy = row4(f1, px, py, pz, 1.0f);
-                const float wz = row4(f2, px, py, pz, 1.0f), ww = row4(f3, px, py, pz, 1.0f);
-                const float ex_ = sub(wx, ox), ey = sub(wy, oy), ez = sub(wz, oz), ew = sub(ww, ow);
-                const float tw = sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
-                const bool better = kOrder == kReferenceOrder ? tw < best.t
-                                                              : (tw < best.t || (tw == best.t && cur < best.rank));
-                if (better) {
+                const float tw = world_distance(sc, cur, ltri, lu, lv, o);
+                if (tw < best.t || (tw == best.t && cur < best.rank)) {
                     best.t = tw; best.rank = cur; best.tri = ltri; best.u = lu; best.v = lv;
                 }
             }
             in_blas = false;
-            ref = PICO_REF_DONE;
-            return kTraceOk;
+            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            continue;
         }
         const uint32_t first = pico_leaf_first(ref), count = pico_leaf_count(ref);
-        ref = PICO_REF_DONE;
-        if (count == 0) return kTraceOk;
+        if (count == 0) {
+            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            continue;
+        }
         if (in_blas) {
             for (uint32_t k = 0; k < count; ++k) {
                 const uint32_t tri = first + k;
                 float t, u, v;
                 if (kCount) cnt->tris++;
-                if (intersect_triangle(sc.tris + tri, qox, qoy, qoz, qdx, qdy, qdz, t, u, v)) {
-                    const bool better = kOrder == kReferenceOrder ? t < lt : (t < lt || (t == lt && tri < ltri));
-                    if (better) {
-                        lt = t; ltri = tri; lu = u; lv = v;
-                    }
+                if (intersect_triangle(sc.tris + tri, q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, t, u, v) &&
+                    (t < lt || (t == lt && tri < ltri))) {
+                    lt = t; ltri = tri; lu = u; lv = v;
                 }
             }
-            return kTraceOk;
+            ref = stack[--sp];   // the END_BLAS sentinel is below, so sp > 0 here
+            continue;
         }
         // TLAS leaf: search instance `first`; the rest of the leaf waits on the stack.
+        if (count > 1) {
+            if (sp >= kTraceStack) return kTraceStackOverflow;
+            stack[sp++] = pico_leaf_ref(first + 1, count - 1);
+        }
+        if (kCount) cnt->insts++;
+        q = to_object(sc.insts + first, o, d);
+        gl = (best.t * 1.001f + omag) * inv_len;
+        bool h;
+        const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
+                              q.oy, q.oz, q.ix, q.iy, q.iz, h);
+        if (!(h && tm < kInf && tm <= gl)) {
+            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            continue;
+        }
+        if (sp >= kTraceStack) return kTraceStackOverflow;
+        stack[sp++] = PICO_REF_END_BLAS;
+        in_blas = true;
+        cur = first;
+        lt = kInf; ltri = kNoHit;
+        ref = __float_as_uint(q.root_lo.w);
+    }
+    return kTraceOk;
+}
+
+// A deferred child of the reference-order walk and its slab distance (NaN: box
+// missed; -inf: nothing to test).
+struct StackEntry { uint32_t ref; float tmin; };
+
+template <bool kCount>
+__device__ __forceinline__ int trace_reference_order(const SceneView& sc, const float4 o, const float4 d,
+                                                     TraceHit& best, TraceCounters* cnt)
+{
+    using namespace ex;
+    const float kInf = __int_as_float(0x7f800000);
+    const float kNan = __int_as_float(0x7fffffff);
+    StackEntry stack[kTraceStack];
+    int sp = 0;
+    best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
+    const float wix = div(1.0f, d.x), wiy = div(1.0f, d.y), wiz = div(1.0f, d.z);
+    ObjectRay q{};
+    float lt = kInf, lu = 0.0f, lv = 0.0f;
+    uint32_t ltri = kNoHit, cur = 0;
+    bool in_blas = false;
+    // the next deferred entry whose box still passes against the best distance now
+    auto pop = [&]() -> uint32_t {
+        while (sp > 0) {
+            const StackEntry e = stack[--sp];
+            if (e.tmin == -kInf || e.tmin < (in_blas ? lt : best.t)) return e.ref;
+        }
+        return PICO_REF_DONE;
+    };
+
+    uint32_t ref = PICO_REF_DONE;
+    {
+        bool h;
+        const float tm = slab(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2], sc.tlas_hi[2],
+                              o.x, o.y, o.z, wix, wiy, wiz, h);
+        if (h && tm < kInf) ref = sc.tlas_root_ref;
+    }
+    for (uint32_t iter = 0;; ++iter) {
+        if (iter >= kTraceMaxIter) return kTraceIterLimit;
+        if (ref == PICO_REF_DONE) break;
+        if (!pico_is_leaf(ref)) {
+            const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
+            const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+            const uint4 n3 = __ldg(reinterpret_cast<const uint4*>(np) + 3);
+            if (kCount) cnt->nodes++;
+            const float rx = in_blas ? q.ox : o.x, ry = in_blas ? q.oy : o.y, rz = in_blas ? q.oz : o.z;
+            const float rix = in_blas ? q.ix : wix, riy = in_blas ? q.iy : wiy, riz = in_blas ? q.iz : wiz;
+            bool h0, h1;
+            const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
+            const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            // child 1 waits on the stack and is tested when reached
+            if (n3.y != PICO_REF_EMPTY) {
+                if (sp >= kTraceStack) return kTraceStackOverflow;
+                stack[sp++] = StackEntry{n3.y, h1 ? t1 : kNan};
+            }
+            ref = (n3.x != PICO_REF_EMPTY && h0 && t0 < (in_blas ? lt : best.t)) ? n3.x : pop();
+            continue;
+        }
+        if (ref == PICO_REF_END_BLAS) {
+            if (ltri != kNoHit) {
+                const float tw = world_distance(sc, cur, ltri, lu, lv, o);
+                if (tw < best.t) {
+                    best.t = tw; best.rank = cur; best.tri = ltri; best.u = lu; best.v = lv;
+                }
+            }
+            in_blas = false;
+            ref = pop();
+            continue;
+        }
+        const uint32_t first = pico_leaf_first(ref), count = pico_leaf_count(ref);
+        if (count == 0) {
+            ref = pop();
+            continue;
+        }
+        if (in_blas) {
+            for (uint32_t k = 0; k < count; ++k) {
+                const uint32_t tri = first + k;
+                float t, u, v;
+                if (kCount) cnt->tris++;
+                if (intersect_triangle(sc.tris + tri, q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, t, u, v) && t < lt) {
+                    lt = t; ltri = tri; lu = u; lv = v;
+                }
+            }
+            ref = pop();
+            continue;
+        }
         if (count > 1) {
             if (sp >= kTraceStack) return kTraceStackOverflow;
             stack[sp++] = StackEntry{pico_leaf_ref(first + 1, count - 1), -kInf};
         }
         if (kCount) cnt->insts++;
-        const float4* ip = reinterpret_cast<const float4*>(sc.insts + first);
-        const float4 i0 = __ldg(ip), i1 = __ldg(ip + 1), i2 = __ldg(ip + 2);
-        const float4 rl = __ldg(ip + 7), rh = __ldg(ip + 8);
-        qox = row4(i0, ox, oy, oz, ow); qoy = row4(i1, ox, oy, oz, ow); qoz = row4(i2, ox, oy, oz, ow);
-        qdx = row3(i0, dx, dy, dz); qdy = row3(i1, dx, dy, dz); qdz = row3(i2, dx, dy, dz);
-        qix = div(1.0f, qdx); qiy = div(1.0f, qdy); qiz = div(1.0f, qdz);
-        // A triangle of this instance at object-space t lies at world distance
-        // t * |D| up to float error (relative ~1e-6, absolute ~1e-7 |O|); the bound
-        // adds 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a
-        // triangle that could beat or tie the best world distance.
-        gl = kOrder == kNearFirst ? (best.t * 1.001f + omag) * inv_len : kInf;
+        q = to_object(sc.insts + first, o, d);
         bool h;
-        const float tm = slab(rl.x, rh.x, rl.y, rh.y, rl.z, rh.z, qox, qoy, qoz, qix, qiy, qiz, h);
-        if (!(h && tm < kInf) || (kOrder == kNearFirst && !(tm <= gl))) return kTraceOk;
+        const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
+                              q.oy, q.oz, q.ix, q.iy, q.iz, h);
+        if (!(h && tm < kInf)) {
+            ref = pop();
+            continue;
+        }
         if (sp >= kTraceStack) return kTraceStackOverflow;
         stack[sp++] = StackEntry{PICO_REF_END_BLAS, -kInf};
         in_blas = true;
         cur = first;
         lt = kInf; ltri = kNoHit;
-        ref = __float_as_uint(rl.w);
-        return kTraceOk;
+        ref = __float_as_uint(q.root_lo.w);
     }
-};
+    return kTraceOk;
+}
 
-// Runs one ray to completion.
 template <bool kCount, int kOrder>
 __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
                                              TraceCounters* cnt)
 {
-    Traversal<kCount, kOrder> tr;
-    StackEntry stack[kTraceStack];
-    tr.start(sc, o, d);
-    for (uint32_t iter = 0; iter < kTraceMaxIter; ++iter) {
-        const int s = tr.step(sc, stack, cnt);
-        if (s == kTraceDone) {
-            best = tr.best;
-            return kTraceOk;
-        }
-        if (s != kTraceOk) {
-            best = tr.best;
-            return s;
-        }
-    }
-    best = tr.best;
-    return kTraceIterLimit;
+    if (kOrder == kReferenceOrder) return trace_reference_order<kCount>(sc, o, d, best, cnt);
+    return trace_near_first<kCount>(sc, o, d, best, cnt);
 }
 
 }  // namespace pico

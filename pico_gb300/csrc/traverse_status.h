@@ -2,5 +2,5 @@
 #pragma once
 
 namespace pico {
-enum TraceStatus : int { kTraceOk = 0, kTraceStackOverflow = 1, kTraceIterLimit = 2, kTraceDone = 4 };
+enum TraceStatus : int { kTraceOk = 0, kTraceStackOverflow = 1, kTraceIterLimit = 2 };
 }  // namespace pico

@@ -250,6 +250,14 @@ def atrous_fixtures(ref):
     out["denoised"] = res.reshape(H, W, 3)
     out["tonemapped"] = ref.reinhard(out["denoised"], W, H)   # Util::reinhard_tone_mapping
     np.savez_compressed(HERE / "atrous.npz", **out)
+    # render_scene_to_file's output step: std::reverse + stbi_write_hdr, on the
+    # tone-mapped image and on a ragged 5 x 3 image (no run-length coding)
+    hdr = {"image": out["tonemapped"]}
+    small = np.random.default_rng(301).gamma(0.5, 2.0, (3, 5, 3)).astype(np.float32)
+    hdr["small"] = small
+    hdr["image_file"] = np.frombuffer(ref.hdr_file(out["tonemapped"], W, H, "/tmp/pico_golden.hdr"), np.uint8)
+    hdr["small_file"] = np.frombuffer(ref.hdr_file(small, 5, 3, "/tmp/pico_golden_small.hdr"), np.uint8)
+    np.savez_compressed(HERE / "hdr.npz", **hdr)
 
 
 def main():

@@ -184,6 +184,14 @@ def test_reinhard_matches_reference(oracle):
     assert_bits(oracle.reinhard(z["denoised"], W, H), z["tonemapped"], "tone mapped")
 
 
+def test_hdr_file_matches_reference(oracle):
+    """Reversal plus stbi_write_hdr, byte for byte (run-length coded and raw widths)."""
+    z = np.load(GOLDEN / "hdr.npz")
+    H, W = z["image"].shape[:2]
+    assert oracle.hdr_file(z["image"], W, H) == z["image_file"].tobytes()
+    assert oracle.hdr_file(z["small"], 5, 3) == z["small_file"].tobytes()
+
+
 def test_accumulate_drops_first_sample(oracle):
     """Scene.cpp:185-191: mean += (x - mean) / prev_count, so the first sample is replaced."""
     s = np.array([[10, 10, 10], [1, 1, 1], [3, 3, 3]], np.float32)

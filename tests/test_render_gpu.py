@@ -110,6 +110,28 @@ def test_tonemap_matches_reference(ctx):
     np.testing.assert_array_equal(got[ok].view(np.uint32), z["tonemapped"][ok].view(np.uint32))
 
 
+def test_hdr_encoding_byte_identical(ctx):
+    """The device RGBE + run-length encoder against stbi_write_hdr's bytes."""
+    z = np.load(GOLDEN / "hdr.npz")
+    H, W = z["image"].shape[:2]
+    flipped = z["image"].reshape(-1, 3)[::-1].copy()    # render_scene_to_file reverses first
+    assert ctx.encode_hdr(flipped, W, H) == z["image_file"].tobytes()
+    assert ctx.encode_hdr(z["small"].reshape(-1, 3)[::-1].copy(), 5, 3) == z["small_file"].tobytes()
+
+
+def test_render_to_file(ctx, oracle, tmp_path):
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(40, 24)
+    cam.aspect = 1.0
+    gs = ctx.upload(scene)
+    path = tmp_path / "out.hdr"
+    pix, cnt, var = gs.render_to_file(cam, 3, 4, path, seed=5)
+    # the caller's buffer is left reversed, as std::reverse leaves it in the reference
+    data = path.read_bytes()
+    assert data == oracle.hdr_file(pix.reshape(-1, 3)[::-1].copy(), 40, 24)
+    assert data.startswith(b"#?RADIANCE\n")
+
+
 def test_render_denoise_and_tonemap_pipeline(ctx, oracle):
     """render -> a-trous -> Reinhard, the post-processing order of Scene.cpp:212-234."""
     scene = scenes.cornell_box()
