@@ -168,6 +168,20 @@ int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals
 int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float* d_normals,
                            const float* d_positions, const float* d_diffuse, uint32_t width,
                            uint32_t height, float* d_out, void* stream);
+/* No counterpart in the reference.  pico_gpu_atrous_device for callers that
+ * must not allocate device memory during their denoise step: a frame loop that
+ * overlaps streams (cudaFree, and often cudaMalloc, synchronises the whole
+ * device) or a process whose device memory belongs to another allocator.  On
+ * success it allocates nothing: its scratch is a fixed 48 MiB + 288 KiB device
+ * array per device, so images are limited to 2,097,152 pixels (1920 x 1080
+ * fits) and 65,535 rows; larger ones return PICO_ERR_INVALID_ARG with a
+ * message.  All calls on a device share that array: calls that overlap on the
+ * GPU race, so order them on one stream.  Nothing in it has to start at zero.
+ * The first call on a device looks up the array's address (set-up); make that
+ * first call before any stream capture. */
+int pico_gpu_atrous_device_noalloc(pico_gpu_ctx* ctx, const float* d_pixels, const float* d_normals,
+                                   const float* d_positions, const float* d_diffuse, uint32_t width,
+                                   uint32_t height, float* d_out, void* stream);
 
 /* Util::reinhard_tone_mapping (Util/ToneMappers.cpp:12-44) in place on W*H*3 floats. */
 int pico_gpu_tonemap(pico_gpu_ctx* ctx, float* pixels, uint32_t width, uint32_t height);

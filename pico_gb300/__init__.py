@@ -49,6 +49,7 @@ SIGNATURES = {
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
+    "pico_gpu_atrous_device_noalloc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
     "pico_gpu_tonemap": (C.c_int, [_vp, _fp, _u32, _u32]),
     "pico_gpu_tonemap_device": (C.c_int, [_vp, _vp, _u32, _u32, _vp]),
     "pico_gpu_render_to_file": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _fp,
@@ -168,6 +169,14 @@ class Context:
                       height: int, d_out: int, stream: int = 0):
         self.check(self.lib.pico_gpu_atrous_device(self.handle, d_pixels, d_normals, d_positions, d_diffuse,
                                                    width, height, d_out, stream or None), "atrous_device")
+
+    def atrous_device_noalloc(self, d_pixels: int, d_normals: int, d_positions: int, d_diffuse: int, width: int,
+                              height: int, d_out: int, stream: int = 0):
+        """atrous_device without device allocation: fixed scratch of at most 2,097,152 pixels, shared by
+        every call on the device (calls that overlap on the GPU race)."""
+        self.check(self.lib.pico_gpu_atrous_device_noalloc(self.handle, d_pixels, d_normals, d_positions, d_diffuse,
+                                                           width, height, d_out, stream or None),
+                   "atrous_device_noalloc")
 
 
 class GpuScene:
