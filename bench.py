@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1 << 22)
     ap.add_argument("--order", type=int, default=0, choices=[0, 1],
                     help="traversal order: 0 near-first (default), 1 the reference's child order")
+    ap.add_argument("--no-render", action="store_true", help="skip the 1080p render and a-trous measurements")
+    ap.add_argument("--render-spp", type=int, default=64)
+    ap.add_argument("--render-depth", type=int, default=8)
+    ap.add_argument("--render-cpu-pixels", type=int, default=8192)
     return ap.parse_args()
 
 
@@ -171,6 +175,109 @@ def dram_traffic_per_ray():
         for line in p.read_text().splitlines():
             parts = line.split()
             if len(parts) == 2 and parts[0] == "dram_bytes_per_ray":
+                return float(parts[1])
+    return None
+
+
+ATROUS_BYTES_PER_PIXEL_LEVEL = 60   # 4 x 12 B in (colour, normal, position, albedo) + 12 B out
+L2_FLUSH_BYTES = 512 << 20
+
+
+def bench_render(ctx, args, torch, local):
+    """1080p render of the lit field through pico_gpu_render (host buffers in and out, denoised):
+    wall time per render, samples added and rays traced (camera, bounce, shadow, G-buffer)."""
+    scene = scenes.lit_field()
+    cam = scenes.lit_field_camera(1920, 1080)
+    gs = ctx.upload(scene)
+    gs.render(cam, args.render_depth, 2, seed=99, denoise=True)          # warm-up
+    runs = []
+    with ClockSampler(local) as clocks:
+        for k in range(2):
+            t0 = time.perf_counter()
+            pix, cnt, var = gs.render(cam, args.render_depth, args.render_spp, seed=1 + k, denoise=True)
+            runs.append((time.perf_counter() - t0, ctx.render_stats()))
+    secs = float(np.mean([r[0] for r in runs]))
+    st = runs[-1][1]
+    rays = st["camera_paths"] + st["bounce_rays"] + st["shadow_rays"] + st["gbuffer_rays"]
+    out = {"workload": f"lit field (4096 level-4 icospheres, ground quad, 8 quad lights), 1920x1080, "
+                       f"{args.render_spp} spp, depth {args.render_depth}, a-trous denoise, reference estimator",
+           "Msamples_per_s": st["samples"] / secs / 1e6, "Mrays_per_s": rays / secs / 1e6,
+           "ms_per_render": secs * 1e3, "samples": st["samples"], "camera_paths": st["camera_paths"],
+           "rays": {k: st[k] for k in ("camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
+           "timing": "wall clock around pico_gpu_render, host buffers in and out",
+           "clocks": clocks.summary()}
+    if not args.no_cpu and args.render_cpu_pixels > 0:
+        out["cpu_baseline"] = cpu_render(scene, cam, args)
+    gs.free()
+    return out
+
+
+def cpu_render(scene, cam, args):
+    """The reference render loop on host cores over a seeded pixel subset (reference code, else the port)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import pico_oracle
+    W, H = cam.resolution
+    rng = np.random.default_rng(3)
+    idx = np.sort(rng.choice(W * H, size=min(args.render_cpu_pixels, W * H), replace=False)).astype(np.uint32)
+    seeds = rng.integers(1, 2**32 - 1, size=len(idx), dtype=np.uint64)
+    cores = os.cpu_count() or 1
+    try:
+        rs = pico_oracle.Reference().scene(scene)
+        _, cnt, _, secs = rs.render_pixels(cam, args.render_depth, args.render_spp, idx, seeds)
+        kind = "reference"
+    except (FileNotFoundError, OSError):
+        os_ = pico_oracle.Oracle().scene(scene)
+        t0 = time.perf_counter()
+        _, cnt, _ = os_.render_pixels(cam, args.render_depth, args.render_spp, idx, seeds)
+        secs = time.perf_counter() - t0
+        kind = "port"
+    samples = int(cnt.reshape(-1)[idx].sum())
+    return {"value": samples / secs / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind,
+            "sample": f"{len(idx)} seeded pixels of the 1920x1080 image, {args.render_spp} spp, "
+                      f"depth {args.render_depth}, no denoise"}
+
+
+def bench_atrous(ctx, args, torch, local):
+    """pico_gpu_atrous_device on 1920x1080 device buffers, L2 flushed before every call."""
+    W, H = 1920, 1080
+    rng = np.random.default_rng(5)
+    dev = f"cuda:{local}"
+    bufs = [torch.from_numpy(a).to(dev) for a in (
+        rng.gamma(1.0, 1.0, (H, W, 3)).astype(np.float32), rng.normal(size=(H, W, 3)).astype(np.float32),
+        (rng.normal(size=(H, W, 3)) * 3).astype(np.float32), rng.random((H, W, 3)).astype(np.float32))]
+    out = torch.empty_like(bufs[0])
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    ptrs = [b.data_ptr() for b in bufs]
+    for _ in range(3):
+        ctx.atrous_device(*ptrs, W, H, out.data_ptr(), stream.cuda_stream)
+    times = []
+    for _ in range(10):
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.atrous_device(*ptrs, W, H, out.data_ptr(), stream.cuda_stream)
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = float(np.mean(times))
+    algo = ATROUS_BYTES_PER_PIXEL_LEVEL * 5 * W * H
+    peak, src = measured_peaks()
+    return {"workload": "a-trous, 5 levels, 1920x1080, device buffers, L2 flushed before each call",
+            "ms_per_call": ms, "Mpixels_per_s": W * H / (ms / 1e3) / 1e6, "gpu_launches_per_call": 10,
+            "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (ms / 1e3) / 1e9 / peak, "peak_source": src,
+                         "algorithmic_bytes_per_call": algo,
+                         "traffic": atrous_traffic_per_call()}}
+
+
+def atrous_traffic_per_call():
+    """DRAM bytes of one 1080p a-trous call measured by ncu (profiles/atrous_1080p.md), if recorded."""
+    p = ROOT / "profiles" / "atrous_1080p.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == "dram_bytes_per_call":
                 return float(parts[1])
     return None
 
@@ -302,11 +409,17 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
+    render = atrous = None
+    if not args.no_render:
+        gs.free()
+        render = bench_render(ctx, args, torch, local)
+        atrous = bench_atrous(ctx, args, torch, local)
+
     line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clocks.summary(), "scene": info}
+            "clocks": clocks.summary(), "scene": info, "render_1080p": render, "atrous_1080p": atrous}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

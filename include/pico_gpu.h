@@ -158,6 +158,11 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
 int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
                     const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
                     float* variance_rgb, const volatile int32_t* should_quit);
+/* Work of the context's last pico_gpu_render call: [0] samples added to the
+ * image (the growth of sample_count), [1] camera paths traced (pixels past their
+ * early exit trace none), [2] bounce rays, [3] next-event shadow rays,
+ * [4] G-buffer primary rays (W*H when denoising, else 0). */
+int pico_gpu_render_stats(const pico_gpu_ctx* ctx, uint64_t* out5);
 
 /* ---- denoiser ------------------------------------------------------------ */
 int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,

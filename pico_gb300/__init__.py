@@ -46,6 +46,7 @@ SIGNATURES = {
     "pico_gpu_trace_stats": (C.c_int, [_vp, _vp, _vp, _u64, C.POINTER(_u64), _vp]),
     "pico_gpu_render": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _fp,
                                   C.POINTER(_u32), _fp, C.POINTER(_i32)]),
+    "pico_gpu_render_stats": (C.c_int, [_vp, C.POINTER(_u64)]),
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
@@ -120,6 +121,13 @@ class Context:
     def set_traversal_order(self, order: int):
         """0: near-first (default), 1: the reference's child order (exact in near-tie cases)."""
         self.check(self.lib.pico_gpu_set_traversal_order(self.handle, order), "set_traversal_order")
+
+    def render_stats(self) -> dict:
+        """Work of the last render: samples added, camera paths, bounce, shadow and G-buffer rays."""
+        out = (C.c_uint64 * 5)()
+        self.check(self.lib.pico_gpu_render_stats(self.handle, out), "render_stats")
+        keys = ["samples", "camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays"]
+        return dict(zip(keys, [int(x) for x in out]))
 
     def upload(self, scene: SceneData) -> "GpuScene":
         return GpuScene(self, scene)

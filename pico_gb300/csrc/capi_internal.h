@@ -36,6 +36,7 @@ struct pico_gpu_ctx {
     pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
     RenderBuffers* render = nullptr;            // wavefront path state and image buffers
     int order = PICO_ORDER_NEAR_FIRST;          // traversal order of every trace in this context
+    uint64_t render_stats[5] = {0, 0, 0, 0, 0}; // tallies of the last pico_gpu_render call
     pico::DeviceStatus* status2() { return status + 1; }
 };
 

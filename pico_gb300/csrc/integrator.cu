@@ -94,10 +94,11 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 template <int kOrder>
 __global__ void __launch_bounds__(128, 8) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                        const uint32_t* count, unsigned long long* work, int* err,
-                                                       bool shadow)
+                                                       bool shadow, unsigned long long* tally)
 {
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t n = *count;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(tally, (unsigned long long)n);
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(work, 32ull);
@@ -323,10 +324,10 @@ static unsigned extend_grid()
 
 template <int kOrder>
 static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
-                          DeviceStatus* status, bool shadow, cudaStream_t st)
+                          DeviceStatus* status, bool shadow, unsigned long long* tally, cudaStream_t st)
 {
     extend_kernel<kOrder><<<extend_grid<kOrder>(), 128, 0, st>>>(sc, b, q, count, &status->work,
-                                                                  &status->trace_error, shadow);
+                                                                  &status->trace_error, shadow, tally);
 }
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
@@ -341,10 +342,11 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     for (uint32_t depth = 0; depth <= max_depth; ++depth) {
         e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
+        unsigned long long* tally = &status->rays[depth == 0 ? 0 : 1];
         if (order == kReferenceOrder)
-            launch_extend<kReferenceOrder>(sc, b, b.queue[cur], &b.counters[cur], status, false, st);
+            launch_extend<kReferenceOrder>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
         else
-            launch_extend<kNearFirst>(sc, b, b.queue[cur], &b.counters[cur], status, false, st);
+            launch_extend<kNearFirst>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
@@ -354,9 +356,10 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
             e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
             if (e != cudaSuccess) return e;
             if (order == kReferenceOrder)
-                launch_extend<kReferenceOrder>(sc, b, b.shadow_queue, &b.counters[2], status, true, st);
+                launch_extend<kReferenceOrder>(sc, b, b.shadow_queue, &b.counters[2], status, true, &status->rays[2],
+                                               st);
             else
-                launch_extend<kNearFirst>(sc, b, b.shadow_queue, &b.counters[2], status, true, st);
+                launch_extend<kNearFirst>(sc, b, b.shadow_queue, &b.counters[2], status, true, &status->rays[2], st);
         }
         cur ^= 1;
     }

@@ -15,6 +15,7 @@ struct DeviceStatus {
     int pad[3];
     unsigned long long work;         // persistent-kernel work counter
     unsigned long long counters[4];  // nodes, triangles, instances, spare
+    unsigned long long rays[4];      // render tallies: camera, bounce, shadow rays traced; spare
 };
 
 int sm_count();

@@ -154,15 +154,19 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
 
     std::vector<uint32_t> active, done(npx, 0u);
     active.reserve(npx);
+    uint64_t samples_before = 0;
     for (size_t p = 0; p < npx; ++p) {
+        samples_before += sample_count[p];
         if (sample_count[p] >= cfg->max_samples) done[p] = 1;
         else active.push_back((uint32_t)p);
     }
+    for (uint64_t& v : ctx->render_stats) v = 0;
     e = cudaMemcpyAsync(r.pixels.ptr, pixels, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.variance.ptr, variance, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.count.ptr, sample_count, npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.done.ptr, done.data(), npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(r.taken.ptr, 0, npx * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->rays, 0, sizeof(ctx->status->rays), st);
     if (e == cudaSuccess && !active.empty())
         e = cudaMemcpyAsync(r.pix_list.ptr, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -224,11 +228,27 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
     e = cudaMemcpyAsync(pixels, r.pixels.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(variance, r.variance.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sample_count, r.count.ptr, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    unsigned long long rays[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rays, ctx->status->rays, sizeof(rays), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "render download");
+    uint64_t samples_after = 0;
+    for (size_t p = 0; p < npx; ++p) samples_after += sample_count[p];
+    ctx->render_stats[0] = samples_after - samples_before;
+    ctx->render_stats[1] = rays[0];
+    ctx->render_stats[2] = rays[1];
+    ctx->render_stats[3] = rays[2];
+    ctx->render_stats[4] = cfg->denoise ? npx : 0;
     status = take_device_status(ctx, st);
     if (status != PICO_OK) return status;
     return cancelled ? set_error(ctx, PICO_ERR_CANCELLED, "render cancelled") : PICO_OK;
+}
+
+int pico_gpu_render_stats(const pico_gpu_ctx* ctx, uint64_t* out5)
+{
+    if (!ctx || !out5) return PICO_ERR_INVALID_ARG;
+    for (int k = 0; k < 5; ++k) out5[k] = ctx->render_stats[k];
+    return PICO_OK;
 }
 
 int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,

@@ -9,6 +9,9 @@
   [-50, 50]^3, uniform scale log-uniform in [0.5, 4] and uniformly random
   rotations; 16,777,216 rays, half coherent primary rays of a 4096 x 4096
   pinhole, half cosine-distributed rays leaving random surface points.
+* Lit field (full renders): the instance field with metalness-roughness
+  materials, a ground quad and eight quad area lights, seen by a 1920 x 1080
+  camera.
 
 Transforms are built in float64 and stored as float32 in glm's column-major
 order (array row c is glm column c).  Everything is a pure function of the
@@ -18,7 +21,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .types import DIFFUSE, LIGHT, RAY_DTYPE, Camera, Instance, Material, Mesh, SceneData
+from .types import DIELECTRIC, DIFFUSE, LIGHT, RAY_DTYPE, Camera, Instance, Material, Mesh, SceneData
 
 
 # ----------------------------------------------------------------------------- matrices
@@ -177,6 +180,60 @@ def instance_field(n_instances: int = 4096, level: int = 4, seed: int = 12345, e
         m = translate(trans[i]) @ quat_matrix(quats[i]) @ scale(scales[i])
         s.instances.append(Instance(0, glm_storage(m), DIFFUSE, 0))
     return s
+
+
+def metalness_roughness(albedo, metalness: float, roughness: float) -> Material:
+    """Render::ConstantMetalnessRoughnessMaterial (Render/BasicMaterials.cpp:28-39) in float32:
+    diffuse = albedo * (1 - 0.04) * (1 - metalness), specular = lerp(0.04, albedo, metalness)."""
+    f = np.float32
+    a = np.asarray(albedo, f)
+    m = f(metalness)
+    diffuse = (a * (f(1.0) - f(0.04))) * (f(1.0) - m)
+    spec = f(0.04) * (f(1.0) - m) + a * m
+    return Material(diffuse=tuple(float(x) for x in diffuse), specular=tuple(float(x) for x in spec),
+                    roughness=float(f(roughness)))
+
+
+def lit_field(n_instances: int = 4096, level: int = 4, seed: int = 12345, n_lights: int = 8,
+              extent: float = 50.0) -> SceneData:
+    """The instance field with a ground plane and quad area lights, for full renders.
+
+    Per instance: base colour U[0.1, 0.9]^3, metalness Bernoulli(0.3), roughness
+    U[0.05, 1], as a Dielectric BSRDF with the reference's metalness-roughness
+    material.  Ground: a 400 x 400 Lambert quad (albedo 0.5) below the field.
+    Lights: n_lights downward-facing quads of side U[4, 12] above the field,
+    radiance log-uniform in [1, 50].  Sky: black (the reference's default).
+    """
+    s = instance_field(n_instances=n_instances, level=level, seed=seed, extent=extent)
+    rng = np.random.default_rng(seed + 1)
+    s.materials = []
+    for i, inst in enumerate(s.instances):
+        albedo = rng.uniform(0.1, 0.9, 3)
+        metal = 1.0 if rng.random() < 0.3 else 0.0
+        rough = rng.uniform(0.05, 1.0)
+        s.materials.append(metalness_roughness(albedo, metal, rough))
+        inst.material = i
+        inst.bsdf = DIELECTRIC
+    y0 = -1.2 * extent
+    s.meshes.append(quad_mesh([[-4 * extent, y0, -4 * extent], [-4 * extent, y0, 4 * extent],
+                               [4 * extent, y0, 4 * extent], [4 * extent, y0, -4 * extent]], [0, 1, 0]))
+    s.materials.append(Material(diffuse=(0.5, 0.5, 0.5)))
+    s.instances.append(Instance(len(s.meshes) - 1, glm_storage(np.eye(4)), DIFFUSE, len(s.materials) - 1))
+    for _ in range(n_lights):
+        cx, cz = rng.uniform(-extent, extent, 2)
+        y = rng.uniform(1.1, 1.3) * extent
+        h = 0.5 * rng.uniform(4.0, 12.0)
+        le = float(np.exp(rng.uniform(np.log(1.0), np.log(50.0))))
+        s.meshes.append(quad_mesh([[cx - h, y, cz - h], [cx + h, y, cz - h], [cx + h, y, cz + h],
+                                   [cx - h, y, cz + h]], [0, -1, 0]))
+        s.materials.append(Material(diffuse=(0.8, 0.8, 0.8), emissive=(le, le, le)))
+        s.instances.append(Instance(len(s.meshes) - 1, glm_storage(np.eye(4)), LIGHT, len(s.materials) - 1))
+    return s
+
+
+def lit_field_camera(width: int = 1920, height: int = 1080) -> Camera:
+    return Camera(position=(0.0, 10.0, -140.0), direction=(0.0, -0.08, 1.0), resolution=(width, height),
+                  aspect=width / height)
 
 
 def field_camera(resolution: int = 4096) -> Camera:

@@ -259,3 +259,24 @@ def test_render_instance_field_runs(ctx):
     assert gs.info()["lights"] == 2
     pix, cnt, var = gs.render(cam, 5, 16, seed=2)
     assert np.isfinite(pix).all() and pix.mean() > 0.0
+
+
+def test_render_stats_count_the_work(ctx):
+    """pico_gpu_render_stats: samples added equal the growth of sample_count; rays are bounded by the paths."""
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(32, 24)
+    gs = ctx.upload(scene)
+    depth, spp = 5, 8
+    pix, cnt, var = gs.render(cam, depth, spp, seed=3)
+    st = ctx.render_stats()
+    assert st["samples"] == int(cnt.sum()) > 0
+    assert st["camera_paths"] >= st["samples"]
+    assert st["camera_paths"] <= 32 * 24 * spp
+    assert 0 < st["bounce_rays"] <= st["camera_paths"] * depth
+    assert 0 < st["shadow_rays"] <= st["camera_paths"] + st["bounce_rays"]
+    assert st["gbuffer_rays"] == 0
+    # a second call continues the progressive buffers: only the new samples are counted
+    gs.render(cam, depth, 2 * spp, seed=4, pixels=pix, sample_count=cnt, variance=var, denoise=True)
+    st2 = ctx.render_stats()
+    assert st2["samples"] == int(cnt.sum()) - st["samples"]
+    assert st2["gbuffer_rays"] == 32 * 24
