@@ -189,6 +189,22 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
         v.tlas_fast_lo[a] = fs.tlas_fast_lo[a]; v.tlas_fast_hi[a] = fs.tlas_fast_hi[a];
     }
     v.ninstances = (uint32_t)fs.inst_shade.size();
+    {
+        bool finite = true;
+        auto fin = [](float x) { return std::isfinite(x); };
+        for (const GpuNode& n : fs.nodes) {
+            if (n.ref0 != PICO_REF_EMPTY)
+                finite = finite && fin(n.c0lox) && fin(n.c0hix) && fin(n.c0loy) && fin(n.c0hiy) && fin(n.c0loz) &&
+                         fin(n.c0hiz);
+            if (n.ref1 != PICO_REF_EMPTY)
+                finite = finite && fin(n.c1lox) && fin(n.c1hix) && fin(n.c1loy) && fin(n.c1hiy) && fin(n.c1loz) &&
+                         fin(n.c1hiz);
+        }
+        for (int a = 0; a < 3; ++a)
+            finite = finite && fin(fs.tlas_lo[a]) && fin(fs.tlas_hi[a]) && fin(fs.tlas_fast_lo[a]) &&
+                     fin(fs.tlas_fast_hi[a]);
+        v.finite_boxes = finite ? 1u : 0u;
+    }
     s->info[0] = fs.tlas_nodes; s->info[1] = fs.blas_nodes; s->info[2] = fs.tris.size();
     s->info[3] = fs.insts.size(); s->info[4] = total; s->info[5] = fs.lights.size();
     *out = s;

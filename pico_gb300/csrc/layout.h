@@ -112,4 +112,5 @@ struct SceneView {
     float tlas_fast_lo[3], tlas_fast_hi[3];
     float sky[3];
     uint32_t ninstances;
+    uint32_t finite_boxes;              // every non-empty child box and both TLAS root boxes are finite
 };

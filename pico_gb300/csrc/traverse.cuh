@@ -58,6 +58,28 @@ __device__ __forceinline__ float slab(float lox, float hix, float loy, float hiy
     return tmin;
 }
 
+// The same slab distance and hit flag for data where no t can be NaN (finite
+// origin, inverse direction and box): the reference's select-based min / max
+// then equal the hardware ones (up to the sign of a zero, which compares equal),
+// and an empty child's all-NaN box still reports a miss.
+__device__ __forceinline__ float slab_fast(float lox, float hix, float loy, float hiy, float loz, float hiz, float ox,
+                                           float oy, float oz, float ix, float iy, float iz, bool& hit)
+{
+    using namespace ex;
+    const float t1 = mul(sub(lox, ox), ix), t2 = mul(sub(hix, ox), ix);
+    const float t3 = mul(sub(loy, oy), iy), t4 = mul(sub(hiy, oy), iy);
+    const float t5 = mul(sub(loz, oz), iz), t6 = mul(sub(hiz, oz), iz);
+    const float tmin = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+    const float tmax = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
+    hit = tmax >= 0.0f && tmin <= tmax;
+    return tmin;
+}
+
+__device__ __forceinline__ bool all_finite(float a, float b, float c, float d, float e, float f)
+{
+    return isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d) && isfinite(e) && isfinite(f);
+}
+
 // Mesh_Intersector::intersects without the interpolation (done once per instance).
 __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, float oy, float oz, float dx,
                                                    float dy, float dz, float& t_out, float& u_out, float& v_out)
@@ -160,6 +182,9 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
     float gl = kInf, lt = kInf, lu = 0.0f, lv = 0.0f;
     uint32_t ltri = kNoHit, cur = 0;
     bool in_blas = false;
+    // node tests take the NaN-free form when the ray (world or object space) and the boxes are finite
+    const bool wfast = sc.finite_boxes && all_finite(o.x, o.y, o.z, wix, wiy, wiz);
+    bool qfast = false;
 
     // A ray with a zero direction component whose origin lies on a box plane gets
     // a NaN slab distance there, and the reference skips that box.  Such rays walk
@@ -190,8 +215,14 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             const float rix = in_blas ? q.ix : wix, riy = in_blas ? q.iy : wiy, riz = in_blas ? q.iz : wiz;
             const float limit = in_blas ? fminf(lt, gl) : best.t;
             bool h0, h1;
-            const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-            const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            float t0, t1;
+            if (in_blas ? qfast : wfast) {
+                t0 = slab_fast(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
+                t1 = slab_fast(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            } else {
+                t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
+                t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            }
             const bool v0 = h0 && t0 <= limit && t0 < kInf;
             const bool v1 = h1 && t1 <= limit && t1 < kInf;
             if (v0 && v1) {
@@ -256,6 +287,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         if (sp >= kTraceStack) return kTraceStackOverflow;
         stack[sp++] = PICO_REF_END_BLAS;
         in_blas = true;
+        qfast = sc.finite_boxes && all_finite(q.ox, q.oy, q.oz, q.ix, q.iy, q.iz);
         cur = first;
         lt = kInf; ltri = kNoHit;
         ref = __float_as_uint(q.root_lo.w);
