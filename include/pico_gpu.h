@@ -81,11 +81,32 @@ typedef struct {
     float diffuse[3], specular[3], roughness, emissive[3];
 } pico_material;
 
+/* The sky and sun of Scene::process_globals (Core/Scene.cpp:639-700): the
+ * radiance of rays that leave the scene is ImageCube::sample4 of their
+ * direction (Core/Image.cpp:361-397, nearest texel; a 6-face cube of RGBA8
+ * images, or one RGBA float equirectangular image), and with use_sun the light
+ * pick of sample_direct_lighting includes a directional sun
+ * (Render/Integrators.cpp:54-76). */
+enum pico_sky_kind {
+    PICO_SKY_CONSTANT = 0,          /* pico_scene_desc::sky_rgb everywhere */
+    PICO_SKY_CUBE_RGBA8 = 1,        /* 6 faces of width*height RGBA bytes: +x, -x, +y, -y, +z, -z */
+    PICO_SKY_EQUIRECT_RGBAF = 2     /* width*height RGBA floats, row 0 at the top */
+};
+typedef struct {
+    uint32_t kind;
+    uint32_t width, height;         /* of one face for the cube */
+    const void* pixels;
+    int32_t use_sun;
+    float sun_direction[3];         /* the direction sunlight travels, normalised */
+    float sun_colour[3];
+} pico_sky;
+
 typedef struct {
     const pico_mesh* meshes; uint32_t nmeshes;
     const pico_instance* instances; uint32_t ninstances;
     const pico_material* materials; uint32_t nmaterials;
     float sky_rgb[3];               /* constant sky radiance (the black 1x1 sky of Scene.cpp:683-690) */
+    const pico_sky* sky;            /* NULL: the constant sky_rgb and no sun */
 } pico_scene_desc;
 
 /* Core::Ray's origin (vec4) and direction; dir[3] carries mLenght (the far distance). */

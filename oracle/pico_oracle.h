@@ -63,10 +63,25 @@ typedef struct {
 
 typedef struct po_scene po_scene;
 
+/* The sky of Scene::process_globals (Core/Scene.cpp:639-700) and its sun; the
+ * same layout as pico_sky of the product's header. */
+enum { PO_SKY_CONSTANT = 0, PO_SKY_CUBE_RGBA8 = 1, PO_SKY_EQUIRECT_RGBAF = 2 };
+typedef struct {
+    uint32_t kind, width, height;
+    const void* pixels;       /* CUBE_RGBA8: 6 faces of W*H RGBA bytes; EQUIRECT_RGBAF: W*H RGBA floats */
+    int32_t use_sun;
+    float sun_direction[3], sun_colour[3];
+} po_sky;
+
 po_scene* po_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes,
                           const po_instance_desc* instances, uint32_t ninstances,
                           const po_material* materials, uint32_t nmaterials);
 void po_scene_destroy(po_scene* s);
+/* Copies the sky into the scene (sky NULL or kind CONSTANT: the constant rgb, no
+ * sun unless sky says so).  A scene without this call has a black sky, no sun. */
+void po_scene_set_sky(po_scene* s, const po_sky* sky, const float* rgb);
+/* ImageCube::sample4 (Core/Image.cpp:361-397): RGBA of n directions (dirs n*3). */
+void po_sky_sample(const po_sky* sky, const float* dirs, uint32_t n, float* rgba);
 
 /* BVH introspection (node arrays in the reference's post-order). */
 uint32_t po_blas_node_count(const po_scene* s, uint32_t mesh);

@@ -18,7 +18,7 @@ from pathlib import Path
 
 import numpy as np
 
-from pico_gb300.types import HIT_DTYPE, RAY_DTYPE, CCamera, CMaterial, MarshalledScene, Material, SceneData
+from pico_gb300.types import HIT_DTYPE, RAY_DTYPE, CCamera, CMaterial, MarshalledScene, Material, SceneData, Sky
 
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "_build" / "libpico_oracle.so"
@@ -66,7 +66,17 @@ class _SceneLib:
         m = MarshalledScene(scene)
         h = getattr(self.lib, f"{self.prefix}scene_create")(m.meshes, len(scene.meshes), m.instances,
                                                             len(scene.instances), m.materials, len(scene.materials))
+        rgb = (C.c_float * 3)(*[float(x) for x in scene.sky])
+        getattr(self.lib, f"{self.prefix}scene_set_sky")(h, C.byref(m.sky) if m.sky is not None else None, rgb)
         return h, m
+
+    def sky_sample(self, sky: Sky, dirs) -> np.ndarray:
+        """ImageCube::sample4 (Core/Image.cpp:361-397): RGBA per direction."""
+        d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+        out = np.empty((len(d), 4), np.float32)
+        c = sky.to_c()
+        getattr(self.lib, f"{self.prefix}sky_sample")(C.byref(c), d.ctypes.data, len(d), out.ctypes.data)
+        return out
 
 
 class Oracle(_SceneLib):
@@ -81,6 +91,8 @@ class Oracle(_SceneLib):
         sig = {
             "po_scene_create": (_vp, [_vp, _u32, _vp, _u32, _vp, _u32]),
             "po_scene_destroy": (None, [_vp]),
+            "po_scene_set_sky": (None, [_vp, _vp, _vp]),
+            "po_sky_sample": (None, [_vp, _vp, _u32, _vp]),
             "po_blas_node_count": (_u32, [_vp, _u32]),
             "po_tlas_node_count": (_u32, [_vp]),
             "po_blas_nodes": (None, [_vp, _u32, _fp, _up, _up]),
@@ -344,6 +356,8 @@ class Reference(_SceneLib):
         sig = {
             "ref_scene_create": (_vp, [_vp, _u32, _vp, _u32, _vp, _u32]),
             "ref_scene_destroy": (None, [_vp]),
+            "ref_scene_set_sky": (None, [_vp, _vp, _vp]),
+            "ref_sky_sample": (None, [_vp, _vp, _u32, _vp]),
             "ref_trace": (None, [_vp, _vp, _u32, _vp]),
             "ref_trace_timed": (C.c_double, [_vp, _vp, _u32, _vp, _i32]),
             "ref_blas_node_count": (_u32, [_vp, _u32]),

@@ -339,6 +339,7 @@ void po_scene_destroy(po_scene* s)
         free(s->meshes[i].alias_index);
     }
     free(s->meshes);
+    free(s->sky_pixels);
     free(s->instances);
     free(s->tlas.nodes);
     free(s->tlas.values);

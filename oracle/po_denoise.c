@@ -61,7 +61,8 @@ void po_denoiser_inputs(const po_scene* s, const po_camera* cam, uint32_t W, uin
                 positions[3 * flat] = d.x * r.dir[3];
                 positions[3 * flat + 1] = d.y * r.dir[3];
                 positions[3 * flat + 2] = d.z * r.dir[3];
-                diffuse[3 * flat] = diffuse[3 * flat + 1] = diffuse[3 * flat + 2] = 0.0f;
+                const po_v4 sky = po_sky_lookup(s, d);   /* m_sky_box->sample4(ray.mDirection) */
+                diffuse[3 * flat] = sky.x; diffuse[3 * flat + 1] = sky.y; diffuse[3 * flat + 2] = sky.z;
             }
         }
     }

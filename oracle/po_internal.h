@@ -44,7 +44,13 @@ struct po_scene {
     po_bvh tlas;
     po_material* materials; uint32_t nmaterials;
     uint32_t* lights; uint32_t nlights;   /* instance indices, insertion order */
+    po_sky sky;                           /* pixels point into sky_pixels (owned) */
+    void* sky_pixels;
+    float sky_rgb[3];
 };
+
+/* ImageCube::sample4 of the scene's sky (Core/Image.cpp:361-397). */
+po_v4 po_sky_lookup(const po_scene* s, po_v3 d);
 
 float po_slab(const po_aabb* b, po_v4 o, po_v3 inv);
 void po_interpolate(const po_mesh_desc* m, uint32_t prim, float u, float v,

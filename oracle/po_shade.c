@@ -488,16 +488,31 @@ static const po_material* material_of(const po_scene* s, uint32_t inst)
     return &s->materials[s->instances[inst].material];
 }
 
-/* Monte_Carlo_Integrator::sample_direct_lighting (Integrators.cpp:46-128), no sun. */
+/* Monte_Carlo_Integrator::sample_direct_lighting (Integrators.cpp:46-128). */
 static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3* radiance, float* pdf)
 {
     const po_scene* s = it->s;
     const int type = (int)s->instances[f->inst].bsdf;
     if (type == PO_BTDF || type == PO_LIGHT) return 0;
     const po_material* mat = material_of(s, f->inst);
-    uint32_t light_count = s->nlights;
+    const int sun = s->sky.use_sun != 0;
+    uint32_t light_count = s->nlights + (sun ? 1u : 0u);
     const uint32_t light_index = (uint32_t)(po_mt64_uniform(it->mt) * (float)light_count);
     if (light_index == light_count) light_count--;
+    if (light_index >= light_count - 1 && sun) {
+        /* the sun: a shadow ray against the light's direction (Integrators.cpp:60-76) */
+        const po_v3 to_sun = v3(-s->sky.sun_direction[0], -s->sky.sun_direction[1], -s->sky.sun_direction[2]);
+        const po_v3 off = v3_scale(to_sun, 0.01f);
+        const po_v4 org = v4(f->position[0] + off.x, f->position[1] + off.y, f->position[2] + off.z,
+                             f->position[3] + 0.0f);
+        po_fragment hit;
+        if (!po_closest_hit(s, org, to_sun, &hit, NULL)) {
+            *pdf = direct_pdf(type, mat, v3(f->normal[0], f->normal[1], f->normal[2]), wi, to_sun);
+            *radiance = v3(s->sky.sun_colour[0], s->sky.sun_colour[1], s->sky.sun_colour[2]);
+            return 1;
+        }
+        return 0;
+    }
     const po_instance* light = &s->instances[s->lights[light_index]];
     const po_mesh* lm = &s->meshes[light->mesh];
 
@@ -537,7 +552,7 @@ static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3
 
 typedef struct { po_v3 payload, throughput; po_v4 org; po_v3 dir; } path_state;
 
-static po_v3 sky_colour(const po_scene* s, po_v3 d) { (void)s; (void)d; return v3(0.0f, 0.0f, 0.0f); }
+static po_v3 sky_colour(const po_scene* s, po_v3 d) { return v3_of4(po_sky_lookup(s, d)); }
 
 /* Monte_Carlo_Integrator::trace_ray (Integrators.cpp:157-209) as a loop. */
 static void trace_path(integrator* it, po_fragment frag, path_state* ray)

@@ -280,6 +280,56 @@ void* ref_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes, const po_in
 
 void ref_scene_destroy(void* p) { delete static_cast<RefScene*>(p); }
 
+}  // extern "C"
+
+// The ImageCube Scene::process_globals builds for a sky (Scene.cpp:639-690): six
+// RGBA8 faces, one RGBA float HDRI, or a 1x1 RGBA float image of a constant colour.
+static std::unique_ptr<Core::ImageCube> make_sky(const po_sky* sky, const float* rgb)
+{
+    if (sky && sky->kind == PO_SKY_CUBE_RGBA8) {
+        const size_t n = (size_t)6 * sky->width * sky->height * 4;
+        unsigned char* data = static_cast<unsigned char*>(malloc(n));
+        std::memcpy(data, sky->pixels, n);
+        return std::make_unique<Core::ImageCube>(data, Core::ImageExtent{sky->width, sky->height, 6},
+                                                 Core::Format::kRBGA_8UNorm);
+    }
+    if (sky && sky->kind == PO_SKY_EQUIRECT_RGBAF) {
+        const size_t n = (size_t)sky->width * sky->height * 4 * sizeof(float);
+        unsigned char* data = static_cast<unsigned char*>(malloc(n));
+        std::memcpy(data, sky->pixels, n);
+        return std::make_unique<Core::ImageCube>(data, Core::ImageExtent{sky->width, sky->height, 1},
+                                                 Core::Format::kRGBA_F);
+    }
+    float* data = static_cast<float*>(malloc(4 * sizeof(float)));
+    for (int c = 0; c < 3; ++c) data[c] = rgb ? rgb[c] : 0.0f;
+    data[3] = 0.0f;
+    return std::make_unique<Core::ImageCube>(reinterpret_cast<unsigned char*>(data), Core::ImageExtent{1, 1, 1},
+                                             Core::Format::kRGBA_F);
+}
+
+extern "C" {
+
+void ref_scene_set_sky(void* p, const po_sky* sky, const float* rgb)
+{
+    auto* s = static_cast<RefScene*>(p);
+    s->sky = make_sky(sky, rgb);
+    s->sun.m_sky_box = s->sky.get();
+    s->sun.m_use_sun = sky && sky->use_sun;
+    if (sky) {
+        s->sun.m_sun_direction = glm::vec3(sky->sun_direction[0], sky->sun_direction[1], sky->sun_direction[2]);
+        s->sun.m_sun_colour = glm::vec3(sky->sun_colour[0], sky->sun_colour[1], sky->sun_colour[2]);
+    }
+}
+
+void ref_sky_sample(const po_sky* sky, const float* dirs, uint32_t n, float* rgba)
+{
+    const std::unique_ptr<Core::ImageCube> cube = make_sky(sky, nullptr);
+    for (uint32_t i = 0; i < n; ++i) {
+        const glm::vec4 c = cube->sample4(glm::vec3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]));
+        rgba[4 * i] = c.x; rgba[4 * i + 1] = c.y; rgba[4 * i + 2] = c.z; rgba[4 * i + 3] = c.w;
+    }
+}
+
 void ref_trace(const void* p, const po_ray* rays, uint32_t n, po_fragment* out)
 {
     const auto* s = static_cast<const RefScene*>(p);

@@ -162,7 +162,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     cudaError_t e = cudaSuccess;
     const GpuNode* nodes; const GpuTri* tris; const GpuTriShade* tshade; const GpuInstance* insts;
     const GpuInstanceShade* ishade; const uint32_t* irank; const GpuMaterial* mats; const GpuLight* lights;
-    const float* law; const uint32_t* lai; const float* lpos;
+    const float* law; const uint32_t* lai; const float* lpos; const unsigned char* skypx;
     if (e == cudaSuccess) e = upload(fs.nodes, nodes);
     if (e == cudaSuccess) e = upload(fs.tris, tris);
     if (e == cudaSuccess) e = upload(fs.tri_shade, tshade);
@@ -174,6 +174,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     if (e == cudaSuccess) e = upload(fs.light_alias_weight, law);
     if (e == cudaSuccess) e = upload(fs.light_alias_index, lai);
     if (e == cudaSuccess) e = upload(fs.light_positions, lpos);
+    if (e == cudaSuccess) e = upload(fs.sky_pixels, skypx);
     if (e != cudaSuccess) {
         pico_gpu_scene_free(s);
         return cuda_error(ctx, e, "scene upload");
@@ -189,6 +190,9 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
         v.tlas_fast_lo[a] = fs.tlas_fast_lo[a]; v.tlas_fast_hi[a] = fs.tlas_fast_hi[a];
     }
     v.ninstances = (uint32_t)fs.inst_shade.size();
+    v.sky_kind = fs.sky_kind; v.sky_w = fs.sky_w; v.sky_h = fs.sky_h; v.sky_pixels = skypx;
+    v.use_sun = fs.use_sun;
+    for (int a = 0; a < 3; ++a) { v.sun_dir[a] = fs.sun_dir[a]; v.sun_col[a] = fs.sun_col[a]; }
     {
         bool finite = true;
         auto fin = [](float x) { return std::isfinite(x); };

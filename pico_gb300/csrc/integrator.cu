@@ -71,19 +71,23 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 {
     const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
     if (shadow) {
-        // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176)
-        if (rank != kNoHit) {
-            const uint32_t inst = sc.insts[rank].inst_id;
-            const GpuInstanceShade is = sc.inst_shade[inst];
-            if (is.bsdf == PICO_BSDF_LIGHT) {
-                const GpuMaterial& m = sc.materials[is.material];
-                const float4 c = b.scontrib[i], e = b.senergy[i];
-                float4 p = b.pay[i];
-                p.x = p.x + (c.x * m.emissive[0]) * e.x;
-                p.y = p.y + (c.y * m.emissive[1]) * e.y;
-                p.z = p.z + (c.z * m.emissive[2]) * e.z;
-                b.pay[i] = p;
-            }
+        // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176);
+        // a sun ray (senergy.w = 1) adds the sun colour when it escapes (Integrators.cpp:60-76)
+        const float4 e = b.senergy[i];
+        const float* le = nullptr;
+        if (e.w != 0.0f) {
+            if (rank == kNoHit && s == kTraceOk) le = sc.sun_col;
+        } else if (rank != kNoHit) {
+            const GpuInstanceShade is = sc.inst_shade[sc.insts[rank].inst_id];
+            if (is.bsdf == PICO_BSDF_LIGHT) le = sc.materials[is.material].emissive;
+        }
+        if (le) {
+            const float4 c = b.scontrib[i];
+            float4 p = b.pay[i];
+            p.x = p.x + (c.x * le[0]) * e.x;
+            p.y = p.y + (c.y * le[1]) * e.y;
+            p.z = p.z + (c.z * le[2]) * e.z;
+            b.pay[i] = p;
         }
     } else {
         b.hit[i] = make_float4(h.t, h.u, h.v, __uint_as_float(rank));
@@ -136,9 +140,10 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
             const float4 dir = b.dir[i];
             if (rank == kNoHit) {
                 // sky on a miss (Integrators.cpp:152, 208)
-                pay.x = pay.x + thr.x * sc.sky[0];
-                pay.y = pay.y + thr.y * sc.sky[1];
-                pay.z = pay.z + thr.z * sc.sky[2];
+                const float3 sk = sky_radiance(sc, dir.x, dir.y, dir.z);
+                pay.x = ex::add(pay.x, ex::mul(thr.x, sk.x));
+                pay.y = ex::add(pay.y, ex::mul(thr.y, sk.y));
+                pay.z = ex::add(pay.z, ex::mul(thr.z, sk.z));
                 b.pay[i] = pay;
             } else if (depth < max_depth) {
                 Pcg32 rng{b.rng[i]};
@@ -153,10 +158,24 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
                     pay.y = pay.y + thr.y * smp.energy.y;
                     pay.z = pay.z + thr.z * smp.energy.z;
                 }
-                // next-event estimation towards one uniformly chosen light
-                if (is.bsdf != PICO_BSDF_LIGHT && sc.nlights > 0) {
-                    uint32_t li = (uint32_t)(rng.uniform() * (float)sc.nlights);
-                    if (li >= sc.nlights) li = sc.nlights - 1;
+                // next-event estimation towards one uniformly chosen light, the sun
+                // counting as the last one (Integrators.cpp:54-76)
+                const uint32_t nl = sc.nlights + (sc.use_sun ? 1u : 0u);
+                uint32_t li = nl;
+                if (is.bsdf != PICO_BSDF_LIGHT && nl > 0) {
+                    li = (uint32_t)(rng.uniform() * (float)nl);
+                    if (li >= nl) li = nl - 1;
+                }
+                if (sc.use_sun && li == nl - 1) {
+                    const ex::V3 ts = ex::v3(-sc.sun_dir[0], -sc.sun_dir[1], -sc.sun_dir[2]);
+                    const float pdf = direct_lighting_pdf(is.bsdf, m, f.n, V, ts);
+                    b.sorg[i] = make_float4(f.px + 0.01f * ts.x, f.py + 0.01f * ts.y, f.pz + 0.01f * ts.z,
+                                            f.pw + 0.0f);
+                    b.sdir[i] = make_float4(ts.x, ts.y, ts.z, 10000.0f);
+                    b.scontrib[i] = make_float4(thr.x * pdf, thr.y * pdf, thr.z * pdf, 0.0f);
+                    b.senergy[i] = make_float4(smp.energy.x, smp.energy.y, smp.energy.z, 1.0f);
+                    shadow = true;
+                } else if (li < sc.nlights) {
                     const GpuLight L = sc.lights[li];
                     const uint32_t bucket = rng.next() % L.ntris;
                     const float coin = (float)rng.next() / 4294967296.0f;
@@ -293,7 +312,8 @@ __global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView c
         } else {
             n[0] = -d.x; n[1] = -d.y; n[2] = -d.z;
             pos[0] = mul(d.x, d.w); pos[1] = mul(d.y, d.w); pos[2] = mul(d.z, d.w);
-            alb[0] = sc.sky[0]; alb[1] = sc.sky[1]; alb[2] = sc.sky[2];
+            const float3 sk = sky_radiance(sc, d.x, d.y, d.z);   // m_sky_box->sample4(ray.mDirection)
+            alb[0] = sk.x; alb[1] = sk.y; alb[2] = sk.z;
         }
         for (int c = 0; c < 3; ++c) {
             normals[3 * (size_t)p + c] = n[c];
@@ -337,7 +357,8 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed);
-    const bool trace_last = sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
+    const bool trace_last =
+        sc.sky_kind != PICO_SKY_CONSTANT || sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
     int cur = 0;
     for (uint32_t depth = 0; depth <= max_depth; ++depth) {
         e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);

@@ -113,4 +113,8 @@ struct SceneView {
     float sky[3];
     uint32_t ninstances;
     uint32_t finite_boxes;              // every non-empty child box and both TLAS root boxes are finite
+    uint32_t sky_kind, sky_w, sky_h;    // pico_sky_kind; texels per row / column (of a face)
+    const void* sky_pixels;             // uchar4 cube faces or float4 equirectangular texels
+    uint32_t use_sun;
+    float sun_dir[3], sun_col[3];
 };

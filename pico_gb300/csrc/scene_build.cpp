@@ -560,6 +560,27 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         fs.lights.push_back(l);
     }
     for (int a = 0; a < 3; ++a) fs.sky[a] = desc.sky_rgb[a];
+
+    // ---- sky image and sun (Scene::process_globals, Core/Scene.cpp:639-700) -----
+    if (const pico_sky* k = desc.sky) {
+        fs.sky_kind = k->kind;
+        if (k->kind == PICO_SKY_CUBE_RGBA8 || k->kind == PICO_SKY_EQUIRECT_RGBAF) {
+            if (!k->pixels || k->width == 0 || k->height == 0) return "sky image without pixels";
+            const size_t texels = (size_t)k->width * k->height * (k->kind == PICO_SKY_CUBE_RGBA8 ? 6 : 1);
+            const size_t bytes = texels * (k->kind == PICO_SKY_CUBE_RGBA8 ? 4 : 16);
+            const unsigned char* p = static_cast<const unsigned char*>(k->pixels);
+            fs.sky_pixels.assign(p, p + bytes);
+            fs.sky_w = k->width;
+            fs.sky_h = k->height;
+        } else if (k->kind != PICO_SKY_CONSTANT) {
+            return "unknown sky kind " + std::to_string(k->kind);
+        }
+        fs.use_sun = k->use_sun ? 1u : 0u;
+        for (int a = 0; a < 3; ++a) {
+            fs.sun_dir[a] = k->sun_direction[a];
+            fs.sun_col[a] = k->sun_colour[a];
+        }
+    }
     return std::string();
 }
 

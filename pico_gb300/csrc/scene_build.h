@@ -28,6 +28,9 @@ struct FlatScene {
     uint32_t tlas_fast_root_ref = PICO_REF_EMPTY;   // refitted TLAS for the near-first walk
     float tlas_fast_lo[3] = {0, 0, 0}, tlas_fast_hi[3] = {0, 0, 0};
     float sky[3] = {0, 0, 0};
+    uint32_t sky_kind = PICO_SKY_CONSTANT, sky_w = 0, sky_h = 0, use_sun = 0;
+    std::vector<unsigned char> sky_pixels;   // RGBA8 cube faces or RGBA float texels, as given
+    float sun_dir[3] = {0, -1, 0}, sun_col[3] = {1, 1, 1};
     uint32_t tlas_nodes = 0, blas_nodes = 0;
 };
 

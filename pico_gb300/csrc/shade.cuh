@@ -283,6 +283,62 @@ __device__ __forceinline__ float direct_lighting_pdf(uint32_t kind, const GpuMat
     return bsdf_pdf(kind, two, H, m.roughness, m.reflectance);
 }
 
+// ---------------------------------------------------------------- sky
+// ImageCube::sample4 (Core/Image.cpp:361-397) of the scene's sky, xyz: the
+// nearest texel of a 6-face RGBA8 cube (resolve_cubemap_UV, Image.cpp:428-455,
+// texels / 255) or of an RGBA float equirectangular image (Image.cpp:457-464:
+// (atan2(z, x), asin(y)) / (2 pi, pi) + 0.5 with v flipped); get_data_ptr
+// (Image.cpp:400-425) truncates uv * size and wraps it modulo the size.  The
+// constant kind returns sky_rgb.
+__device__ __forceinline__ uint32_t sky_texel(float uv, uint32_t n)
+{
+    return __float2uint_rz(ex::mul(uv, (float)n)) % n;
+}
+
+__device__ __forceinline__ float3 sky_radiance(const SceneView& sc, float vx, float vy, float vz)
+{
+    using namespace ex;
+    if (sc.sky_kind == PICO_SKY_CUBE_RGBA8) {
+        const float ax = vx >= 0.0f ? vx : -vx, ay = vy >= 0.0f ? vy : -vy, az = vz >= 0.0f ? vz : -vz;
+        uint32_t face;
+        float ma, u, w;
+        if (az >= ax && az >= ay) {
+            face = vz < 0.0f ? 5 : 4;
+            ma = div(0.5f, az);
+            u = vz < 0.0f ? -vx : vx;
+            w = -vy;
+        } else if (ay >= ax) {
+            face = vy < 0.0f ? 3 : 2;
+            ma = div(0.5f, ay);
+            u = vx;
+            w = vy < 0.0f ? -vz : vz;
+        } else {
+            face = vx < 0.0f ? 1 : 0;
+            ma = div(0.5f, ax);
+            u = vx < 0.0f ? vz : -vz;
+            w = -vy;
+        }
+        u = add(mul(u, ma), 0.5f);
+        w = add(mul(w, ma), 0.5f);
+        const uint32_t x = sky_texel(u, sc.sky_w), y = sky_texel(w, sc.sky_h);
+        const uchar4 p = __ldg(static_cast<const uchar4*>(sc.sky_pixels) +
+                               ((size_t)face * sc.sky_w * sc.sky_h + (size_t)y * sc.sky_w + x));
+        return make_float3(div((float)p.x, 255.0f), div((float)p.y, 255.0f), div((float)p.z, 255.0f));
+    }
+    if (sc.sky_kind == PICO_SKY_EQUIRECT_RGBAF) {
+        float u = (float)atan2((double)vz, (double)vx);
+        float w = (float)asin((double)vy);
+        u = mul(u, (float)(1.0 / (3.14159265358979323846 * 2.0f)));
+        w = mul(w, (float)(1.0 / 3.14159265358979323846));
+        u = add(u, 0.5f);
+        w = sub(1.0f, add(w, 0.5f));
+        const uint32_t x = sky_texel(u, sc.sky_w), y = sky_texel(w, sc.sky_h);
+        const float4 p = __ldg(static_cast<const float4*>(sc.sky_pixels) + ((size_t)y * sc.sky_w + x));
+        return make_float3(p.x, p.y, p.z);
+    }
+    return make_float3(sc.sky[0], sc.sky[1], sc.sky[2]);
+}
+
 // ---------------------------------------------------------------- hit fragments
 struct Fragment {
     float px, py, pz, pw;   // world position (vec4)

@@ -37,11 +37,21 @@ class CMaterial(C.Structure):
                 ("emissive", C.c_float * 3)]
 
 
+# Sky kinds (pico_sky_kind).
+SKY_CONSTANT, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF = 0, 1, 2
+
+
+class CSky(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pixels", C.c_void_p), ("use_sun", C.c_int32),
+                ("sun_direction", C.c_float * 3), ("sun_colour", C.c_float * 3)]
+
+
 class CSceneDesc(C.Structure):
     _fields_ = [("meshes", C.POINTER(CMesh)), ("nmeshes", C.c_uint32),
                 ("instances", C.POINTER(CInstance)), ("ninstances", C.c_uint32),
                 ("materials", C.POINTER(CMaterial)), ("nmaterials", C.c_uint32),
-                ("sky_rgb", C.c_float * 3)]
+                ("sky_rgb", C.c_float * 3), ("sky", C.POINTER(CSky))]
 
 
 class CCamera(C.Structure):
@@ -96,11 +106,46 @@ class Instance:
 
 
 @dataclass
+class Sky:
+    """The scene's sky image and sun (Scene::process_globals, Core/Scene.cpp:639-700).
+
+    kind SKY_CUBE_RGBA8: pixels (6, H, W, 4) uint8, faces in the order of the
+    scene file's "Skybox" array (+x, -x, +y, -y, +z, -z); SKY_EQUIRECT_RGBAF:
+    pixels (H, W, 4) float32 (an HDRI); SKY_CONSTANT: no image (SceneData.sky).
+    """
+    kind: int = SKY_CONSTANT
+    pixels: np.ndarray | None = None
+    use_sun: bool = False
+    sun_direction: tuple = (0.0, -1.0, 0.0)
+    sun_colour: tuple = (1.0, 1.0, 1.0)
+
+    def __post_init__(self):
+        if self.kind == SKY_CUBE_RGBA8:
+            self.pixels = np.ascontiguousarray(self.pixels, dtype=np.uint8)
+            assert self.pixels.ndim == 4 and self.pixels.shape[0] == 6 and self.pixels.shape[3] == 4
+        elif self.kind == SKY_EQUIRECT_RGBAF:
+            self.pixels = np.ascontiguousarray(self.pixels, dtype=np.float32)
+            assert self.pixels.ndim == 3 and self.pixels.shape[2] == 4
+
+    def to_c(self) -> CSky:
+        c = CSky()
+        c.kind = self.kind
+        if self.pixels is not None:
+            c.height, c.width = self.pixels.shape[-3], self.pixels.shape[-2]
+            c.pixels = self.pixels.ctypes.data
+        c.use_sun = int(bool(self.use_sun))
+        c.sun_direction[:] = [float(x) for x in self.sun_direction]
+        c.sun_colour[:] = [float(x) for x in self.sun_colour]
+        return c
+
+
+@dataclass
 class SceneData:
     meshes: list = field(default_factory=list)
     instances: list = field(default_factory=list)
     materials: list = field(default_factory=list)
     sky: tuple = (0.0, 0.0, 0.0)
+    sky_image: Sky | None = None
 
 
 @dataclass
@@ -166,3 +211,8 @@ class MarshalledScene:
         self.desc.instances, self.desc.ninstances = self.instances, k
         self.desc.materials, self.desc.nmaterials = self.materials, q
         self.desc.sky_rgb[:] = [float(x) for x in scene.sky]
+        self.sky = None
+        if scene.sky_image is not None:
+            self.sky = scene.sky_image.to_c()
+            self.keep.append(scene.sky_image)
+            self.desc.sky = C.pointer(self.sky)

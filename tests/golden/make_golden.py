@@ -22,9 +22,9 @@ sys.path[:0] = [str(ROOT), str(ROOT / "oracle"), str(HERE)]
 
 import pico_oracle  # noqa: E402
 from pico_gb300 import scenes  # noqa: E402
-from pico_gb300.types import (DIELECTRIC, DIFFUSE, LIGHT, RAY_DTYPE, SPECULAR, Camera, CMaterial, Instance,  # noqa: E402
-                              Material)
-from scene_io import camera_array, scene_arrays  # noqa: E402
+from pico_gb300.types import (DIELECTRIC, DIFFUSE, LIGHT, RAY_DTYPE, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF,  # noqa: E402
+                              SPECULAR, Camera, CMaterial, Instance, Material, Sky)
+from scene_io import camera_array, scene_arrays, sky_arrays  # noqa: E402
 
 import ctypes as C  # noqa: E402
 
@@ -260,6 +260,56 @@ def atrous_fixtures(ref):
     np.savez_compressed(HERE / "hdr.npz", **hdr)
 
 
+def sky_dirs(rng, n):
+    """Random unit directions plus face diagonals, axes and signed zeros."""
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    e = np.array([[1, 1, 0], [1, 0, 1], [0, 1, 1], [1, 1, 1], [-1, 1, -1], [0, 0, 1], [1, 0, 0], [0, 1, 0],
+                  [0.5, -0.5, 0.5], [-0.0, 1, 0], [0, -0.0, 1], [3, 4, 0]], np.float32)
+    e /= np.linalg.norm(e, axis=1, keepdims=True)
+    return np.concatenate([d, e, -e]).astype(np.float32)
+
+
+def sky_scene(kind, seed):
+    rng = np.random.default_rng(seed)
+    if kind == SKY_CUBE_RGBA8:
+        px = rng.integers(0, 256, (6, 8, 8, 4), dtype=np.uint8)
+    else:
+        px = (rng.gamma(1.0, 2.0, (16, 32, 4))).astype(np.float32)
+    sun = np.array([0.3, -0.4, 0.9], np.float64)
+    sun = tuple((sun / np.linalg.norm(sun)).astype(np.float32))
+    return Sky(kind, px, True, sun, (4.0, 3.5, 3.0))
+
+
+def sky_fixtures(ref):
+    """ImageCube::sample4 on both sky kinds, and integrator samples / G-buffer of the
+    Cornell box under a cube sky and a sun (Integrators.cpp:54-76, 152, 208)."""
+    out = {}
+    rng = np.random.default_rng(501)
+    dirs = sky_dirs(rng, 4096)
+    out["dirs"] = dirs
+    for name, kind in (("cube", SKY_CUBE_RGBA8), ("equirect", SKY_EQUIRECT_RGBAF)):
+        sky = sky_scene(kind, 502 if kind == SKY_CUBE_RGBA8 else 503)
+        out.update(sky_arrays(sky, name))
+        out[f"{name}_rgba"] = ref.sky_sample(sky, dirs)
+    scene = scenes.cornell_box()
+    scene.sky_image = sky_scene(SKY_CUBE_RGBA8, 502)
+    cam = scenes.cornell_camera(64, 32)
+    cam.aspect = 2.0
+    out.update(scene_arrays(scene, "cornell"))
+    out["cam"] = camera_array(cam)
+    rs = ref.scene(scene)
+    px = np.array([[32, 16], [2, 16], [62, 30], [20, 8], [45, 25], [0, 0], [40, 16]], np.uint32)
+    seeds = np.array([3, 5, 77, 2024, 0xFFFFFFFE, 9, 31337], np.uint64)
+    samples = np.empty((len(px), 48, 3), np.float32)
+    for i in range(len(px)):
+        samples[i] = rs.integrate(cam, int(px[i, 0]), int(px[i, 1]), 5, int(seeds[i]), 48)
+    out["integ_px"], out["integ_seed"], out["integ_samples"] = px, seeds, samples
+    n, p, d = rs.denoiser_inputs(cam)
+    out["normals"], out["positions"], out["diffuse"] = n, p, d
+    np.savez_compressed(HERE / "sky.npz", **out)
+
+
 def main():
     pico_oracle.build_reference()
     ref = pico_oracle.Reference()
@@ -267,6 +317,7 @@ def main():
     sampling_fixtures(ref)
     integrator_fixtures(ref)
     atrous_fixtures(ref)
+    sky_fixtures(ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

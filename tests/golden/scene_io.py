@@ -3,7 +3,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from pico_gb300.types import Camera, Instance, Material, Mesh, SceneData
+from pico_gb300.types import Camera, Instance, Material, Mesh, SceneData, Sky
 
 
 def scene_arrays(scene: SceneData, prefix: str = "scene") -> dict:
@@ -18,7 +18,24 @@ def scene_arrays(scene: SceneData, prefix: str = "scene") -> dict:
     out[f"{prefix}_mats"] = np.array([[*m.diffuse, *m.specular, m.roughness, *m.emissive] for m in scene.materials],
                                      np.float32)
     out[f"{prefix}_sky"] = np.array(scene.sky, np.float32)
+    if scene.sky_image is not None:
+        out.update(sky_arrays(scene.sky_image, f"{prefix}_skyimg"))
     return out
+
+
+def sky_arrays(sky: Sky, prefix: str) -> dict:
+    out = {f"{prefix}_kind": np.array(sky.kind), f"{prefix}_sun": np.array(int(sky.use_sun)),
+           f"{prefix}_sun_dir": np.array(sky.sun_direction, np.float32),
+           f"{prefix}_sun_col": np.array(sky.sun_colour, np.float32)}
+    if sky.pixels is not None:
+        out[f"{prefix}_pixels"] = sky.pixels
+    return out
+
+
+def load_sky(z, prefix: str) -> Sky:
+    px = z[f"{prefix}_pixels"] if f"{prefix}_pixels" in z else None
+    return Sky(int(z[f"{prefix}_kind"]), px, bool(int(z[f"{prefix}_sun"])), tuple(z[f"{prefix}_sun_dir"]),
+               tuple(z[f"{prefix}_sun_col"]))
 
 
 def load_scene(z, prefix: str = "scene") -> SceneData:
@@ -26,7 +43,8 @@ def load_scene(z, prefix: str = "scene") -> SceneData:
     meshes = [Mesh(z[f"{prefix}_m{i}_pos"], z[f"{prefix}_m{i}_nrm"], z[f"{prefix}_m{i}_idx"]) for i in range(n)]
     insts = [Instance(int(a), x, int(b), int(c)) for (a, b, c), x in zip(z[f"{prefix}_inst_meta"], z[f"{prefix}_inst_xf"])]
     mats = [Material(tuple(r[0:3]), tuple(r[3:6]), float(r[6]), tuple(r[7:10])) for r in z[f"{prefix}_mats"]]
-    return SceneData(meshes, insts, mats, tuple(z[f"{prefix}_sky"]))
+    sky = load_sky(z, f"{prefix}_skyimg") if f"{prefix}_skyimg_kind" in z else None
+    return SceneData(meshes, insts, mats, tuple(z[f"{prefix}_sky"]), sky)
 
 
 def camera_array(cam: Camera) -> np.ndarray:

@@ -14,7 +14,7 @@ import pytest
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE / "golden"))
-from scene_io import load_camera, load_scene  # noqa: E402
+from scene_io import load_camera, load_scene, load_sky  # noqa: E402
 
 from pico_gb300.types import Material  # noqa: E402
 
@@ -190,6 +190,29 @@ def test_hdr_file_matches_reference(oracle):
     H, W = z["image"].shape[:2]
     assert oracle.hdr_file(z["image"], W, H) == z["image_file"].tobytes()
     assert oracle.hdr_file(z["small"], 5, 3) == z["small_file"].tobytes()
+
+
+def test_sky_lookup_matches_reference(oracle):
+    """ImageCube::sample4 on a 6-face RGBA8 cube and an RGBA float HDRI, including
+    face diagonals, axes and signed zeros."""
+    z = np.load(GOLDEN / "sky.npz")
+    for name in ("cube", "equirect"):
+        got = oracle.sky_sample(load_sky(z, name), z["dirs"])
+        assert_bits(got, z[f"{name}_rgba"], f"{name} sky")
+
+
+def test_integrator_with_sky_and_sun_matches_reference(oracle):
+    """integrate_ray with sky radiance on misses and the sun in the light pick."""
+    z = np.load(GOLDEN / "sky.npz")
+    scene, cam = load_scene(z, "cornell"), load_camera(z["cam"])
+    assert scene.sky_image is not None and scene.sky_image.use_sun
+    os_ = oracle.scene(scene)
+    for i, (px, py) in enumerate(z["integ_px"]):
+        got = os_.integrate(cam, int(px), int(py), 5, int(z["integ_seed"][i]), z["integ_samples"].shape[1])
+        assert_bits(got, z["integ_samples"][i], f"pixel {i} samples")
+    n, p, d = os_.denoiser_inputs(cam)
+    for got, key in ((n, "normals"), (p, "positions"), (d, "diffuse")):
+        assert_bits(got, z[key], f"G-buffer {key}")
 
 
 def test_accumulate_drops_first_sample(oracle):

@@ -26,7 +26,7 @@ from pico_gb300.types import Material
 
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE / "golden"))
-from scene_io import load_camera, load_scene  # noqa: E402
+from scene_io import load_camera, load_scene, load_sky  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 GOLDEN = HERE / "golden"
@@ -280,3 +280,59 @@ def test_render_stats_count_the_work(ctx):
     st2 = ctx.render_stats()
     assert st2["samples"] == int(cnt.sum()) - st["samples"]
     assert st2["gbuffer_rays"] == 32 * 24
+
+
+def test_denoiser_inputs_with_sky_bit_exact(ctx, oracle):
+    """Misses take the sky texel as albedo (Scene.cpp:283-288): the cube sky bit-exact,
+    the equirectangular one exact except where atan2 / asin land on a texel edge."""
+    z = np.load(GOLDEN / "sky.npz")
+    scene, cam = load_scene(z, "cornell"), load_camera(z["cam"])
+    gs = ctx.upload(scene)
+    try:
+        ctx.set_traversal_order(1)
+        n, p, d = gs.denoiser_inputs(cam)
+    finally:
+        ctx.set_traversal_order(0)
+    for got, key in ((n, "normals"), (p, "positions"), (d, "diffuse")):
+        np.testing.assert_array_equal(got.view(np.uint32), z[key].view(np.uint32), err_msg=key)
+    miss = (np.abs(p).max(-1) > 100)
+    assert miss.mean() > 0.2 and (d[miss] > 0).any()
+    # an HDRI sky seen by a wide camera
+    scene.sky_image = load_sky(z, "equirect")
+    wide = load_camera(z["cam"])
+    wide.position, wide.direction = (0.5, 0.5, -0.2), (0.3, 0.4, -1.0)
+    gs2 = ctx.upload(scene)
+    _, _, d2 = gs2.denoiser_inputs(wide)
+    _, _, w2 = oracle.scene(scene).denoiser_inputs(wide)
+    same = (d2.view(np.uint32) == w2.view(np.uint32)).all(-1)
+    assert same.mean() > 0.999, f"{(~same).sum()} albedo texels differ"
+
+
+def test_render_with_sky_and_sun_statistically_matches(ctx, oracle):
+    """Camera misses see the sky, escaping bounces add throughput * sky, and the sun
+    joins the light pick; per-pixel batch means agree with the oracle."""
+    z = np.load(GOLDEN / "sky.npz")
+    scene, cam = load_scene(z, "cornell"), load_camera(z["cam"])
+    W, H = cam.resolution
+    K, spp, depth = 16, 16, 5
+    gs = ctx.upload(scene)
+    os_ = oracle.scene(scene)
+    idx = np.arange(W * H, dtype=np.uint32)
+    rng = np.random.default_rng(78)
+
+    def gpu_batch(k):
+        pix, cnt, _ = gs.render(cam, depth, spp, seed=2000 + k, max_variance=-1.0)
+        return pix, cnt
+
+    def ref_batch(k):
+        pix, cnt, _ = os_.render_pixels(cam, depth, spp, idx, rng.integers(0, 2 ** 32, W * H, dtype=np.uint64),
+                                        max_variance=-1.0)
+        return pix, cnt
+
+    g_mean, g_se, _ = batch_means(gpu_batch, K)
+    r_mean, r_se, _ = batch_means(ref_batch, K)
+    z_ = np.abs(g_mean - r_mean) / np.maximum(np.sqrt(g_se ** 2 + r_se ** 2), 1e-6)
+    frac = (z_ <= 4.0).mean()
+    assert frac >= 0.995, f"only {frac:.4f} of pixel channels within 4 standard errors"
+    assert z_.mean() < 1.0, f"mean |z| {z_.mean():.3f}"
+    assert abs(g_mean.mean() - r_mean.mean()) < 0.01 * r_mean.mean()
