@@ -50,12 +50,19 @@ enum pico_status {
 
 /* BSRDF kinds, numbered like Render::BSRDF_Type (Render/BSRDF.hpp:32-39). */
 enum pico_bsdf {
-    PICO_BSDF_DIFFUSE = 0,
-    PICO_BSDF_SPECULAR = 1,
-    PICO_BSDF_DIELECTRIC = 2,
-    PICO_BSDF_BTDF = 3,             /* not supported on the GPU path */
-    PICO_BSDF_LIGHT = 4
+    PICO_BSDF_DIFFUSE = 0,          /* Diffuse_BRDF */
+    PICO_BSDF_SPECULAR = 1,         /* Specular_BRDF */
+    PICO_BSDF_DIELECTRIC = 2,       /* Dielectric_BRDF */
+    PICO_BSDF_BTDF = 3,             /* Transparent_BTDF (type kBTDF) */
+    PICO_BSDF_LIGHT = 4,            /* Light_BRDF */
+    PICO_BSDF_FRESNEL = 5,          /* Fresnel_BTDF (type kBTDF) */
+    PICO_BSDF_DELTA = 6             /* Specular_Delta_BRDF (type kSpecular_BRDF) */
 };
+
+/* Mesh shapes: triangles, or the implicit assets every reference scene holds
+ * (Core/Scene.cpp:49-57): "Sphere", LowerLevelSphereBVH(0.5), and "Cube",
+ * LowerLevelCube over [-0.5, 0.5]^3 (Core/LowerLevelImplicitShapesBVH.cpp). */
+enum pico_shape { PICO_SHAPE_TRIANGLES = 0, PICO_SHAPE_SPHERE = 1, PICO_SHAPE_CUBE = 2 };
 
 typedef struct pico_gpu_ctx pico_gpu_ctx;
 typedef struct pico_gpu_scene pico_gpu_scene;
@@ -68,6 +75,7 @@ typedef struct {
     const float* uvs;               /* nverts * 2, or NULL */
     const uint32_t* indices;        /* ntris * 3 */
     float aabb_min[3], aabb_max[3]; /* aiMesh::mAABB */
+    uint32_t shape;                 /* pico_shape; implicit shapes ignore the fields above */
 } pico_mesh;
 
 /* One UpperLevelBVH::Entry: mesh, object->world transform, BSRDF and material. */
@@ -79,6 +87,7 @@ typedef struct {
 /* Core::EvaluatedMaterial of a constant material (Core/MaterialManager.hpp:17-46). */
 typedef struct {
     float diffuse[3], specular[3], roughness, emissive[3];
+    float index_of_refraction;      /* of a ConstantTransparentMaterial (Render/BasicMaterials.hpp:41-66) */
 } pico_material;
 
 /* The sky and sun of Scene::process_globals (Core/Scene.cpp:639-700): the

@@ -21,8 +21,13 @@
 extern "C" {
 #endif
 
-/* BSRDF kinds, numbered like Render::BSRDF_Type (Render/BSRDF.hpp:32-39). */
-enum { PO_DIFFUSE = 0, PO_SPECULAR = 1, PO_DIELECTRIC = 2, PO_BTDF = 3, PO_LIGHT = 4 };
+/* BSRDF kinds: 0-4 numbered like Render::BSRDF_Type (Render/BSRDF.hpp:32-39), where
+ * kBTDF is Transparent_BTDF; 5 Fresnel_BTDF (also kBTDF), 6 Specular_Delta_BRDF
+ * (type kSpecular_BRDF). */
+enum { PO_DIFFUSE = 0, PO_SPECULAR = 1, PO_DIELECTRIC = 2, PO_BTDF = 3, PO_LIGHT = 4, PO_FRESNEL = 5, PO_DELTA = 6 };
+/* Mesh shapes: a triangle mesh, or the implicit "Sphere" (LowerLevelSphereBVH(0.5)) and
+ * "Cube" (LowerLevelCube) assets every scene starts with (Core/Scene.cpp:49-57). */
+enum { PO_SHAPE_TRIANGLES = 0, PO_SHAPE_SPHERE = 1, PO_SHAPE_CUBE = 2 };
 
 typedef struct {
     uint32_t nverts, ntris;
@@ -31,6 +36,7 @@ typedef struct {
     const float* uvs;         /* nverts * 2, or NULL (interpolates to 0) */
     const uint32_t* indices;  /* ntris * 3 */
     float aabb_min[3], aabb_max[3]; /* aiMesh::mAABB: min/max over the positions */
+    uint32_t shape;                 /* PO_SHAPE_*; the other fields are ignored for implicit shapes */
 } po_mesh_desc;
 
 typedef struct {
@@ -41,11 +47,14 @@ typedef struct {
 /* Core::EvaluatedMaterial for constant materials (Core/MaterialManager.hpp:17-46). */
 typedef struct {
     float diffuse[3], specular[3], roughness, emissive[3];
+    float index_of_refraction;      /* ConstantTransparentMaterial's IoR (Transparent / Fresnel lobes) */
 } po_material;
 
 /* Core::Ray (Core/AABB.hpp:24-42): origin is a vec4, dir[3] carries mLenght. */
 typedef struct { float org[4]; float dir[4]; } po_ray;
 
+/* A hit on an implicit shape reports prim = PO_IMPLICIT_PRIM and u = its object-space t. */
+#define PO_IMPLICIT_PRIM 0xfffffffeu
 typedef struct { uint32_t inst, prim; float t, u, v; } po_hit;
 
 /* Full closest-hit record: the reference's InterpolatedVertex plus IDs. */

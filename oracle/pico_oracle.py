@@ -52,6 +52,7 @@ def _mat(m: Material) -> CMaterial:
     c.specular[:] = list(m.specular)
     c.roughness = m.roughness
     c.emissive[:] = list(m.emissive)
+    c.index_of_refraction = m.ior
     return c
 
 

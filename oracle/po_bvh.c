@@ -284,6 +284,14 @@ po_scene* po_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes,
         const po_mesh_desc* d = &meshes[mi];
         po_mesh* m = &s->meshes[mi];
         m->desc = *d;
+        if (d->shape != PO_SHAPE_TRIANGLES) {
+            /* LowerLevelSphereBVH::get_bounds (radius 0.5) and LowerLevelCube's m_box are both
+             * [-0.5, 0.5]^3 with w = 1 (LowerLevelImplicitShapesBVH.cpp:54-57, 66-68) */
+            m->desc.ntris = 0;
+            m->aabb.mn = v4(-0.5f, -0.5f, -0.5f, 1.0f);
+            m->aabb.mx = v4(0.5f, 0.5f, 0.5f, 1.0f);
+            continue;
+        }
         po_bounded* items = (po_bounded*)malloc(sizeof(po_bounded) * (d->ntris ? d->ntris : 1));
         for (uint32_t t = 0; t < d->ntris; ++t) {            /* LowerLevelMeshBVH.cpp:48-64 */
             po_v3 mn = v3(INFINITY, INFINITY, INFINITY), mx = v3(-INFINITY, -INFINITY, -INFINITY);
@@ -468,6 +476,47 @@ typedef struct {
     float t; uint32_t inst, prim; float u, v; po_v4 pos; po_v3 nrm; po_v2 uv;
 } tlas_best;
 
+/* LowerLevelSphereBVH::calculate_intersection (radius 0.5, LowerLevelImplicitShapesBVH.cpp:24-52)
+ * and LowerLevelCube::calculate_intersection (:71-91): object-space hit position, normal and uv. */
+static int intersect_implicit(uint32_t shape, const tray* r, po_v4* P, po_v3* N, po_v2* uv, float* t_out)
+{
+    if (shape == PO_SHAPE_SPHERE) {
+        const float radius = 0.5f;
+        const po_v3 m = v3(r->org.x, r->org.y, r->org.z);
+        const float b = v3_dot(m, r->dir);
+        const float c = v3_dot(m, m) - radius * radius;
+        if (c > 0.0f && b > 0.0f) return 0;
+        const float discr = b * b - c;
+        if (discr < 0.0f) return 0;
+        float t = (float)(-(double)b - sqrt((double)discr));
+        if (t < 0.0f) t = 0.0f;
+        *P = v4(r->org.x + t * r->dir.x, r->org.y + t * r->dir.y, r->org.z + t * r->dir.z, r->org.w + t * 1.0f);
+        P->w = 1.0f;
+        *N = v3_normalize(v3(P->x, P->y, P->z));
+        uv->x = (float)(atan2((double)N->x, (double)N->z) / (2.0f * 3.14159265358979323846) + 0.5f);
+        uv->y = N->y * 0.5f + 0.5f;
+        *t_out = t;
+        return 1;
+    }
+    /* the cube: AABB::intersection_distance of [-0.5, 0.5]^3; the normal is the sign of the
+     * largest |component| of the hit point (maximum_component_index, AABB.cpp:31-41) */
+    po_aabb box;
+    box.mn = v4(-0.5f, -0.5f, -0.5f, 1.0f);
+    box.mx = v4(0.5f, 0.5f, 0.5f, 1.0f);
+    const float t = po_slab(&box, r->org, r->inv);
+    if (t == INFINITY) return 0;
+    *P = v4(r->org.x + r->dir.x * t, r->org.y + r->dir.y * t, r->org.z + r->dir.z * t, r->org.w + 1.0f);
+    P->w = 1.0f;
+    uv->x = 0.0f; uv->y = 0.0f;
+    const uint32_t k = max_component(v3(P->x, P->y, P->z));
+    const float pk = k == 0 ? P->x : (k == 1 ? P->y : P->z);
+    const float sgn = (float)((0.0f < pk) - (pk < 0.0f));
+    *N = v3(0.0f, 0.0f, 0.0f);
+    if (k == 0) N->x = 1.0f * sgn; else if (k == 1) N->y = 1.0f * sgn; else N->z = 1.0f * sgn;
+    *t_out = t;
+    return 1;
+}
+
 /* lower_level_intersector::intersects (UpperLevelBVH.cpp:59-80). */
 static int intersect_instance(const po_scene* s, uint32_t inst, const tray* wr, tlas_best* out,
                               visit_stats* st)
@@ -479,6 +528,15 @@ static int intersect_instance(const po_scene* s, uint32_t inst, const tray* wr, 
     r.dir = m4_mul_v3(&in->Tinv, wr->dir);
     r.inv = v3(1.0f / r.dir.x, 1.0f / r.dir.y, 1.0f / r.dir.z);
     if (st) st->insts++;
+    if (m->desc.shape != PO_SHAPE_TRIANGLES) {
+        po_v4 P; po_v3 N; po_v2 uv; float t;
+        if (!intersect_implicit(m->desc.shape, &r, &P, &N, &uv, &t)) return 0;
+        out->pos = m4_mul_v4(&in->T, P);
+        out->nrm = v3_normalize(m4_mul_v3(&in->T, N));
+        out->t = v4_length(v4_sub(out->pos, wr->org));
+        out->inst = inst; out->prim = PO_IMPLICIT_PRIM; out->u = t; out->v = 0.0f; out->uv = uv;
+        return 1;
+    }
     blas_best b = {INFINITY, PO_INVALID, 0, 0};
     if (m->bvh.nnodes) blas_walk(m, m->bvh.root, &r, &b, st);
     if (b.t == INFINITY) return 0;                              /* BVH.cpp:16-25 */

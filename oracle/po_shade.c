@@ -331,9 +331,98 @@ typedef struct { po_v3 L; float P; po_v3 energy; } bsdf_sample;
 /* next2() supplies successive Hammersley points; `ctx` is the generator. */
 typedef void (*next2_fn)(void* ctx, float* xi);
 
-static bsdf_sample sample_bsdf(int type, const po_material* mat, po_v3 V, po_v3 N,
-                               next2_fn next2, void* ctx)
+/* Core::Ray's index-of-refraction stack (AABB.cpp:54-81): camera rays start with 1.0
+ * (Camera.cpp:23).  Popping an empty stack or reading it empty is undefined in the
+ * reference; here the pop is ignored and the read gives 1.0. */
+#define PO_IOR_MAX 64
+typedef struct { float v[PO_IOR_MAX]; uint32_t n; } po_ior_stack;
+static void ior_push(po_ior_stack* s, float x) { if (s->n < PO_IOR_MAX) s->v[s->n] = x; s->n++; }
+static void ior_pop(po_ior_stack* s) { if (s->n) s->n--; }
+static float ior_top(const po_ior_stack* s)
 {
+    return s->n ? s->v[(s->n < PO_IOR_MAX ? s->n : PO_IOR_MAX) - 1] : 1.0f;
+}
+static int ior_inside(const po_ior_stack* s) { return s->n > 1; }
+
+/* glm::refract (glm/detail/func_geometric.inl:119-127): the product with (k >= 0) keeps a
+ * NaN from sqrt of a negative k, so total internal reflection gives a NaN vector. */
+static po_v3 refract3(po_v3 I, po_v3 N, float eta)
+{
+    const float d = v3_dot(N, I);
+    const float k = 1.0f - eta * eta * (1.0f - d * d);
+    const float s = eta * d + sqrtf(k);
+    const float g = (float)(k >= 0.0f);
+    return v3((eta * I.x - s * N.x) * g, (eta * I.y - s * N.y) * g, (eta * I.z - s * N.z) * g);
+}
+
+/* Transparent_BTDF::sample (BSRDF.cpp:238-297). */
+static bsdf_sample transparent_sample(const po_material* mat, po_v3 V, po_v3 N, po_ior_stack* ior,
+                                      next2_fn next2, void* ctx)
+{
+    const po_m3 w2t = tangent_frame(V, N);
+    const po_m3 t2w = m3_inverse(&w2t);
+    const po_v3 vt = v3_normalize(m3_mul_v3(&w2t, V));
+    const int enter = vt.z >= 0.0f;
+    float xi[2];
+    next2(ctx, xi);
+    const po_v3 H = beckmann_sample(xi, vt, mat->roughness);
+    const float eta = 1.0f / mat->index_of_refraction;
+    if (enter) ior_push(ior, mat->index_of_refraction); else ior_pop(ior);
+    const po_v3 L = refract3(vt, H, eta);
+    bsdf_sample s;
+    s.L = v3_normalize(m3_mul_v3(&t2w, L));
+    const float pdf = beckmann_pdf(H, mat->roughness);
+    const po_v3 wh = v3_normalize(v3_add(vt, v3_scale(L, eta)));
+    const float denom = v3_dot(vt, wh) + eta * v3_dot(L, wh);
+    const float dwh_dwi = fabsf((eta * eta * v3_dot(L, wh)) / (denom * denom));
+    s.P = pdf * dwh_dwi;
+    s.energy = v3(mat->diffuse[0], mat->diffuse[1], mat->diffuse[2]);
+    return s;
+}
+
+/* Fresnel_BTDF::fresnel_factor (BSRDF.cpp:395-421). */
+static float fresnel_factor(float cos_i, float eta_i, float eta_t)
+{
+    cos_i = clampf(cos_i, -1.0f, 1.0f);
+    if (!(cos_i > 0.0f)) {
+        const float tmp = eta_i; eta_i = eta_t; eta_t = tmp;
+        cos_i = fabsf(cos_i);
+    }
+    const float sin_i = sqrtf((0.0f < 1.0f - cos_i * cos_i) ? 1.0f - cos_i * cos_i : 0.0f);
+    const float sin_t = eta_i / eta_t * sin_i;
+    const float cos_t = sqrtf((0.0f < 1.0f - sin_t * sin_t) ? 1.0f - sin_t * sin_t : 0.0f);
+    const float rparl = ((eta_t * cos_i) - (eta_i * cos_t)) / ((eta_t * cos_i) + (eta_i * cos_t));
+    const float rperp = ((eta_i * cos_i) - (eta_t * cos_t)) / ((eta_i * cos_i) + (eta_t * cos_t));
+    return (rparl * rparl + rperp * rperp) / 2;
+}
+
+static bsdf_sample sample_bsdf(int type, const po_material* mat, po_v3 V, po_v3 N,
+                               next2_fn next2, void* ctx, po_ior_stack* ior)
+{
+    if (type == PO_DELTA) {                                /* BSRDF.cpp:216-229 */
+        bsdf_sample s;
+        s.energy = v3(mat->specular[0], mat->specular[1], mat->specular[2]);
+        s.L = reflect3(v3_neg(V), N);
+        s.P = 1.0f;
+        return s;
+    }
+    if (type == PO_BTDF) return transparent_sample(mat, V, N, ior, next2, ctx);
+    if (type == PO_FRESNEL) {                              /* BSRDF.cpp:364-385 */
+        const po_m3 w2t = tangent_frame(V, N);
+        const po_v3 vt = v3_normalize(m3_mul_v3(&w2t, V));
+        float xi[2];
+        next2(ctx, xi);
+        const float F = fresnel_factor(vt.z, mat->index_of_refraction, ior_top(ior));
+        bsdf_sample s;
+        if (xi[0] < F) {
+            s = sample_bsdf(PO_SPECULAR, mat, V, N, next2, ctx, ior);
+            s.P *= F;
+        } else {
+            s = transparent_sample(mat, V, N, ior, next2, ctx);
+            s.P *= 1.0f - F;
+        }
+        return s;
+    }
     const po_m3 w2t = tangent_frame(V, N);
     const po_m3 t2w = m3_inverse(&w2t);
     const po_v3 vt = v3_normalize(m3_mul_v3(&w2t, V));
@@ -389,7 +478,8 @@ void po_bsdf_sample(int bsdf, const po_material* mat, const float* V, const floa
                     const float* xi, float* L, float* P, float* energy)
 {
     fixed_xi f = {xi, 0};
-    bsdf_sample s = sample_bsdf(bsdf, mat, v3(V[0], V[1], V[2]), v3(N[0], N[1], N[2]), fixed_next2, &f);
+    po_ior_stack ior = {{1.0f}, 1};
+    bsdf_sample s = sample_bsdf(bsdf, mat, v3(V[0], V[1], V[2]), v3(N[0], N[1], N[2]), fixed_next2, &f, &ior);
     L[0] = s.L.x; L[1] = s.L.y; L[2] = s.L.z;
     *P = s.P;
     energy[0] = s.energy.x; energy[1] = s.energy.y; energy[2] = s.energy.z;
@@ -462,7 +552,7 @@ void po_scene_build_light_tables(po_scene* s)
 {
     for (uint32_t l = 0; l < s->nlights; ++l) {
         po_mesh* m = &s->meshes[s->instances[s->lights[l]].mesh];
-        if (m->alias_weight) continue;
+        if (m->alias_weight || m->desc.shape != PO_SHAPE_TRIANGLES) continue;
         float* w = (float*)malloc(sizeof(float) * (m->desc.ntris ? m->desc.ntris : 1));
         po_triangle_weights(&m->desc, w);
         m->alias_n = m->desc.ntris;
@@ -488,12 +578,42 @@ static const po_material* material_of(const po_scene* s, uint32_t inst)
     return &s->materials[s->instances[inst].material];
 }
 
+/* sample_geometry of the implicit shapes (LowerLevelImplicitShapesBVH.cpp:59-67, 93-112): a
+ * uniform point on the radius-0.5 sphere (uniform_sample_sphere, RandUtils.cpp:43-49: phi in
+ * double from M_PI, std::cos / std::sin of the float phi) or on a face of the unit cube. */
+static po_v3 implicit_light_point(uint32_t shape, integrator* it)
+{
+    float xi[2];
+    if (shape == PO_SHAPE_SPHERE) {
+        po_hammersley_next(it->xs, xi);
+        const float z = 1 - 2 * xi[0];
+        const float r = sqrtf((0.0f < 1.0f - z * z) ? 1.0f - z * z : 0.0f);
+        const float phi = (float)(2 * M_PI * (double)xi[1]);
+        const po_v3 u = v3(r * cosf(phi), r * sinf(phi), z);
+        return v3_scale(u, 0.5f);
+    }
+    float xj[2], xk[2];
+    po_hammersley_next(it->xs, xi);
+    po_hammersley_next(it->xs, xj);
+    po_hammersley_next(it->xs, xk);
+    const float c[3] = {xi[0] - 0.5f, xi[1] - 0.5f, xj[0] - 0.5f};
+    float corner[3], face[3];
+    for (int a = 0; a < 3; ++a) corner[a] = (float)((0.0f < c[a]) - (c[a] < 0.0f));
+    uint32_t zero_axis = (uint32_t)(xj[1] * 3.0f);
+    if (zero_axis == 3) zero_axis = 2;
+    face[zero_axis] = 0.0f;
+    face[(zero_axis + 1) % 3] = xk[0];
+    face[(zero_axis + 2) % 3] = xk[1];
+    return v3(corner[0] * 0.5f + -corner[0] * face[0], corner[1] * 0.5f + -corner[1] * face[1],
+              corner[2] * 0.5f + -corner[2] * face[2]);
+}
+
 /* Monte_Carlo_Integrator::sample_direct_lighting (Integrators.cpp:46-128). */
 static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3* radiance, float* pdf)
 {
     const po_scene* s = it->s;
     const int type = (int)s->instances[f->inst].bsdf;
-    if (type == PO_BTDF || type == PO_LIGHT) return 0;
+    if (type == PO_BTDF || type == PO_FRESNEL || type == PO_LIGHT) return 0;   /* both BTDFs are kBTDF */
     const po_material* mat = material_of(s, f->inst);
     const int sun = s->sky.use_sun != 0;
     uint32_t light_count = s->nlights + (sun ? 1u : 0u);
@@ -515,7 +635,10 @@ static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3
     }
     const po_instance* light = &s->instances[s->lights[light_index]];
     const po_mesh* lm = &s->meshes[light->mesh];
-
+    po_v3 sp;
+    if (lm->desc.shape != PO_SHAPE_TRIANGLES) {
+        sp = implicit_light_point(lm->desc.shape, it);
+    } else {
     /* AliasTable::sample (AliasTable.cpp:89-104) then a uniform triangle point. */
     const uint32_t bucket = po_xorshift_next(it->xs) % lm->alias_n;
     const float coin = (float)po_xorshift_next(it->xs) / (float)4294967295u;
@@ -528,8 +651,9 @@ static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3
     const float* p1 = lm->desc.positions + 3 * lm->desc.indices[3 * tri + 1];
     const float* p2 = lm->desc.positions + 3 * lm->desc.indices[3 * tri + 2];
     const float w0 = (1.0f - bary[0]) - bary[1];
-    po_v3 sp = v3_add(v3_add(v3_scale(v3(p0[0], p0[1], p0[2]), w0), v3_scale(v3(p1[0], p1[1], p1[2]), bary[0])),
-                      v3_scale(v3(p2[0], p2[1], p2[2]), bary[1]));
+    sp = v3_add(v3_add(v3_scale(v3(p0[0], p0[1], p0[2]), w0), v3_scale(v3(p1[0], p1[1], p1[2]), bary[0])),
+                v3_scale(v3(p2[0], p2[1], p2[2]), bary[1]));
+    }
     sp = v3_of4(m4_mul_v4(&light->T, v4_of3(sp, 1.0f)));
 
     const po_v4 P = v4(f->position[0], f->position[1], f->position[2], f->position[3]);
@@ -550,7 +674,7 @@ static int direct_lighting(integrator* it, const po_fragment* f, po_v3 wi, po_v3
     return 0;
 }
 
-typedef struct { po_v3 payload, throughput; po_v4 org; po_v3 dir; } path_state;
+typedef struct { po_v3 payload, throughput; po_v4 org; po_v3 dir; po_ior_stack ior; } path_state;
 
 static po_v3 sky_colour(const po_scene* s, po_v3 d) { return v3_of4(po_sky_lookup(s, d)); }
 
@@ -563,7 +687,7 @@ static void trace_path(integrator* it, po_fragment frag, path_state* ray)
         const int type = (int)s->instances[frag.inst].bsdf;
         const po_material* mat = material_of(s, frag.inst);
         const po_v3 N = v3(frag.normal[0], frag.normal[1], frag.normal[2]);
-        const bsdf_sample smp = sample_bsdf(type, mat, v3_neg(ray->dir), N, ham_next2, it);
+        const bsdf_sample smp = sample_bsdf(type, mat, v3_neg(ray->dir), N, ham_next2, it, &ray->ior);
         if (type == PO_LIGHT)
             ray->payload = v3_add(ray->payload, v3_mul(ray->throughput, smp.energy));
         po_v3 rad; float pdf;
@@ -575,7 +699,7 @@ static void trace_path(integrator* it, po_fragment frag, path_state* ray)
         if (po_mt64_uniform(it->mt) > q) return;
         ray->throughput = v3_scale(ray->throughput, 1.0f / q);
         ray->throughput = v3_mul(ray->throughput, v3_scale(smp.energy, smp.P));
-        const po_v3 off = v3_scale(N, 0.01f);
+        const po_v3 off = v3_scale(ior_inside(&ray->ior) ? v3_neg(N) : N, 0.01f);   /* Integrators.cpp:199 */
         ray->org = v4(frag.position[0] + off.x, frag.position[1] + off.y, frag.position[2] + off.z,
                       frag.position[3] + 0.0f);
         ray->dir = smp.L;
@@ -609,6 +733,8 @@ static po_v3 integrate(integrator* it, const po_camera* cam, uint32_t px, uint32
     ps.dir = v3(r.dir[0], r.dir[1], r.dir[2]);
     ps.payload = v3(0.0f, 0.0f, 0.0f);
     ps.throughput = v3(1.0f, 1.0f, 1.0f);
+    ps.ior.n = 0;
+    ior_push(&ps.ior, 1.0f);
     po_fragment f;
     if (po_closest_hit(it->s, ps.org, ps.dir, &f, NULL)) {
         trace_path(it, f, &ps);

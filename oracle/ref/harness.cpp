@@ -20,6 +20,7 @@
 
 #include "Core/Camera.hpp"
 #include "Core/Image.hpp"
+#include "Core/LowerLevelImplicitShapesBVH.hpp"
 #include "Core/LowerLevelMeshBVH.hpp"
 #include "Core/MaterialManager.hpp"
 #include "Core/RandUtils.hpp"
@@ -27,6 +28,7 @@
 #include "Core/ThreadPool.hpp"
 #include "Core/UpperLevelBVH.hpp"
 #include "Core/vectorUtils.hpp"
+#include "Render/BasicMaterials.hpp"
 #include "Render/BSRDF.hpp"
 #include "Render/Distributions.hpp"
 #include "Render/Integrators.hpp"
@@ -98,8 +100,27 @@ private:
     Core::EvaluatedMaterial e;
 };
 
+// A constant transparent material (what Scene::add_material makes for an
+// "IndexOfRefraction" entry, Core/Scene.cpp:526-530), fixed EvaluatedMaterial.
+class FixedTransparentMaterial : public Render::ConstantTransparentMaterial {
+public:
+    explicit FixedTransparentMaterial(const po_material& m) : Render::ConstantTransparentMaterial(1.0f, m.index_of_refraction)
+    {
+        e.diffuse = glm::vec3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+        e.specular = glm::vec3(m.specular[0], m.specular[1], m.specular[2]);
+        e.roughness = m.roughness;
+        e.normal = glm::vec3(0.0f, 1.0f, 0.0f);
+        e.emissive = glm::vec3(m.emissive[0], m.emissive[1], m.emissive[2]);
+    }
+    Core::EvaluatedMaterial evaluate_material(const glm::vec2&) const override { return e; }
+    bool is_light() const override { return e.emits_light(); }
+private:
+    Core::EvaluatedMaterial e;
+};
+
 struct RefScene {
-    std::vector<std::unique_ptr<LowerLevelMeshBVH>> blas;
+    std::vector<std::unique_ptr<LowerLevelBVH>> blas;
+    std::vector<uint32_t> shape;
     UpperLevelBVH tlas;
     Core::MaterialManager materials;
     std::vector<Scene::Light> lights;
@@ -141,14 +162,29 @@ std::unique_ptr<Render::BSRDF> make_bsrdf(RefScene& s, uint32_t kind, uint32_t m
         b = std::make_unique<Render::Dielectric_BRDF>(d0, d1, s.materials, material);
     } else if (kind == PO_LIGHT) {
         b = std::make_unique<Render::Light_BRDF>(s.materials, material);
+    } else if (kind == PO_BTDF) {                                 // "Transparent", Scene.cpp:392-398
+        std::unique_ptr<Render::Distribution> d = std::make_unique<Render::Beckmann_All_Microfacet_Distribution>();
+        b = std::make_unique<Render::Transparent_BTDF>(d, s.materials, material);
+    } else if (kind == PO_FRESNEL) {                              // "Fresnel", Scene.cpp:399-405
+        std::unique_ptr<Render::Distribution> d0 = std::make_unique<Render::Beckmann_All_Microfacet_Distribution>();
+        std::unique_ptr<Render::Distribution> d1 = std::make_unique<Render::Beckmann_All_Microfacet_Distribution>();
+        b = std::make_unique<Render::Fresnel_BTDF>(d0, d1, s.materials, material);
+    } else if (kind == PO_DELTA) {                                // "Delta", Scene.cpp:413-416
+        b = std::make_unique<Render::Specular_Delta_BRDF>(s.materials, material);
     }
     return b;
+}
+
+// The triangle index carried in the vertex colour; implicit shapes have none.
+uint32_t prim_of(const RefScene& s, uint32_t inst, const InterpolatedVertex& v)
+{
+    return s.shape[inst] != PO_SHAPE_TRIANGLES ? PO_IMPLICIT_PRIM : (uint32_t)std::lround(v.mVertexColour.x);
 }
 
 void fill_fragment(const RefScene& s, const InterpolatedVertex& v, float t_world, po_fragment* f)
 {
     f->inst = s.instance_of.at(v.m_bsrdf);
-    f->prim = (uint32_t)std::lround(v.mVertexColour.x);
+    f->prim = prim_of(s, f->inst, v);
     f->t = t_world;
     f->u = v.mUV.x;
     f->v = v.mUV.y;
@@ -223,6 +259,12 @@ void* ref_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes, const po_in
     auto* s = new RefScene();
     for (uint32_t m = 0; m < nmeshes; ++m) {
         const po_mesh_desc& d = meshes[m];
+        if (d.shape == PO_SHAPE_SPHERE || d.shape == PO_SHAPE_CUBE) {   // Scene.cpp:49-57
+            if (d.shape == PO_SHAPE_SPHERE) s->blas.push_back(std::make_unique<LowerLevelSphereBVH>(0.5f));
+            else s->blas.push_back(std::make_unique<LowerLevelCube>());
+            s->ntris.push_back(0);
+            continue;
+        }
         aiMesh mesh;
         mesh.mName = aiString("mesh");
         mesh.mNumVertices = 3 * d.ntris;
@@ -252,7 +294,9 @@ void* ref_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes, const po_in
         s->ntris.push_back(d.ntris);
     }
     for (uint32_t i = 0; i < nmats; ++i) {
-        std::unique_ptr<Core::Material> m = std::make_unique<FixedMaterial>(mats[i]);
+        std::unique_ptr<Core::Material> m;
+        if (mats[i].index_of_refraction > 0.0f) m = std::make_unique<FixedTransparentMaterial>(mats[i]);
+        else m = std::make_unique<FixedMaterial>(mats[i]);
         s->materials.add_material(m);
     }
     std::vector<bool> sampled(nmeshes, false);
@@ -265,6 +309,7 @@ void* ref_scene_create(const po_mesh_desc* meshes, uint32_t nmeshes, const po_in
             s->lights.push_back({T, glm::inverse(T), s->blas[inst[i].mesh].get()});
         }
         s->instance_of[b.get()] = i;
+        s->shape.push_back(meshes[inst[i].mesh].shape);
         s->tlas.add_lower_level_bvh(s->blas[inst[i].mesh].get(), T, b);
     }
     s->tlas.build();
@@ -352,7 +397,7 @@ double ref_trace_timed(const void* p, const po_ray* rays, uint32_t n, po_hit* hi
             InterpolatedVertex v{};
             if (s->tlas.get_closest_intersection(ray, &v)) {
                 hits[i].inst = s->instance_of.at(v.m_bsrdf);
-                hits[i].prim = (uint32_t)std::lround(v.mVertexColour.x);
+                hits[i].prim = prim_of(*s, hits[i].inst, v);
                 hits[i].t = glm::length(v.mPosition - ray.mOrigin);
                 hits[i].u = v.mUV.x; hits[i].v = v.mUV.y;
             } else {
@@ -371,19 +416,19 @@ double ref_trace_timed(const void* p, const po_ray* rays, uint32_t n, po_hit* hi
 uint32_t ref_blas_node_count(const void* p, uint32_t mesh)
 {
     const auto* s = static_cast<const RefScene*>(p);
-    const auto* bvh = (*s->blas[mesh]).*robbed(BlasTag{});
+    const auto* bvh = (*static_cast<LowerLevelMeshBVH*>(s->blas[mesh].get())).*robbed(BlasTag{});
     return (uint32_t)((*bvh).*robbed(BNodesTag{})).size();
 }
 uint32_t ref_blas_root(const void* p, uint32_t mesh)
 {
     const auto* s = static_cast<const RefScene*>(p);
-    const auto* bvh = (*s->blas[mesh]).*robbed(BlasTag{});
+    const auto* bvh = (*static_cast<LowerLevelMeshBVH*>(s->blas[mesh].get())).*robbed(BlasTag{});
     return (*bvh).*robbed(BRootTag{});
 }
 void ref_blas_nodes(const void* p, uint32_t mesh, float* boxes, uint32_t* links, uint32_t* values)
 {
     const auto* s = static_cast<const RefScene*>(p);
-    const auto* bvh = (*s->blas[mesh]).*robbed(BlasTag{});
+    const auto* bvh = (*static_cast<LowerLevelMeshBVH*>(s->blas[mesh].get())).*robbed(BlasTag{});
     dump_nodes(bvh, 0, boxes, links, values, nullptr);
 }
 uint32_t ref_tlas_node_count(const void* p)
@@ -415,8 +460,8 @@ void ref_instance_inverse(const void* p, uint32_t inst, float* out)
 uint32_t ref_light_table(const void* p, uint32_t mesh, float* areas, float* bucket_weight, uint32_t* bucket_alias)
 {
     const auto* s = static_cast<const RefScene*>(p);
-    const auto& area = (*s->blas[mesh]).*robbed(AreaTag{});
-    const auto& table = (*s->blas[mesh]).*robbed(AliasTag{});
+    const auto& area = (*static_cast<LowerLevelMeshBVH*>(s->blas[mesh].get())).*robbed(AreaTag{});
+    const auto& table = (*static_cast<LowerLevelMeshBVH*>(s->blas[mesh].get())).*robbed(AliasTag{});
     const auto& buckets = table.*robbed(BucketsTag{});
     for (size_t i = 0; i < area.size(); ++i) {
         if (areas) areas[i] = area[i];

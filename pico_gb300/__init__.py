@@ -166,6 +166,7 @@ class Context:
             mats[i].specular[:] = list(m.specular)
             mats[i].roughness = m.roughness
             mats[i].emissive[:] = list(m.emissive)
+            mats[i].index_of_refraction = m.ior
         arr = [np.ascontiguousarray(a, np.float32) for a in (V, N, H, xi)]
         pdf, P, dl = (np.empty(n, np.float32) for _ in range(3))
         L, E = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)

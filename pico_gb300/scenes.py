@@ -21,7 +21,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .types import DIELECTRIC, DIFFUSE, LIGHT, RAY_DTYPE, Camera, Instance, Material, Mesh, SceneData
+from .types import (BTDF, DELTA, DIELECTRIC, DIFFUSE, FRESNEL, LIGHT, RAY_DTYPE, SHAPE_CUBE, SHAPE_SPHERE, Camera,
+                    Instance, Material, Mesh, SceneData)
 
 
 # ----------------------------------------------------------------------------- matrices
@@ -75,6 +76,12 @@ def quad_mesh(corners, normal) -> Mesh:
     p = np.asarray(corners, np.float64)
     n = np.tile(np.asarray(normal, np.float64), (4, 1))
     return Mesh(p, n, np.array([[0, 1, 2], [0, 2, 3]], np.uint32))
+
+
+def implicit_mesh(shape: int) -> Mesh:
+    """The implicit "Sphere" (radius 0.5) or "Cube" ([-0.5, 0.5]^3) asset."""
+    z = np.zeros((0, 3))
+    return Mesh(z, z, np.zeros((0, 3), np.uint32), shape=shape)
 
 
 def cube_mesh() -> Mesh:
@@ -228,6 +235,29 @@ def lit_field(n_instances: int = 4096, level: int = 4, seed: int = 12345, n_ligh
                                    [cx - h, y, cz + h]], [0, -1, 0]))
         s.materials.append(Material(diffuse=(0.8, 0.8, 0.8), emissive=(le, le, le)))
         s.instances.append(Instance(len(s.meshes) - 1, glm_storage(np.eye(4)), LIGHT, len(s.materials) - 1))
+    return s
+
+
+def cornell_shapes() -> SceneData:
+    """The Cornell box with the implicit assets and the remaining lobes: a Transparent
+    and a Fresnel glass sphere (IoR 1.5), a Delta mirror cube, and a small sphere and a
+    small cube as extra area lights."""
+    s = cornell_box()
+    sph, cub = len(s.meshes), len(s.meshes) + 1
+    s.meshes += [implicit_mesh(SHAPE_SPHERE), implicit_mesh(SHAPE_CUBE)]
+    glass, mirror, lamp = len(s.materials), len(s.materials) + 1, len(s.materials) + 2
+    s.materials += [Material(diffuse=(0.9, 0.9, 0.9), specular=(0.04, 0.04, 0.04), roughness=0.1, ior=1.5),
+                    Material(diffuse=(0.1, 0.1, 0.1), specular=(0.9, 0.8, 0.7), roughness=0.2),
+                    Material(diffuse=(0.8, 0.8, 0.8), emissive=(6.0, 6.0, 6.0))]
+
+    def place(t, sc, rot=0.0):
+        return glm_storage(translate(t) @ rotate_y(rot) @ scale(sc))
+
+    s.instances += [Instance(sph, place((0.3, 0.25, 0.4), 0.35), BTDF, glass),
+                    Instance(sph, place((0.7, 0.2, 0.6), 0.3), FRESNEL, glass),
+                    Instance(cub, place((0.55, 0.6, 0.3), 0.2, 30.0), DELTA, mirror),
+                    Instance(sph, place((0.2, 0.8, 0.7), 0.1), LIGHT, lamp),
+                    Instance(cub, place((0.8, 0.85, 0.3), 0.08), LIGHT, lamp)]
     return s
 
 

@@ -13,7 +13,9 @@ from dataclasses import dataclass, field
 import numpy as np
 
 # BSRDF kinds, numbered like Render::BSRDF_Type (Render/BSRDF.hpp:32-39).
-DIFFUSE, SPECULAR, DIELECTRIC, BTDF, LIGHT = 0, 1, 2, 3, 4
+DIFFUSE, SPECULAR, DIELECTRIC, BTDF, LIGHT, FRESNEL, DELTA = 0, 1, 2, 3, 4, 5, 6
+# Mesh shapes (pico_shape).
+SHAPE_TRIANGLES, SHAPE_SPHERE, SHAPE_CUBE = 0, 1, 2
 
 RAY_DTYPE = np.dtype([("org", "<f4", (4,)), ("dir", "<f4", (4,))])
 HIT_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -24,7 +26,7 @@ class CMesh(C.Structure):
     _fields_ = [("nverts", C.c_uint32), ("ntris", C.c_uint32),
                 ("positions", C.POINTER(C.c_float)), ("normals", C.POINTER(C.c_float)),
                 ("uvs", C.POINTER(C.c_float)), ("indices", C.POINTER(C.c_uint32)),
-                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3)]
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("shape", C.c_uint32)]
 
 
 class CInstance(C.Structure):
@@ -34,7 +36,7 @@ class CInstance(C.Structure):
 
 class CMaterial(C.Structure):
     _fields_ = [("diffuse", C.c_float * 3), ("specular", C.c_float * 3), ("roughness", C.c_float),
-                ("emissive", C.c_float * 3)]
+                ("emissive", C.c_float * 3), ("index_of_refraction", C.c_float)]
 
 
 # Sky kinds (pico_sky_kind).
@@ -72,6 +74,7 @@ class Mesh:
     normals: np.ndarray              # (nverts, 3) float32
     indices: np.ndarray              # (ntris, 3) uint32
     uvs: np.ndarray | None = None    # (nverts, 2) float32
+    shape: int = SHAPE_TRIANGLES     # SHAPE_SPHERE / SHAPE_CUBE: implicit asset, arrays empty
 
     def __post_init__(self):
         self.positions = np.ascontiguousarray(self.positions, dtype=np.float32).reshape(-1, 3)
@@ -95,6 +98,7 @@ class Material:
     specular: tuple = (0.0, 0.0, 0.0)
     roughness: float = 1.0
     emissive: tuple = (0.0, 0.0, 0.0)
+    ior: float = 0.0                 # index of refraction of a transparent material
 
 
 @dataclass
@@ -190,6 +194,7 @@ class MarshalledScene:
             lo, hi = m.aabb
             cm.aabb_min[:] = [float(x) for x in lo]
             cm.aabb_max[:] = [float(x) for x in hi]
+            cm.shape = m.shape
             self.keep.append(m)
         k = len(scene.instances)
         self.instances = (CInstance * max(k, 1))()
@@ -206,6 +211,7 @@ class MarshalledScene:
             cm.specular[:] = list(mat.specular)
             cm.roughness = mat.roughness
             cm.emissive[:] = list(mat.emissive)
+            cm.index_of_refraction = mat.ior
         self.desc = CSceneDesc()
         self.desc.meshes, self.desc.nmeshes = self.meshes, n
         self.desc.instances, self.desc.ninstances = self.instances, k

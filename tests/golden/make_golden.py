@@ -310,6 +310,38 @@ def sky_fixtures(ref):
     np.savez_compressed(HERE / "sky.npz", **out)
 
 
+def shapes_fixtures(ref):
+    """Implicit sphere / cube instances, the Transparent, Fresnel and Delta lobes with the
+    ray's index-of-refraction stack, and implicit area lights (Cornell box)."""
+    out = {}
+    scene = scenes.cornell_shapes()
+    out.update(scene_arrays(scene, "shapes"))
+    rs = ref.scene(scene)
+    rng = np.random.default_rng(601)
+    n = 8192
+    org = rng.uniform(0.05, 0.95, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(n, RAY_DTYPE)
+    rays["org"][:, :3], rays["org"][:, 3] = org, 1.0
+    rays["dir"][:, :3], rays["dir"][:, 3] = d, 10000.0
+    out["rays"] = rays
+    f = rs.fragments(rays)
+    for k in ("inst", "prim", "t", "position", "normal"):
+        out[f"hit_{k}"] = f[k]
+    cam = scenes.cornell_camera(48, 48)
+    out["cam"] = camera_array(cam)
+    px = np.array([[24, 24], [14, 34], [34, 30], [16, 12], [33, 14], [24, 8], [8, 40], [40, 40]], np.uint32)
+    seeds = np.array([11, 12, 13, 14, 15, 16, 17, 18], np.uint64)
+    samples = np.empty((len(px), 64, 3), np.float32)
+    for i in range(len(px)):
+        samples[i] = rs.integrate(cam, int(px[i, 0]), int(px[i, 1]), 6, int(seeds[i]), 64)
+    out["integ_px"], out["integ_seed"], out["integ_samples"] = px, seeds, samples
+    n_, p_, d_ = rs.denoiser_inputs(cam)
+    out["normals"], out["positions"], out["diffuse"] = n_, p_, d_
+    np.savez_compressed(HERE / "shapes.npz", **out)
+
+
 def main():
     pico_oracle.build_reference()
     ref = pico_oracle.Reference()
@@ -318,6 +350,7 @@ def main():
     integrator_fixtures(ref)
     atrous_fixtures(ref)
     sky_fixtures(ref)
+    shapes_fixtures(ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

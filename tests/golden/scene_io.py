@@ -12,11 +12,13 @@ def scene_arrays(scene: SceneData, prefix: str = "scene") -> dict:
         out[f"{prefix}_m{i}_pos"] = m.positions
         out[f"{prefix}_m{i}_nrm"] = m.normals
         out[f"{prefix}_m{i}_idx"] = m.indices
+        if m.shape:
+            out[f"{prefix}_m{i}_shape"] = np.array(m.shape)
     out[f"{prefix}_inst_meta"] = np.array([[i.mesh, i.bsdf, i.material] for i in scene.instances], np.uint32)
     out[f"{prefix}_inst_xf"] = np.stack([np.asarray(i.transform, np.float32).reshape(4, 4)
                                          for i in scene.instances])
-    out[f"{prefix}_mats"] = np.array([[*m.diffuse, *m.specular, m.roughness, *m.emissive] for m in scene.materials],
-                                     np.float32)
+    out[f"{prefix}_mats"] = np.array([[*m.diffuse, *m.specular, m.roughness, *m.emissive, m.ior]
+                                      for m in scene.materials], np.float32)
     out[f"{prefix}_sky"] = np.array(scene.sky, np.float32)
     if scene.sky_image is not None:
         out.update(sky_arrays(scene.sky_image, f"{prefix}_skyimg"))
@@ -40,9 +42,11 @@ def load_sky(z, prefix: str) -> Sky:
 
 def load_scene(z, prefix: str = "scene") -> SceneData:
     n = int(z[f"{prefix}_nmeshes"])
-    meshes = [Mesh(z[f"{prefix}_m{i}_pos"], z[f"{prefix}_m{i}_nrm"], z[f"{prefix}_m{i}_idx"]) for i in range(n)]
+    meshes = [Mesh(z[f"{prefix}_m{i}_pos"], z[f"{prefix}_m{i}_nrm"], z[f"{prefix}_m{i}_idx"],
+                   shape=int(z[f"{prefix}_m{i}_shape"]) if f"{prefix}_m{i}_shape" in z else 0) for i in range(n)]
     insts = [Instance(int(a), x, int(b), int(c)) for (a, b, c), x in zip(z[f"{prefix}_inst_meta"], z[f"{prefix}_inst_xf"])]
-    mats = [Material(tuple(r[0:3]), tuple(r[3:6]), float(r[6]), tuple(r[7:10])) for r in z[f"{prefix}_mats"]]
+    mats = [Material(tuple(r[0:3]), tuple(r[3:6]), float(r[6]), tuple(r[7:10]), float(r[10]) if len(r) > 10 else 0.0)
+            for r in z[f"{prefix}_mats"]]
     sky = load_sky(z, f"{prefix}_skyimg") if f"{prefix}_skyimg_kind" in z else None
     return SceneData(meshes, insts, mats, tuple(z[f"{prefix}_sky"]), sky)
 

@@ -215,6 +215,32 @@ def test_integrator_with_sky_and_sun_matches_reference(oracle):
         assert_bits(got, z[key], f"G-buffer {key}")
 
 
+def test_implicit_shapes_match_reference(oracle):
+    """LowerLevelSphereBVH / LowerLevelCube hits through scaled, rotated instances."""
+    z = np.load(GOLDEN / "shapes.npz")
+    f = oracle.scene(load_scene(z, "shapes")).fragments(z["rays"])
+    for k in ("inst", "prim"):
+        np.testing.assert_array_equal(f[k], z[f"hit_{k}"], err_msg=k)
+    hit = z["hit_inst"] != 0xFFFFFFFF
+    assert (z["hit_prim"] == 0xFFFFFFFE).sum() > 1000
+    for k in ("t", "position", "normal"):
+        assert_bits(f[k][hit], z[f"hit_{k}"][hit], k)
+
+
+def test_integrator_with_btdfs_and_implicit_lights_matches_reference(oracle):
+    """Transparent and Fresnel glass (index-of-refraction stack), a Delta mirror, and
+    sphere / cube area lights, sample for sample."""
+    z = np.load(GOLDEN / "shapes.npz")
+    scene, cam = load_scene(z, "shapes"), load_camera(z["cam"])
+    os_ = oracle.scene(scene)
+    for i, (px, py) in enumerate(z["integ_px"]):
+        got = os_.integrate(cam, int(px), int(py), 6, int(z["integ_seed"][i]), z["integ_samples"].shape[1])
+        assert_bits(got, z["integ_samples"][i], f"pixel {i} samples")
+    n, p, d = os_.denoiser_inputs(cam)
+    for got, key in ((n, "normals"), (p, "positions"), (d, "diffuse")):
+        assert_bits(got, z[key], f"G-buffer {key}")
+
+
 def test_accumulate_drops_first_sample(oracle):
     """Scene.cpp:185-191: mean += (x - mean) / prev_count, so the first sample is replaced."""
     s = np.array([[10, 10, 10], [1, 1, 1], [3, 3, 3]], np.float32)
