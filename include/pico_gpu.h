@@ -123,7 +123,9 @@ typedef struct { float org[4]; float dir[4]; } pico_ray;
 
 /* Closest hit: instance (insertion index), triangle (mesh index), world distance
  * |T * P(u,v) - O| exactly as lower_level_intersector::intersects computes it,
- * and the barycentrics.  A miss has inst = prim = 0xffffffff and t = +inf. */
+ * and the barycentrics.  A miss has inst = prim = 0xffffffff and t = +inf; a hit
+ * on an implicit sphere or cube has prim = 0xfffffffe and its object-space ray
+ * parameter in u. */
 typedef struct { uint32_t inst, prim; float t, u, v; } pico_hit;
 
 /* Scene::Camera members (Core/Camera.hpp:98-107); the FOV is carried but, as in
@@ -158,7 +160,10 @@ const char* pico_gpu_last_error(const pico_gpu_ctx* ctx);
  * comparisons exactly like BVH::get_closest_intersections (Core/BVH.cpp:27-63).
  * They differ only where the reference's float slab test prunes a box whose
  * triangle is a few ulp nearer than the best so far (near-ties at shared
- * edges); REFERENCE reproduces the reference's choice there too. */
+ * edges); REFERENCE reproduces the reference's choice there too.  Scenes with
+ * implicit sphere instances are always walked in the REFERENCE order: the
+ * reference's sphere test reports points off a scaled sphere, and which of them
+ * it returns depends on its own visit order. */
 enum pico_traversal_order { PICO_ORDER_NEAR_FIRST = 0, PICO_ORDER_REFERENCE = 1 };
 int pico_gpu_set_traversal_order(pico_gpu_ctx* ctx, int order);
 

@@ -18,7 +18,8 @@ from pathlib import Path
 
 import numpy as np
 
-from .types import (SKY_CONSTANT, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF, Sky,  # noqa: F401
+from .types import (SKY_CONSTANT, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF, Sky, SHAPE_TRIANGLES, SHAPE_SPHERE,  # noqa: F401
+                    SHAPE_CUBE, BTDF, FRESNEL, DELTA,  # noqa: F401
                     CCamera, CRenderConfig, CSceneDesc, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
                     MarshalledScene, Material, Mesh, SceneData, DIFFUSE, SPECULAR, DIELECTRIC, LIGHT, MISS)
 

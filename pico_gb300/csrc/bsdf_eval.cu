@@ -25,7 +25,10 @@ __global__ void bsdf_eval_kernel(uint64_t n, const uint32_t* kinds, const GpuMat
         b = xi[4 * i + 2 * used + 1];
         ++used;
     };
-    const BsdfSample s = sample_bsdf(kind, m, v, nn, next_xi);
+    IorStack ior;   // a camera path's stack: {1.0}
+    ior.n = 0;
+    ior.push(1.0f);
+    const BsdfSample s = sample_bsdf(kind, m, v, nn, next_xi, ior);
     L[3 * i] = s.L.x; L[3 * i + 1] = s.L.y; L[3 * i + 2] = s.L.z;
     P[i] = s.P;
     energy[3 * i] = s.energy.x; energy[3 * i + 1] = s.energy.y; energy[3 * i + 2] = s.energy.z;
@@ -52,6 +55,7 @@ extern "C" int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t*
             g.diffuse[a] = m.diffuse[a]; g.specular[a] = m.specular[a]; g.emissive[a] = m.emissive[a];
         }
         g.roughness = m.roughness;
+        g.ior = m.index_of_refraction;
         const float s = std::sqrt((m.specular[0] * m.specular[0] + m.specular[1] * m.specular[1]) +
                                   m.specular[2] * m.specular[2]);
         const float d = std::sqrt((m.diffuse[0] * m.diffuse[0] + m.diffuse[1] * m.diffuse[1]) +

@@ -139,6 +139,12 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     s->nlights = (uint32_t)fs.lights.size();
     s->ninstances = (uint32_t)fs.inst_shade.size();
     s->inst_rank_host = fs.inst_rank;
+    bool implicit = false;
+    for (uint32_t i = 0; i < desc->ninstances; ++i) {
+        const uint32_t shape = desc->meshes[desc->instances[i].mesh].shape;
+        if (shape == PICO_SHAPE_SPHERE) s->needs_reference_order = true;
+        if (shape != PICO_SHAPE_TRIANGLES) implicit = true;
+    }
     s->light_inst_host.reserve(fs.lights.size());
     for (const GpuLight& l : fs.lights) s->light_inst_host.push_back(l.inst);
 
@@ -190,6 +196,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
         v.tlas_fast_lo[a] = fs.tlas_fast_lo[a]; v.tlas_fast_hi[a] = fs.tlas_fast_hi[a];
     }
     v.ninstances = (uint32_t)fs.inst_shade.size();
+    v.has_implicit = implicit ? 1u : 0u;
     v.sky_kind = fs.sky_kind; v.sky_w = fs.sky_w; v.sky_h = fs.sky_h; v.sky_pixels = skypx;
     v.use_sun = fs.use_sun;
     for (int a = 0; a < 3; ++a) { v.sun_dir[a] = fs.sun_dir[a]; v.sun_col[a] = fs.sun_col[a]; }
@@ -236,7 +243,7 @@ int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene
     if (!ctx || !scene || (n && (!d_rays || !d_hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return set_error(ctx, PICO_ERR_INVALID_ARG, "rays not 16-byte aligned");
     const cudaError_t e = launch_trace(scene->view, d_rays, n, d_hits, ctx->status, false,
-                                       ctx->order, static_cast<cudaStream_t>(stream));
+                                       scene_order(ctx, scene), static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_error(ctx, e, "trace launch");
     return PICO_OK;
 }
@@ -258,7 +265,7 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
     cudaError_t e = ctx->buf_e.reserve(sizeof(pico_hit) * (n ? n : 1));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->counters, 0, sizeof(ctx->status->counters), st);
     if (e == cudaSuccess)
-        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, ctx->order, st);
+        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, scene_order(ctx, scene), st);
     unsigned long long c[4] = {0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(c, ctx->status->counters, sizeof c, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -291,7 +298,7 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
         pico_hit* dh = static_cast<pico_hit*>(hbuf[s]->ptr);
         e = cudaMemcpyAsync(dr, rays + off, m * sizeof(pico_ray), cudaMemcpyHostToDevice, streams[s]);
         if (e == cudaSuccess)
-            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, ctx->order, streams[s]);
+            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, scene_order(ctx, scene), streams[s]);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(hits + off, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, streams[s]);
     }

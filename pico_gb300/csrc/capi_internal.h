@@ -47,10 +47,21 @@ struct pico_gpu_scene {
     std::vector<uint32_t> inst_rank_host;
     std::vector<uint32_t> light_inst_host;
     uint32_t nlights = 0, ninstances = 0;
+    // The reference's sphere intersector solves its quadratic as if the object-space
+    // direction had unit length, so through a scaled instance it reports points off the
+    // sphere, even for rays that miss it (Core/LowerLevelImplicitShapesBVH.cpp:24-52).
+    // Which of those the reference returns depends on its own visit order and pruning,
+    // so scenes with sphere instances are always traversed in the reference's order.
+    bool needs_reference_order = false;
     uint64_t info[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace pico {
+// The traversal order a context uses on a scene.
+inline int scene_order(const pico_gpu_ctx* ctx, const pico_gpu_scene* scene)
+{
+    return scene->needs_reference_order ? PICO_ORDER_REFERENCE : ctx->order;
+}
 int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg);
 int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what);
 int take_device_status(pico_gpu_ctx* ctx, cudaStream_t stream);

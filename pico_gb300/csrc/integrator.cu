@@ -58,6 +58,8 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
             b.pay[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             b.rng[i] = rng.state;
             b.depth[i] = 0;
+            b.ior_n[i] = 1;   // Camera::generate_ray pushes 1.0 (Core/Camera.cpp:23)
+            b.ior_lo[i] = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         }
         const uint32_t at = warp_append(live, &b.counters[0]);
         if (live) b.queue[0][at] = i;
@@ -147,12 +149,26 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
                 b.pay[i] = pay;
             } else if (depth < max_depth) {
                 Pcg32 rng{b.rng[i]};
-                const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z);
+                const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z, b.org[i], dir);
                 const GpuInstanceShade is = sc.inst_shade[f.inst];
                 const GpuMaterial m = sc.materials[is.material];
                 const ex::V3 V = ex::v3(-dir.x, -dir.y, -dir.z);
                 auto next_xi = [&](float& a, float& c) { hammersley(rng, a, c); };
-                const BsdfSample smp = sample_bsdf(is.bsdf, m, V, f.n, next_xi);
+                // the path's index-of-refraction stack; only the BTDF lobes change it
+                const bool btdf = is.bsdf == PICO_BSDF_BTDF || is.bsdf == PICO_BSDF_FRESNEL;
+                IorStack ior;
+                ior.n = b.ior_n[i];
+                if (btdf) {
+                    const float4 lo = b.ior_lo[i], hi = b.ior_hi[i];
+                    ior.v[0] = lo.x; ior.v[1] = lo.y; ior.v[2] = lo.z; ior.v[3] = lo.w;
+                    ior.v[4] = hi.x; ior.v[5] = hi.y; ior.v[6] = hi.z; ior.v[7] = hi.w;
+                }
+                const BsdfSample smp = sample_bsdf(is.bsdf, m, V, f.n, next_xi, ior);
+                if (btdf) {
+                    b.ior_n[i] = ior.n;
+                    b.ior_lo[i] = make_float4(ior.v[0], ior.v[1], ior.v[2], ior.v[3]);
+                    b.ior_hi[i] = make_float4(ior.v[4], ior.v[5], ior.v[6], ior.v[7]);
+                }
                 if (is.bsdf == PICO_BSDF_LIGHT) {
                     pay.x = pay.x + thr.x * smp.energy.x;
                     pay.y = pay.y + thr.y * smp.energy.y;
@@ -162,7 +178,7 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
                 // counting as the last one (Integrators.cpp:54-76)
                 const uint32_t nl = sc.nlights + (sc.use_sun ? 1u : 0u);
                 uint32_t li = nl;
-                if (is.bsdf != PICO_BSDF_LIGHT && nl > 0) {
+                if (is.bsdf != PICO_BSDF_LIGHT && !btdf && nl > 0) {
                     li = (uint32_t)(rng.uniform() * (float)nl);
                     if (li >= nl) li = nl - 1;
                 }
@@ -177,20 +193,25 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
                     shadow = true;
                 } else if (li < sc.nlights) {
                     const GpuLight L = sc.lights[li];
-                    const uint32_t bucket = rng.next() % L.ntris;
-                    const float coin = (float)rng.next() / 4294967296.0f;
-                    const uint32_t t = coin <= sc.light_alias_weight[L.tri_base + bucket]
-                                           ? bucket
-                                           : sc.light_alias_index[L.tri_base + bucket];
-                    float x0, x1;
-                    hammersley(rng, x0, x1);
-                    const float su0 = ex::sqrt_(x0);
-                    const float bx = 1.0f - su0, by = x1 * su0;
-                    const float* lp = sc.light_positions + 9 * (size_t)(L.tri_base + t);
-                    const float w0 = (1.0f - bx) - by;
-                    const float sx = (w0 * lp[0] + bx * lp[3]) + by * lp[6];
-                    const float sy = (w0 * lp[1] + bx * lp[4]) + by * lp[7];
-                    const float sz = (w0 * lp[2] + bx * lp[5]) + by * lp[8];
+                    float sx, sy, sz;
+                    if (L.shape != PICO_SHAPE_TRIANGLES) {
+                        implicit_light_point(L.shape, rng, sx, sy, sz);
+                    } else {
+                        const uint32_t bucket = rng.next() % L.ntris;
+                        const float coin = (float)rng.next() / 4294967296.0f;
+                        const uint32_t t = coin <= sc.light_alias_weight[L.tri_base + bucket]
+                                               ? bucket
+                                               : sc.light_alias_index[L.tri_base + bucket];
+                        float x0, x1;
+                        hammersley(rng, x0, x1);
+                        const float su0 = ex::sqrt_(x0);
+                        const float bx = 1.0f - su0, by = x1 * su0;
+                        const float* lp = sc.light_positions + 9 * (size_t)(L.tri_base + t);
+                        const float w0 = (1.0f - bx) - by;
+                        sx = (w0 * lp[0] + bx * lp[3]) + by * lp[6];
+                        sy = (w0 * lp[1] + bx * lp[4]) + by * lp[7];
+                        sz = (w0 * lp[2] + bx * lp[5]) + by * lp[8];
+                    }
                     const float4* lip = reinterpret_cast<const float4*>(sc.insts + sc.inst_rank[L.inst]);
                     const float4 r0 = __ldg(lip + 3), r1 = __ldg(lip + 4), r2 = __ldg(lip + 5);
                     const ex::V3 spw = ex::v3(ex::row4(r0, sx, sy, sz, 1.0f), ex::row4(r1, sx, sy, sz, 1.0f),
@@ -216,7 +237,9 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
                         thr.y = (thr.y * iq) * (smp.P * smp.energy.y);
                         thr.z = (thr.z * iq) * (smp.P * smp.energy.z);
                         b.thr[i] = thr;
-                        b.org[i] = make_float4(f.px + 0.01f * f.n.x, f.py + 0.01f * f.n.y, f.pz + 0.01f * f.n.z,
+                        // offset along N, or -N inside a transparent object (Integrators.cpp:199)
+                        const float sgn = ior.inside() ? -0.01f : 0.01f;
+                        b.org[i] = make_float4(f.px + sgn * f.n.x, f.py + sgn * f.n.y, f.pz + sgn * f.n.z,
                                                f.pw + 0.0f);
                         b.dir[i] = make_float4(smp.L.x, smp.L.y, smp.L.z, dir.w);
                         b.depth[i] = depth + 1;
@@ -301,7 +324,7 @@ __global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView c
         if (s != kTraceOk) atomicOr(err, s);
         float n[3], pos[3], alb[3];
         if (s == kTraceOk && h.rank != kNoHit) {
-            const Fragment f = make_fragment(sc, h.rank, h.tri, h.u, h.v);
+            const Fragment f = make_fragment(sc, h.rank, h.tri, h.u, h.v, o, d);
             n[0] = f.n.x; n[1] = f.n.y; n[2] = f.n.z;
             const float* V = cam.view;
             for (int r = 0; r < 3; ++r)
@@ -364,10 +387,9 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         unsigned long long* tally = &status->rays[depth == 0 ? 0 : 1];
-        if (order == kReferenceOrder)
-            launch_extend<kReferenceOrder>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
-        else
-            launch_extend<kNearFirst>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
+        with_variant(order, sc, [&](auto v) {
+            launch_extend<decltype(v)::value>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
+        });
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
@@ -376,11 +398,10 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         if (depth < max_depth) {
             e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
             if (e != cudaSuccess) return e;
-            if (order == kReferenceOrder)
-                launch_extend<kReferenceOrder>(sc, b, b.shadow_queue, &b.counters[2], status, true, &status->rays[2],
-                                               st);
-            else
-                launch_extend<kNearFirst>(sc, b, b.shadow_queue, &b.counters[2], status, true, &status->rays[2], st);
+            with_variant(order, sc, [&](auto v) {
+                launch_extend<decltype(v)::value>(sc, b, b.shadow_queue, &b.counters[2], status, true,
+                                                  &status->rays[2], st);
+            });
         }
         cur ^= 1;
     }
@@ -392,12 +413,10 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st)
 {
-    if (order == kReferenceOrder)
-        gbuffer_kernel<kReferenceOrder><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions,
-                                                                             diffuse, &status->trace_error);
-    else
-        gbuffer_kernel<kNearFirst><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions, diffuse,
-                                                                        &status->trace_error);
+    with_variant(order, sc, [&](auto v) {
+        gbuffer_kernel<decltype(v)::value><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions,
+                                                                                 diffuse, &status->trace_error);
+    });
     return cudaGetLastError();
 }
 

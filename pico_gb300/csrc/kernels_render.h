@@ -26,6 +26,7 @@ struct PathBatch {
     float4* hit; uint32_t* hit_tri;
     unsigned long long* rng;
     uint32_t* depth;
+    uint32_t* ior_n; float4* ior_lo; float4* ior_hi;   // index-of-refraction stack: size, entries 0-3, 4-7
     float4* sorg; float4* sdir; float4* scontrib; float4* senergy;
     uint32_t* queue[2];
     uint32_t* shadow_queue;

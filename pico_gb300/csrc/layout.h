@@ -27,6 +27,8 @@
 #define PICO_REF_EMPTY 0x80000000u          // a leaf with no items (absent child)
 #define PICO_REF_END_BLAS 0xffffffffu       // stack sentinel: leave object space
 #define PICO_REF_DONE 0xfffffffeu           // traversal finished
+#define PICO_REF_SPHERE 0xfffffffdu         // BLAS root of the implicit radius-0.5 sphere
+#define PICO_REF_CUBE 0xfffffffcu           // BLAS root of the implicit [-0.5, 0.5]^3 cube
 #define PICO_LEAF_MAX 31u
 #define PICO_FIRST_MAX ((1u << 26) - 2u)
 
@@ -81,15 +83,15 @@ struct alignas(16) GpuInstanceShade {
 struct alignas(16) GpuMaterial {
     float diffuse[3], reflectance;
     float specular[3], roughness;
-    float emissive[3], pad;
+    float emissive[3], ior;   // index of refraction of a transparent material
 };
 
-// One NEE light: the instance and its triangle alias table.
+// One NEE light: the instance and its triangle alias table, or an implicit shape.
 struct alignas(16) GpuLight {
     uint32_t inst;        // original instance index
     uint32_t tri_base;    // first entry in the light-triangle arrays
     uint32_t ntris;
-    uint32_t pad;
+    uint32_t shape;       // pico_shape of the light's mesh
 };
 
 // What a kernel needs to walk the scene.
@@ -113,6 +115,7 @@ struct SceneView {
     float sky[3];
     uint32_t ninstances;
     uint32_t finite_boxes;              // every non-empty child box and both TLAS root boxes are finite
+    uint32_t has_implicit;              // some instance is an implicit sphere or cube
     uint32_t sky_kind, sky_w, sky_h;    // pico_sky_kind; texels per row / column (of a face)
     const void* sky_pixels;             // uchar4 cube faces or float4 equirectangular texels
     uint32_t use_sun;

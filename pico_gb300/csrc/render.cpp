@@ -71,13 +71,14 @@ T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }
 
 // Path state and image buffers owned by the context, grown on demand.
 struct RenderBuffers {
-    DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, sorg, sdir, scontrib, senergy, q0, q1, sq,
-        counters, samples;
+    DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, ior_n, ior_lo, ior_hi, sorg, sdir, scontrib, senergy,
+        q0, q1, sq, counters, samples;
     DeviceBuffer pixels, variance, count, taken, done, pix_list;
     DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
     ~RenderBuffers()
     {
-        for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &sorg, &sdir, &scontrib,
+        for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
+                                &sorg, &sdir, &scontrib,
                                 &senergy, &q0, &q1, &sq, &counters, &samples, &pixels, &variance, &count, &taken,
                                 &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out, &tonemap})
             b->release();
@@ -103,9 +104,9 @@ cudaError_t reserve_paths(RenderBuffers& r, size_t n)
 {
     cudaError_t e = cudaSuccess;
     for (DeviceBuffer* b : {&r.org, &r.dir, &r.thr, &r.pay, &r.hit, &r.sorg, &r.sdir, &r.scontrib, &r.senergy,
-                            &r.samples})
+                            &r.samples, &r.ior_lo, &r.ior_hi})
         if (e == cudaSuccess) e = b->reserve(n * sizeof(float4));
-    for (DeviceBuffer* b : {&r.hit_tri, &r.depth, &r.q0, &r.q1, &r.sq})
+    for (DeviceBuffer* b : {&r.hit_tri, &r.depth, &r.ior_n, &r.q0, &r.q1, &r.sq})
         if (e == cudaSuccess) e = b->reserve(n * sizeof(uint32_t));
     if (e == cudaSuccess) e = r.rng.reserve(n * sizeof(unsigned long long));
     if (e == cudaSuccess) e = r.counters.reserve(4 * sizeof(uint32_t));
@@ -190,6 +191,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
                 b.org = as<float4>(r.org); b.dir = as<float4>(r.dir); b.thr = as<float4>(r.thr);
                 b.pay = as<float4>(r.pay); b.hit = as<float4>(r.hit); b.hit_tri = as<uint32_t>(r.hit_tri);
                 b.rng = as<unsigned long long>(r.rng); b.depth = as<uint32_t>(r.depth);
+                b.ior_n = as<uint32_t>(r.ior_n); b.ior_lo = as<float4>(r.ior_lo); b.ior_hi = as<float4>(r.ior_hi);
                 b.sorg = as<float4>(r.sorg); b.sdir = as<float4>(r.sdir); b.scontrib = as<float4>(r.scontrib);
                 b.senergy = as<float4>(r.senergy); b.queue[0] = as<uint32_t>(r.q0); b.queue[1] = as<uint32_t>(r.q1);
                 b.shadow_queue = as<uint32_t>(r.sq); b.counters = as<uint32_t>(r.counters);
@@ -197,7 +199,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
                 b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
                 b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
                 e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
-                                        cfg->max_variance, ctx->status, ctx->order, st);
+                                        cfg->max_variance, ctx->status, scene_order(ctx, scene), st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
             }
@@ -211,7 +213,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
             if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
         if (e == cudaSuccess)
-            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, ctx->order, st);
+            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, scene_order(ctx, scene), st);
         if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
         status = run_atrous(ctx, r, as<float>(r.pixels), as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
                             as<float>(r.out), st);
@@ -266,7 +268,7 @@ int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, con
         if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
     if (e == cudaSuccess)
         e = launch_gbuffer(scene->view, make_camera_view(*camera), W, H, as<float>(r.gn), as<float>(r.gp),
-                           as<float>(r.gd), ctx->status, ctx->order, st);
+                           as<float>(r.gd), ctx->status, scene_order(ctx, scene), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(normals, r.gn.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(positions, r.gp.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(diffuse, r.gd.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);

@@ -358,6 +358,17 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
     std::vector<MeshRoot> roots(desc.nmeshes);
     for (uint32_t mi = 0; mi < desc.nmeshes; ++mi) {
         const pico_mesh& m = desc.meshes[mi];
+        if (m.shape != PICO_SHAPE_TRIANGLES) {
+            // the implicit assets have no BLAS: their bounds are [-0.5, 0.5]^3 with w = 1
+            // (LowerLevelImplicitShapesBVH.cpp:54-57, 66-68)
+            if (m.shape != PICO_SHAPE_SPHERE && m.shape != PICO_SHAPE_CUBE)
+                return "mesh " + std::to_string(mi) + ": unknown shape";
+            roots[mi].ref = m.shape == PICO_SHAPE_SPHERE ? PICO_REF_SPHERE : PICO_REF_CUBE;
+            roots[mi].box.lo = {-0.5f, -0.5f, -0.5f, 1.0f};
+            roots[mi].box.hi = {0.5f, 0.5f, 0.5f, 1.0f};
+            roots[mi].tri_base = 0;
+            continue;
+        }
         if (m.ntris && (!m.positions || !m.normals || !m.indices)) return "mesh " + std::to_string(mi) + " lacks arrays";
         for (uint64_t k = 0; k < 3ull * m.ntris; ++k)
             if (m.indices[k] >= m.nverts) return "mesh " + std::to_string(mi) + " index out of range";
@@ -410,14 +421,16 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         const pico_instance& in = desc.instances[i];
         if (in.mesh >= desc.nmeshes) return "instance " + std::to_string(i) + " names a missing mesh";
         if (in.material >= desc.nmaterials) return "instance " + std::to_string(i) + " names a missing material";
-        if (in.bsdf != PICO_BSDF_DIFFUSE && in.bsdf != PICO_BSDF_SPECULAR && in.bsdf != PICO_BSDF_DIELECTRIC &&
-            in.bsdf != PICO_BSDF_LIGHT)
-            return "instance " + std::to_string(i) + ": BSRDF kind not supported";
+        if (in.bsdf > PICO_BSDF_DELTA) return "instance " + std::to_string(i) + ": BSRDF kind not supported";
         mat4_inverse(in.transform, inverses[i].data());
         const pico_mesh& m = desc.meshes[in.mesh];
-        Box mb;
-        mb.lo = {m.aabb_min[0], m.aabb_min[1], m.aabb_min[2], 1.0f};
-        mb.hi = {m.aabb_max[0], m.aabb_max[1], m.aabb_max[2], 1.0f};
+        Box mb;   // LowerLevelBVH::get_bounds: the mesh AABB, or the implicit shape's box
+        if (m.shape != PICO_SHAPE_TRIANGLES) {
+            mb = roots[in.mesh].box;
+        } else {
+            mb.lo = {m.aabb_min[0], m.aabb_min[1], m.aabb_min[2], 1.0f};
+            mb.hi = {m.aabb_max[0], m.aabb_max[1], m.aabb_max[2], 1.0f};
+        }
         items[i].box = transform_box(mb, in.transform);
         items[i].value = i;
         fs.inst_shade[i] = GpuInstanceShade{in.bsdf, in.material, in.mesh, 0};
@@ -465,10 +478,16 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         const pico_mesh& m = desc.meshes[in.mesh];
         std::array<double, 6>& e = extent[i];
         e = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
-        if (work > 400000000ull || m.nverts == 0) continue;
+        const bool implicit = m.shape != PICO_SHAPE_TRIANGLES;   // bounded by its box's 8 corners
+        if (!implicit && (work > 400000000ull || m.nverts == 0)) continue;
+        static const float kCorners[8][3] = {{-0.5f, -0.5f, -0.5f}, {0.5f, -0.5f, -0.5f}, {-0.5f, 0.5f, -0.5f},
+                                             {0.5f, 0.5f, -0.5f},   {-0.5f, -0.5f, 0.5f}, {0.5f, -0.5f, 0.5f},
+                                             {-0.5f, 0.5f, 0.5f},   {0.5f, 0.5f, 0.5f}};
         const float* T = in.transform;
-        for (uint32_t v = 0; v < m.nverts; ++v) {
-            const double x = m.positions[3 * v], y = m.positions[3 * v + 1], z = m.positions[3 * v + 2];
+        const uint32_t nv = implicit ? 8u : m.nverts;
+        for (uint32_t v = 0; v < nv; ++v) {
+            const float* pv = implicit ? kCorners[v] : m.positions + 3 * v;
+            const double x = pv[0], y = pv[1], z = pv[2];
             for (int r = 0; r < 3; ++r) {
                 const double w = (double)T[0 * 4 + r] * x + (double)T[1 * 4 + r] * y + (double)T[2 * 4 + r] * z +
                                  (double)T[3 * 4 + r];
@@ -532,6 +551,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
             g.diffuse[a] = m.diffuse[a]; g.specular[a] = m.specular[a]; g.emissive[a] = m.emissive[a];
         }
         g.roughness = m.roughness;
+        g.ior = m.index_of_refraction;
         const float s = length3(m.specular), d = length3(m.diffuse);
         g.reflectance = s / (s + d);
         fs.materials[i] = g;
@@ -542,8 +562,12 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         const pico_instance& in = desc.instances[i];
         if (in.bsdf != PICO_BSDF_LIGHT) continue;
         const pico_mesh& m = desc.meshes[in.mesh];
+        if (m.shape != PICO_SHAPE_TRIANGLES) {   // sampled by the shape itself (sample_geometry)
+            fs.lights.push_back(GpuLight{i, 0, 0, m.shape});
+            continue;
+        }
         if (m.ntris == 0) return "light instance " + std::to_string(i) + " has an empty mesh";
-        GpuLight l{i, (uint32_t)fs.light_alias_weight.size(), m.ntris, 0};
+        GpuLight l{i, (uint32_t)fs.light_alias_weight.size(), m.ntris, PICO_SHAPE_TRIANGLES};
         std::vector<float> w(m.ntris);
         for (uint32_t t = 0; t < m.ntris; ++t) {
             const float* a = m.positions + 3 * m.indices[3 * t];

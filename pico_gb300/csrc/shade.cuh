@@ -21,6 +21,7 @@
 #include "exact_math.cuh"
 #include "kernels_render.h"
 #include "layout.h"
+#include "traverse.cuh"
 
 namespace pico {
 
@@ -230,11 +231,128 @@ struct BsdfSample {
     ex::V3 energy;
 };
 
-// BSRDF::sample; `xi` yields the Hammersley points the lobe consumes in the reference's order.
-template <class NextXi>
-__device__ __forceinline__ BsdfSample sample_bsdf(uint32_t kind, const GpuMaterial& m, ex::V3 V, ex::V3 N, NextXi&& next_xi)
+// Core::Ray's index-of-refraction stack (Core/AABB.cpp:54-81), 8 entries deep: a
+// camera path starts with 1.0 and each Transparent_BTDF sample pushes the
+// material's IoR on entering or pops on leaving.  Entries past the eighth are
+// counted but not stored; popping an empty stack is ignored and reading one gives
+// 1.0 (both undefined in the reference).
+constexpr uint32_t kIorDepth = 8;
+struct IorStack {
+    float v[kIorDepth];
+    uint32_t n;
+    __device__ __forceinline__ void push(float x) { if (n < kIorDepth) v[n] = x; ++n; }
+    __device__ __forceinline__ void pop() { if (n) --n; }
+    __device__ __forceinline__ float top() const { return n ? v[(n < kIorDepth ? n : kIorDepth) - 1] : 1.0f; }
+    __device__ __forceinline__ bool inside() const { return n > 1; }
+};
+
+// glm::refract (glm/detail/func_geometric.inl:119-127); the product with (k >= 0)
+// keeps sqrt's NaN, so total internal reflection yields a NaN direction.
+__device__ __forceinline__ ex::V3 refract3(ex::V3 I, ex::V3 N, float eta)
 {
     using namespace ex;
+    const float d = dot(N, I);
+    const float k = sub(1.0f, mul(mul(eta, eta), sub(1.0f, mul(d, d))));
+    const float s = add(mul(eta, d), sqrt_(k));
+    const float g = (float)(k >= 0.0f);
+    return v3(mul(sub(mul(eta, I.x), mul(s, N.x)), g), mul(sub(mul(eta, I.y), mul(s, N.y)), g),
+              mul(sub(mul(eta, I.z), mul(s, N.z)), g));
+}
+
+// Transparent_BTDF::sample (Render/BSRDF.cpp:238-297).
+template <class NextXi>
+__device__ __forceinline__ BsdfSample transparent_sample(const GpuMaterial& m, ex::V3 V, ex::V3 N, IorStack& ior,
+                                                         NextXi&& next_xi)
+{
+    using namespace ex;
+    const M3 w2t = tangent_frame(V, N);
+    const M3 t2w = m3_inverse(w2t);
+    const V3 vt = normalize(m3_mul(w2t, V));
+    const bool enter = vt.z >= 0.0f;
+    float x0, x1;
+    next_xi(x0, x1);
+    const V3 H = beckmann_sample(x0, x1, vt, m.roughness);
+    const float eta = div(1.0f, m.ior);
+    if (enter) ior.push(m.ior); else ior.pop();
+    const V3 L = refract3(vt, H, eta);
+    BsdfSample s;
+    s.L = normalize(m3_mul(t2w, L));
+    const float pdf = beckmann_pdf(H, m.roughness);
+    const V3 wh = normalize(vadd(vt, vscale(L, eta)));
+    const float denom = add(dot(vt, wh), mul(eta, dot(L, wh)));
+    const float dwh_dwi = fabsf(div(mul(mul(eta, eta), dot(L, wh)), mul(denom, denom)));
+    s.P = mul(pdf, dwh_dwi);
+    s.energy = v3(m.diffuse[0], m.diffuse[1], m.diffuse[2]);
+    return s;
+}
+
+// Fresnel_BTDF::fresnel_factor (Render/BSRDF.cpp:395-421).
+__device__ __forceinline__ float fresnel_factor(float cos_i, float eta_i, float eta_t)
+{
+    using namespace ex;
+    cos_i = clampf(cos_i, -1.0f, 1.0f);
+    if (!(cos_i > 0.0f)) {
+        const float tmp = eta_i; eta_i = eta_t; eta_t = tmp;
+        cos_i = fabsf(cos_i);
+    }
+    const float a = sub(1.0f, mul(cos_i, cos_i));
+    const float sin_i = sqrt_((0.0f < a) ? a : 0.0f);
+    const float sin_t = mul(div(eta_i, eta_t), sin_i);
+    const float b = sub(1.0f, mul(sin_t, sin_t));
+    const float cos_t = sqrt_((0.0f < b) ? b : 0.0f);
+    const float rparl = div(sub(mul(eta_t, cos_i), mul(eta_i, cos_t)), add(mul(eta_t, cos_i), mul(eta_i, cos_t)));
+    const float rperp = div(sub(mul(eta_i, cos_i), mul(eta_t, cos_t)), add(mul(eta_i, cos_i), mul(eta_t, cos_t)));
+    return div(add(mul(rparl, rparl), mul(rperp, rperp)), 2.0f);
+}
+
+// Specular_BRDF::sample (Render/BSRDF.cpp:54-84).
+template <class NextXi>
+__device__ __forceinline__ BsdfSample specular_sample(const GpuMaterial& m, ex::V3 V, ex::V3 N, NextXi&& next_xi)
+{
+    using namespace ex;
+    const M3 w2t = tangent_frame(V, N);
+    const M3 t2w = m3_inverse(w2t);
+    const V3 vt = normalize(m3_mul(w2t, V));
+    float x0, x1;
+    next_xi(x0, x1);
+    const V3 H = beckmann_sample(x0, x1, vt, m.roughness);
+    const V3 L = normalize(reflect3(vneg(vt), H));
+    BsdfSample s;
+    s.L = normalize(m3_mul(t2w, L));
+    s.P = bsdf_pdf(PICO_BSDF_SPECULAR, vt, H, m.roughness, m.reflectance);
+    s.energy = v3(m.specular[0], m.specular[1], m.specular[2]);
+    return s;
+}
+
+// BSRDF::sample; `xi` yields the Hammersley points the lobe consumes in the reference's order.
+template <class NextXi>
+__device__ __forceinline__ BsdfSample sample_bsdf(uint32_t kind, const GpuMaterial& m, ex::V3 V, ex::V3 N, NextXi&& next_xi,
+                                                  IorStack& ior)
+{
+    using namespace ex;
+    if (kind == PICO_BSDF_DELTA) {   // Specular_Delta_BRDF (Render/BSRDF.cpp:216-229)
+        BsdfSample s;
+        s.energy = v3(m.specular[0], m.specular[1], m.specular[2]);
+        s.L = reflect3(vneg(V), N);
+        s.P = 1.0f;
+        return s;
+    }
+    if (kind == PICO_BSDF_BTDF) return transparent_sample(m, V, N, ior, next_xi);
+    if (kind == PICO_BSDF_FRESNEL) {   // Fresnel_BTDF::sample (Render/BSRDF.cpp:364-385)
+        const M3 fw = tangent_frame(V, N);
+        const V3 fvt = normalize(m3_mul(fw, V));
+        float f0, f1;
+        next_xi(f0, f1);
+        const float F = fresnel_factor(fvt.z, m.ior, ior.top());
+        if (f0 < F) {
+            BsdfSample s = specular_sample(m, V, N, next_xi);
+            s.P = mul(s.P, F);
+            return s;
+        }
+        BsdfSample s = transparent_sample(m, V, N, ior, next_xi);
+        s.P = mul(s.P, sub(1.0f, F));
+        return s;
+    }
     const M3 w2t = tangent_frame(V, N);
     const M3 t2w = m3_inverse(w2t);
     const V3 vt = normalize(m3_mul(w2t, V));
@@ -248,12 +366,7 @@ __device__ __forceinline__ BsdfSample sample_bsdf(uint32_t kind, const GpuMateri
         s.energy = kind == PICO_BSDF_DIFFUSE ? v3(m.diffuse[0], m.diffuse[1], m.diffuse[2])
                                              : v3(m.emissive[0], m.emissive[1], m.emissive[2]);
     } else if (kind == PICO_BSDF_SPECULAR) {
-        next_xi(x0, x1);
-        const V3 H = beckmann_sample(x0, x1, vt, m.roughness);
-        const V3 L = normalize(reflect3(vneg(vt), H));
-        s.L = normalize(m3_mul(t2w, L));
-        s.P = bsdf_pdf(PICO_BSDF_SPECULAR, vt, H, m.roughness, m.reflectance);
-        s.energy = v3(m.specular[0], m.specular[1], m.specular[2]);
+        return specular_sample(m, V, N, next_xi);
     } else {
         next_xi(x0, x1);
         if (x1 >= m.reflectance) {
@@ -281,6 +394,42 @@ __device__ __forceinline__ float direct_lighting_pdf(uint32_t kind, const GpuMat
     const V3 two = m3_mul(t, wo);
     const V3 H = m3_mul(t, normalize(vadd(wi, wo)));
     return bsdf_pdf(kind, two, H, m.roughness, m.reflectance);
+}
+
+// ---------------------------------------------------------------- implicit lights
+// sample_geometry of the implicit assets (Core/LowerLevelImplicitShapesBVH.cpp:59-67,
+// 93-112): a uniform point on the radius-0.5 sphere (uniform_sample_sphere,
+// Core/RandUtils.cpp:43-49) or on a face of the unit cube (a random corner, a random
+// axis whose face offset is zero, two uniform offsets).
+__device__ __forceinline__ void implicit_light_point(uint32_t shape, Pcg32& rng, float& x, float& y, float& z)
+{
+    using namespace ex;
+    float a0, a1;
+    hammersley(rng, a0, a1);
+    if (shape == PICO_SHAPE_SPHERE) {
+        const float zz = sub(1.0f, mul(2.0f, a0));
+        const float q = sub(1.0f, mul(zz, zz));
+        const float r = sqrt_((0.0f < q) ? q : 0.0f);
+        const float phi = (float)(2.0 * kPi * (double)a1);
+        x = mul(0.5f, mul(r, cosf(phi)));
+        y = mul(0.5f, mul(r, sinf(phi)));
+        z = mul(0.5f, zz);
+        return;
+    }
+    float b0, b1, c0, c1;
+    hammersley(rng, b0, b1);
+    hammersley(rng, c0, c1);
+    const float c[3] = {sub(a0, 0.5f), sub(a1, 0.5f), sub(b0, 0.5f)};
+    float corner[3], face[3];
+    for (int a = 0; a < 3; ++a) corner[a] = (float)((0.0f < c[a]) - (c[a] < 0.0f));
+    uint32_t zero_axis = (uint32_t)mul(b1, 3.0f);
+    if (zero_axis >= 3) zero_axis = 2;
+    face[zero_axis] = 0.0f;
+    face[(zero_axis + 1) % 3] = c0;
+    face[(zero_axis + 2) % 3] = c1;
+    x = add(mul(corner[0], 0.5f), mul(-corner[0], face[0]));
+    y = add(mul(corner[1], 0.5f), mul(-corner[1], face[1]));
+    z = add(mul(corner[2], 0.5f), mul(-corner[2], face[2]));
 }
 
 // ---------------------------------------------------------------- sky
@@ -346,10 +495,38 @@ struct Fragment {
     uint32_t inst;          // original instance index
 };
 
-// interpolate_fragment + lower_level_intersector's world transform for a hit.
-__device__ __forceinline__ Fragment make_fragment(const SceneView& sc, uint32_t rank, uint32_t tri, float u, float v)
+// interpolate_fragment + lower_level_intersector's world transform for a hit; an
+// implicit hit (tri = kImplicitTri, object-space t in u) is rebuilt from the ray o, d.
+__device__ __forceinline__ Fragment make_fragment(const SceneView& sc, uint32_t rank, uint32_t tri, float u, float v,
+                                                  const float4 o, const float4 d)
 {
     using namespace ex;
+    if (tri == kImplicitTri) {
+        const ObjectRay q = to_object(sc.insts + rank, o, d);
+        const float t = u;
+        float px, py, pz;
+        V3 nobj;
+        if (__float_as_uint(q.root_lo.w) == PICO_REF_SPHERE) {   // N = normalize(P.xyz)
+            px = add(q.ox, mul(t, q.dx)); py = add(q.oy, mul(t, q.dy)); pz = add(q.oz, mul(t, q.dz));
+            nobj = normalize(v3(px, py, pz));
+        } else {   // the cube: the sign of the largest |component| (maximum_component_index)
+            px = add(q.ox, mul(q.dx, t)); py = add(q.oy, mul(q.dy, t)); pz = add(q.oz, mul(q.dz, t));
+            const float ax = px >= 0.0f ? px : -px, ay = py >= 0.0f ? py : -py, az = pz >= 0.0f ? pz : -pz;
+            const int k = (ax >= ay && ax >= az) ? 0 : ((ay >= ax && ay >= az) ? 1 : 2);
+            const float pk = k == 0 ? px : (k == 1 ? py : pz);
+            const float sg = (float)((0.0f < pk) - (pk < 0.0f));
+            nobj = v3(k == 0 ? sg : 0.0f, k == 1 ? sg : 0.0f, k == 2 ? sg : 0.0f);
+        }
+        const float4* ip = reinterpret_cast<const float4*>(sc.insts + rank);
+        const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
+        Fragment f;
+        f.px = row4(f0, px, py, pz, 1.0f); f.py = row4(f1, px, py, pz, 1.0f);
+        f.pz = row4(f2, px, py, pz, 1.0f); f.pw = row4(f3, px, py, pz, 1.0f);
+        f.n = normalize(v3(row3(f0, nobj.x, nobj.y, nobj.z), row3(f1, nobj.x, nobj.y, nobj.z),
+                           row3(f2, nobj.x, nobj.y, nobj.z)));
+        f.inst = sc.insts[rank].inst_id;
+        return f;
+    }
     const float4* tp = reinterpret_cast<const float4*>(sc.tris + tri);
     const float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
     const float4* np = reinterpret_cast<const float4*>(sc.tri_shade + tri);

@@ -20,7 +20,7 @@ __device__ __forceinline__ void write_hit(const SceneView& sc, const TraceHit& h
     pico_hit r;
     if (h.rank != kNoHit && s == kTraceOk) {
         r.inst = sc.insts[h.rank].inst_id;
-        r.prim = sc.tris[h.tri].prim;
+        r.prim = h.tri == kImplicitTri ? kImplicitTri : sc.tris[h.tri].prim;
         r.t = h.t; r.u = h.u; r.v = h.v;
     } else {
         r.inst = kNoHit; r.prim = kNoHit;
@@ -101,11 +101,11 @@ cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, 
     cudaError_t e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), stream);
     if (e != cudaSuccess || n == 0) return e;
     const float4* r = reinterpret_cast<const float4*>(rays);
-    if (order == kReferenceOrder)
-        return count ? launch_trace_t<true, kReferenceOrder>(sc, r, n, hits, status, stream)
-                     : launch_trace_t<false, kReferenceOrder>(sc, r, n, hits, status, stream);
-    return count ? launch_trace_t<true, kNearFirst>(sc, r, n, hits, status, stream)
-                 : launch_trace_t<false, kNearFirst>(sc, r, n, hits, status, stream);
+    return with_variant(order, sc, [&](auto v) {
+        constexpr int V = decltype(v)::value;
+        return count ? launch_trace_t<true, V>(sc, r, n, hits, status, stream)
+                     : launch_trace_t<false, V>(sc, r, n, hits, status, stream);
+    });
 }
 
 }  // namespace pico

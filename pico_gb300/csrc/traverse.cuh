@@ -23,17 +23,20 @@
 
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace pico {
 
 constexpr int kTraceStack = 96;
 constexpr uint32_t kTraceMaxIter = 1u << 24;
 constexpr uint32_t kNoHit = 0xffffffffu;
+constexpr uint32_t kImplicitTri = 0xfffffffeu;   // TraceHit::tri of a hit on an implicit shape
 
 struct TraceHit {
     float t;          // world distance, +inf on a miss
     uint32_t rank;    // TLAS rank of the instance
-    uint32_t tri;     // global triangle slot
-    float u, v;
+    uint32_t tri;     // global triangle slot, or kImplicitTri
+    float u, v;       // barycentrics; an implicit hit keeps its object-space t in u
 };
 
 struct TraceCounters {
@@ -123,6 +126,14 @@ __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, 
 // choice.
 enum TraversalOrder : int { kNearFirst = 0, kReferenceOrder = 1 };
 
+// Kernel variants: a traversal order, plus kWithImplicit when the scene holds implicit
+// shapes (the instance-entry check for them is compiled out otherwise).
+constexpr int kWithImplicit = 2;
+__host__ __device__ constexpr int traversal_variant(int order, bool implicit)
+{
+    return (order == kReferenceOrder ? kReferenceOrder : kNearFirst) | (implicit ? kWithImplicit : 0);
+}
+
 // Object-space ray of an instance (transform_ray, Core/AABB.cpp:43-52) and its BLAS root.
 struct ObjectRay {
     float ox, oy, oz, dx, dy, dz, ix, iy, iz;
@@ -143,6 +154,69 @@ __device__ __forceinline__ ObjectRay to_object(const GpuInstance* inst, const fl
     return r;
 }
 
+// |T * (p, 1) - O| as a 4-vector (Core/UpperLevelBVH.cpp:70-73).
+__device__ __forceinline__ float world_distance_at(const SceneView& sc, uint32_t rank, float px, float py, float pz,
+                                                   const float4 o)
+{
+    using namespace ex;
+    const float4* ip = reinterpret_cast<const float4*>(sc.insts + rank);
+    const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
+    const float ex_ = sub(row4(f0, px, py, pz, 1.0f), o.x), ey = sub(row4(f1, px, py, pz, 1.0f), o.y);
+    const float ez = sub(row4(f2, px, py, pz, 1.0f), o.z), ew = sub(row4(f3, px, py, pz, 1.0f), o.w);
+    return sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
+}
+
+// Object-space hit of an implicit asset: LowerLevelSphereBVH::calculate_intersection
+// (radius 0.5; a ray starting inside hits at t = 0) and LowerLevelCube's slab test
+// (Core/LowerLevelImplicitShapesBVH.cpp:24-52, 71-91).  Returns the ray parameter t
+// and the hit point.
+__device__ __forceinline__ bool implicit_hit(uint32_t root, const ObjectRay& q, float& t, float& px, float& py,
+                                             float& pz)
+{
+    using namespace ex;
+    if (root == PICO_REF_SPHERE) {
+        const V3 m = v3(q.ox, q.oy, q.oz);
+        const float b = dot(m, v3(q.dx, q.dy, q.dz));
+        const float c = sub(dot(m, m), 0.25f);
+        if (c > 0.0f && b > 0.0f) return false;
+        const float discr = sub(mul(b, b), c);
+        if (discr < 0.0f) return false;
+        t = (float)(-(double)b - sqrt((double)discr));
+        if (t < 0.0f) t = 0.0f;
+        px = add(q.ox, mul(t, q.dx)); py = add(q.oy, mul(t, q.dy)); pz = add(q.oz, mul(t, q.dz));
+        return true;
+    }
+    bool h;
+    const float tm = slab(-0.5f, 0.5f, -0.5f, 0.5f, -0.5f, 0.5f, q.ox, q.oy, q.oz, q.ix, q.iy, q.iz, h);
+    if (!h || tm == __int_as_float(0x7f800000)) return false;
+    t = tm;
+    px = add(q.ox, mul(q.dx, t)); py = add(q.oy, mul(q.dy, t)); pz = add(q.oz, mul(q.dz, t));
+    return true;
+}
+
+// The candidate of an implicit instance: its world distance and object-space t.
+// Kept out of line so the traversal loop does not pay registers for the rare case.
+static __device__ __noinline__ bool implicit_candidate(const GpuInstance* inst, const float4 o, const float4 d, float& tw,
+                                                float& t)
+{
+    const ObjectRay q = to_object(inst, o, d);
+    float px, py, pz;
+    if (!implicit_hit(__float_as_uint(q.root_lo.w), q, t, px, py, pz)) return false;
+    using namespace ex;
+    const float4* ip = reinterpret_cast<const float4*>(inst);
+    const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
+    const float ex_ = sub(row4(f0, px, py, pz, 1.0f), o.x), ey = sub(row4(f1, px, py, pz, 1.0f), o.y);
+    const float ez = sub(row4(f2, px, py, pz, 1.0f), o.z), ew = sub(row4(f3, px, py, pz, 1.0f), o.w);
+    tw = sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
+    return true;
+}
+
+__device__ __forceinline__ bool is_implicit_root(const GpuInstance* inst)
+{
+    const uint32_t root = __ldg(&inst->root_ref);
+    return root == PICO_REF_SPHERE || root == PICO_REF_CUBE;
+}
+
 // World distance of an instance's closest triangle: |T * interpolate(u, v) - O|
 // as a 4-vector (Core/LowerLevelMeshBVH.cpp:134-163, Core/UpperLevelBVH.cpp:70-73).
 __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t rank, uint32_t tri, float u, float v,
@@ -155,14 +229,10 @@ __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t ra
     const float px = add(add(mul(w, a.x), mul(u, b.x)), mul(v, c.x));
     const float py = add(add(mul(w, a.y), mul(u, b.y)), mul(v, c.y));
     const float pz = add(add(mul(w, a.z), mul(u, b.z)), mul(v, c.z));
-    const float4* ip = reinterpret_cast<const float4*>(sc.insts + rank);
-    const float4 f0 = __ldg(ip + 3), f1 = __ldg(ip + 4), f2 = __ldg(ip + 5), f3 = __ldg(ip + 6);
-    const float ex_ = sub(row4(f0, px, py, pz, 1.0f), o.x), ey = sub(row4(f1, px, py, pz, 1.0f), o.y);
-    const float ez = sub(row4(f2, px, py, pz, 1.0f), o.z), ew = sub(row4(f3, px, py, pz, 1.0f), o.w);
-    return sqrt_(dot4(ex_, ey, ez, ew, ex_, ey, ez, ew));
+    return world_distance_at(sc, rank, px, py, pz, o);
 }
 
-template <bool kCount>
+template <bool kCount, bool kImplicit>
 __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
                                                 TraceCounters* cnt)
 {
@@ -275,6 +345,16 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             stack[sp++] = pico_leaf_ref(first + 1, count - 1);
         }
         if (kCount) cnt->insts++;
+        if (kImplicit && is_implicit_root(sc.insts + first)) {
+            // an implicit shape: one candidate, no BLAS and no root box test
+            float tw, t;
+            if (implicit_candidate(sc.insts + first, o, d, tw, t) &&
+                (tw < best.t || (tw == best.t && first < best.rank))) {
+                best.t = tw; best.rank = first; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+            }
+            ref = sp ? stack[--sp] : PICO_REF_DONE;
+            continue;
+        }
         q = to_object(sc.insts + first, o, d);
         gl = (best.t * 1.001f + omag) * inv_len;
         bool h;
@@ -299,7 +379,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // missed; -inf: nothing to test).
 struct StackEntry { uint32_t ref; float tmin; };
 
-template <bool kCount>
+template <bool kCount, bool kImplicit>
 __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const float4 o, const float4 d,
                                                      TraceHit& best, TraceCounters* cnt)
 {
@@ -384,6 +464,14 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             stack[sp++] = StackEntry{pico_leaf_ref(first + 1, count - 1), -kInf};
         }
         if (kCount) cnt->insts++;
+        if (kImplicit && is_implicit_root(sc.insts + first)) {
+            float tw, t;
+            if (implicit_candidate(sc.insts + first, o, d, tw, t) && tw < best.t) {
+                best.t = tw; best.rank = first; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+            }
+            ref = pop();
+            continue;
+        }
         q = to_object(sc.insts + first, o, d);
         bool h;
         const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
@@ -402,12 +490,25 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
     return kTraceOk;
 }
 
-template <bool kCount, int kOrder>
+template <bool kCount, int kVariant>
 __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
                                              TraceCounters* cnt)
 {
-    if (kOrder == kReferenceOrder) return trace_reference_order<kCount>(sc, o, d, best, cnt);
-    return trace_near_first<kCount>(sc, o, d, best, cnt);
+    constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
+    if ((kVariant & kReferenceOrder) != 0) return trace_reference_order<kCount, kImplicit>(sc, o, d, best, cnt);
+    return trace_near_first<kCount, kImplicit>(sc, o, d, best, cnt);
+}
+
+// Calls f(std::integral_constant<int, V>) for the kernel variant V of (order, scene).
+template <class F>
+__host__ auto with_variant(int order, const SceneView& sc, F&& f)
+{
+    switch (traversal_variant(order, sc.has_implicit != 0)) {
+    case 0: return f(std::integral_constant<int, 0>{});
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    default: return f(std::integral_constant<int, 3>{});
+    }
 }
 
 }  // namespace pico

@@ -6,6 +6,8 @@ Here the GPU result must equal the oracle's exactly: same instance, same
 triangle, same float bits for t, u and v.  Ties (equal distances) must resolve
 like the reference's depth-first first-found rule, which the tie scenes check.
 """
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -174,7 +176,36 @@ def test_scene_info(ctx):
 
 def test_unsupported_bsdf_is_rejected(ctx):
     s = scenes.cornell_box()
-    s.instances[0].bsdf = 3   # BTDF
+    s.instances[0].bsdf = 7   # past Specular_Delta_BRDF
     with pytest.raises(pico_gb300.PicoError) as e:
         ctx.upload(s)
     assert e.value.status == -8
+
+
+def test_implicit_spheres_and_cubes(ctx, oracle):
+    """LowerLevelSphereBVH / LowerLevelCube instances (scaled, rotated) among meshes:
+    both orders reproduce the oracle (and so the reference's golden hits) exactly,
+    including the object-space t an implicit hit reports in u."""
+    z = np.load(Path(__file__).resolve().parent / "golden" / "shapes.npz")
+    scene = scenes.cornell_shapes()
+    got, want = check(ctx, oracle, scene, z["rays"], "shapes")
+    np.testing.assert_array_equal(got["inst"], z["hit_inst"])
+    np.testing.assert_array_equal(got["prim"], z["hit_prim"])
+    hit = z["hit_inst"] != pico_gb300.MISS
+    np.testing.assert_array_equal(got["t"][hit].view(np.uint32), z["hit_t"][hit].view(np.uint32))
+    assert (got["prim"] == 0xFFFFFFFE).sum() > 1000
+
+
+def test_implicit_cubes_in_near_first_order(ctx, oracle):
+    """Cube instances alone keep the near-first walk: every cube hit lies inside its
+    instance's box along the ray, so near-first reproduces the reference."""
+    s = scenes.cornell_box()
+    cube = len(s.meshes)
+    s.meshes.append(scenes.implicit_mesh(pico_gb300.SHAPE_CUBE))
+    for k, (t, sc, rot) in enumerate([((0.3, 0.3, 0.4), 0.2, 15.0), ((0.7, 0.25, 0.6), 0.3, -40.0),
+                                      ((0.5, 0.75, 0.5), 0.15, 60.0)]):
+        m = scenes.translate(t) @ scenes.rotate_y(rot) @ scenes.scale(sc)
+        s.instances.append(Instance(cube, scenes.glm_storage(m), DIFFUSE, 0))
+    rays = random_rays(np.random.default_rng(5), 20000, 0.02, 0.98)
+    got, want = check(ctx, oracle, s, rays, "cubes")
+    assert (want["prim"] == 0xFFFFFFFE).sum() > 1000
