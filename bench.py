@@ -160,6 +160,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest rank's time (replicas: every rank traces the whole batch)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(units_per_rank: int, world: int, seconds: float) -> float:
+    """Whole-job throughput in millions of units per second: every rank processed its
+    own units in at most `seconds` (the max over ranks)."""
+    return world * units_per_rank / seconds / 1e6
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -271,6 +287,49 @@ def bench_atrous(ctx, args, torch, local):
                          "traffic": atrous_traffic_per_call()}}
 
 
+def bench_tonemap_and_hdr(ctx, args, torch, local):
+    """Reinhard tone mapping on a 1920x1080 device image (L2 flushed before each call;
+    algorithmic bytes: the white-point pass reads 12 B per pixel, the map reads and
+    writes 12 B each) and the Radiance .hdr encoder on the same image from host memory."""
+    W, H = 1920, 1080
+    rng = np.random.default_rng(6)
+    img = rng.gamma(1.0, 1.0, (H, W, 3)).astype(np.float32)
+    dev = f"cuda:{local}"
+    src = torch.from_numpy(img).to(dev)
+    buf = torch.empty_like(src)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(3):
+        buf.copy_(src)
+        ctx.check(ctx.lib.pico_gpu_tonemap_device(ctx.handle, buf.data_ptr(), W, H, stream.cuda_stream), "tonemap")
+    times = []
+    for _ in range(10):
+        buf.copy_(src)
+        flush.fill_(1)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.check(ctx.lib.pico_gpu_tonemap_device(ctx.handle, buf.data_ptr(), W, H, stream.cuda_stream), "tonemap")
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = float(np.mean(times))
+    algo = 36 * W * H
+    peak, src_ = measured_peaks()
+    tonemap = {"workload": "Reinhard tone map, 1920x1080, device buffer, L2 flushed before each call",
+               "ms_per_call": ms, "gpu_launches_per_call": 2,
+               "roofline": {"bound": "hbm", "achieved": algo / (ms / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                            "frac": algo / (ms / 1e3) / 1e9 / peak, "peak_source": src_,
+                            "algorithmic_bytes_per_call": algo}}
+    ctx.encode_hdr(img, W, H)   # warm-up
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        data = ctx.encode_hdr(img, W, H)
+    hdr = {"workload": "stbi_write_hdr-compatible RGBE + run-length encode of a 1920x1080 image, host buffers",
+           "ms_per_image": (time.perf_counter() - t0) / reps * 1e3, "file_bytes": len(data)}
+    return tonemap, hdr
+
+
 def atrous_traffic_per_call():
     """DRAM bytes of one 1080p a-trous call measured by ncu (profiles/atrous_1080p.md), if recorded."""
     p = ROOT / "profiles" / "atrous_1080p.md"
@@ -355,13 +414,11 @@ def main():
     gs.check(sh)
     per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
     total_ms = evs[0].elapsed_time(evs[-1])
+    total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
     if dist:
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
         dist.barrier()
     ms = total_ms / args.steps
-    value = world * n / (ms / 1e3) / 1e6
+    value = replica_throughput(n, world, ms / 1e3)
 
     # end to end from pinned host memory through the host-buffer entry point
     e2e = None
@@ -375,12 +432,8 @@ def main():
         t0 = time.perf_counter()
         for _ in range(args.steps):
             gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
-        e2e_s = (time.perf_counter() - t0) / args.steps
-        if dist:
-            t = torch.tensor([e2e_s], device=f"cuda:{local}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        e2e = {"value": world * n / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, f"cuda:{local}")
+        e2e = {"value": replica_throughput(n, world, e2e_s), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
                "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3}
 
     if rank != 0:
@@ -409,17 +462,19 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
-    render = atrous = None
+    render = atrous = tonemap = hdr = None
     if not args.no_render:
         gs.free()
         render = bench_render(ctx, args, torch, local)
         atrous = bench_atrous(ctx, args, torch, local)
+        tonemap, hdr = bench_tonemap_and_hdr(ctx, args, torch, local)
 
     line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clocks.summary(), "scene": info, "render_1080p": render, "atrous_1080p": atrous}
+            "clocks": clocks.summary(), "scene": info, "render_1080p": render, "atrous_1080p": atrous,
+            "tonemap_1080p": tonemap, "hdr_1080p": hdr}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

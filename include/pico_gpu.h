@@ -212,7 +212,7 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
  * must not allocate device memory during their denoise step: a frame loop that
  * overlaps streams (cudaFree, and often cudaMalloc, synchronises the whole
  * device) or a process whose device memory belongs to another allocator.  On
- * success it allocates nothing: its scratch is a fixed 48 MiB + 288 KiB device
+ * success it allocates nothing: its scratch is a fixed 48 MiB + 2.25 MiB device
  * array per device, so images are limited to 2,097,152 pixels (1920 x 1080
  * fits) and 65,535 rows; larger ones return PICO_ERR_INVALID_ARG with a
  * message.  All calls on a device share that array: calls that overlap on the

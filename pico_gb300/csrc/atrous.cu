@@ -33,7 +33,8 @@ __constant__ float kAtrousWeights[25] = {
     0.00292f, 0.01306f, 0.02154f, 0.01306f, 0.00292f};
 
 constexpr int kTile = 64;
-constexpr int kStatsThreads = 512;
+constexpr int kStatsThreads = 256;
+constexpr int kStatsSplit = 4;   // CTAs per tile; each reduces every fourth footprint row group
 constexpr int kMaxSpan = kTile + 4 * 16;   // tap footprint of a tile along one axis, spacing <= 16
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -77,11 +78,12 @@ __device__ __forceinline__ float luminance(float r, float g, float b)
 
 __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float* __restrict__ pix,
                                                                       const float* __restrict__ pos, uint32_t W,
-                                                                      uint32_t H, int s, float2* __restrict__ stats)
+                                                                      uint32_t H, int s, float4* __restrict__ parts)
 {
     using namespace ex;
     const int tiles_x = (int)((W + kTile - 1) / kTile);
-    const int tx = blockIdx.x % tiles_x, ty = blockIdx.x / tiles_x;
+    const int tile = (int)(blockIdx.x / kStatsSplit), part = (int)(blockIdx.x % kStatsSplit);
+    const int tx = tile % tiles_x, ty = tile / tiles_x;
     const int x0 = tx * kTile, y0 = ty * kTile;
     const int x1 = min(x0 + kTile, (int)W) - 1, y1 = min(y0 + kTile, (int)H) - 1;
     __shared__ int cols[kMaxSpan], rows[kMaxSpan];
@@ -94,13 +96,14 @@ __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float
     const int ncols = list_spans(span[0], span[1], nspan[0], cols);
     const int nrows = list_spans(span[2], span[3], nspan[1], rows);
     __syncthreads();
-    // maximum luminance and min / max |position| over the footprint; max / min are
-    // exact, so the visiting order is free, and the selects keep std::max / std::min's
-    // NaN behaviour
+    // maximum luminance and min / max |position| over this CTA's share of the
+    // footprint rows; max / min are exact, so the visiting order and the split are
+    // free, and the selects keep std::max / std::min's NaN behaviour
     const float kInf = __int_as_float(0x7f800000);
     float white = 0.0f, mind = kInf, maxd = -kInf;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = warp; r < nrows; r += kStatsThreads / 32) {
+    constexpr int kWarps = kStatsThreads / 32;
+    for (int r = part * kWarps + warp; r < nrows; r += kStatsSplit * kWarps) {
         const size_t rb = (size_t)rows[r] * W;
         for (int c = lane; c < ncols; c += 32) {
             const size_t f = rb + (size_t)cols[c];
@@ -119,17 +122,31 @@ __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float
         mind = (a2 < mind) ? a2 : mind;
         maxd = (maxd < b2) ? b2 : maxd;
     }
-    __shared__ float sw[kStatsThreads / 32], sa[kStatsThreads / 32], sb[kStatsThreads / 32];
+    __shared__ float sw[kWarps], sa[kWarps], sb[kWarps];
     if (lane == 0) { sw[warp] = white; sa[warp] = mind; sb[warp] = maxd; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < kStatsThreads / 32; ++w) {
+        for (int w = 1; w < kWarps; ++w) {
             white = (white < sw[w]) ? sw[w] : white;
             mind = (sa[w] < mind) ? sa[w] : mind;
             maxd = (maxd < sb[w]) ? sb[w] : maxd;
         }
-        stats[blockIdx.x] = make_float2(white, sub(maxd, mind));
+        parts[blockIdx.x] = make_float4(white, mind, maxd, 0.0f);
     }
+}
+
+// A tile's white point and |position| range from its kStatsSplit partial records.
+__device__ __forceinline__ float2 tile_stats(const float4* __restrict__ parts, int tile)
+{
+    float4 t = parts[tile * kStatsSplit];
+#pragma unroll
+    for (int k = 1; k < kStatsSplit; ++k) {
+        const float4 p = parts[tile * kStatsSplit + k];
+        t.x = (t.x < p.x) ? p.x : t.x;
+        t.y = (p.y < t.y) ? p.y : t.y;
+        t.z = (t.z < p.z) ? p.z : t.z;
+    }
+    return make_float2(t.x, __fsub_rn(t.z, t.y));
 }
 
 // One thread per pixel, 25 taps.  The reference's weight
@@ -145,13 +162,13 @@ __global__ void __launch_bounds__(256) atrous_blend_kernel(const float* __restri
                                                            const float* __restrict__ nrm,
                                                            const float* __restrict__ pos,
                                                            const float* __restrict__ dif, uint32_t W, uint32_t H,
-                                                           int s, const float2* __restrict__ stats,
+                                                           int s, const float4* __restrict__ stats,
                                                            float* __restrict__ dst)
 {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= W) return;
     const int tiles_x = (int)((W + kTile - 1) / kTile);
-    const float2 st = stats[(y / kTile) * tiles_x + x / kTile];
+    const float2 st = tile_stats(stats, (int)((y / kTile) * tiles_x + x / kTile));
     const float ip = __frcp_rn(__fmul_rn(st.y, st.y));   // 1 / range^2 (inf for a zero range)
     const float iw = __frcp_rn(__fmul_rn(st.x, st.x));   // 1 / white^2
     const Idx c = ((Idx)y * W + x) * 3;
@@ -188,24 +205,138 @@ __global__ void __launch_bounds__(256) atrous_blend_kernel(const float* __restri
     dst[c + 2] = __fdiv_rn(r2, wsum);
 }
 
+// The same blend with its taps staged in shared memory, for small spacings.  At
+// spacing s every tap of a pixel lands on the pixel's own sub-lattice (x mod s,
+// y mod s), so a CTA takes a kLatX x kLatY tile of one sub-lattice; the
+// (kLatX + 4) x (kLatY + 4) lattice points its taps read (coordinates clamped
+// exactly as the taps clamp them) are staged once as 48-byte records (normal,
+// position, albedo, colour) and read back with 128-bit loads.  Each thread blends
+// two horizontally adjacent lattice pixels, which share four of their five tap
+// columns; the records of a footprint row are split into even and odd columns so
+// that a warp's loads hit consecutive records.  The arithmetic per tap is the
+// direct kernel's above, so the two kernels give identical results.
+constexpr int kLatX = 64, kLatY = 8, kBlendThreads = (kLatX / 2) * kLatY;
+constexpr int kFootX = kLatX + 4, kHalfX = kFootX / 2, kFootY = kLatY + 4;
+
+__device__ __forceinline__ void blend_tap(const float4 t0, const float4 t1, const float4 t2, float k, const float* c,
+                                          float ip, float iw, float* acc)
+{
+    const float nx = c[0] - t0.x, ny = c[1] - t0.y, nz = c[2] - t0.z;
+    const float px = c[3] - t0.w, py = c[4] - t1.x, pz = c[5] - t1.y;
+    const float ax = c[6] - t1.z, ay = c[7] - t1.w, az = c[8] - t2.x;
+    const float dn = nx * nx + ny * ny + nz * nz;
+    const float dp = px * px + py * py + pz * pz;
+    const float da = ax * ax + ay * ay + az * az;
+    const float w = k * __expf(-(4.0f * dn + dp * ip + da * iw));
+    acc[0] += t2.y * w;
+    acc[1] += t2.z * w;
+    acc[2] += t2.w * w;
+    acc[3] += w;
+}
+
+template <typename Idx>
+__global__ void __launch_bounds__(kBlendThreads) atrous_blend_tiled_kernel(
+    const float* __restrict__ src, const float* __restrict__ nrm, const float* __restrict__ pos,
+    const float* __restrict__ dif, uint32_t W, uint32_t H, int s, const float4* __restrict__ stats,
+    float* __restrict__ dst)
+{
+    __shared__ float4 rec[kFootY * kFootX * 3];   // [row][column parity][column / 2] records
+    const int rx = (int)(blockIdx.x % (uint32_t)s), tx = (int)(blockIdx.x / (uint32_t)s);
+    const int ry = (int)(blockIdx.y % (uint32_t)s), ty = (int)(blockIdx.y / (uint32_t)s);
+    const int lx0 = tx * kLatX - 2, ly0 = ty * kLatY - 2;   // lattice coordinate of footprint entry (0, 0)
+    for (int e = threadIdx.x; e < kFootX * kFootY; e += blockDim.x) {
+        const int ex = e % kFootX, ey = e / kFootX;
+        const int x = clampi(rx + (lx0 + ex) * s, 0, (int)W - 1);
+        const int y = clampi(ry + (ly0 + ey) * s, 0, (int)H - 1);
+        const Idx f = ((Idx)y * W + (Idx)x) * 3;
+        const int slot = 3 * ((ey * 2 + (ex & 1)) * kHalfX + (ex >> 1));
+        rec[slot] = make_float4(__ldg(nrm + f), __ldg(nrm + f + 1), __ldg(nrm + f + 2), __ldg(pos + f));
+        rec[slot + 1] = make_float4(__ldg(pos + f + 1), __ldg(pos + f + 2), __ldg(dif + f), __ldg(dif + f + 1));
+        rec[slot + 2] = make_float4(__ldg(dif + f + 2), __ldg(src + f), __ldg(src + f + 1), __ldg(src + f + 2));
+    }
+    __syncthreads();
+    const int h = (int)(threadIdx.x % (kLatX / 2)), b = (int)(threadIdx.x / (kLatX / 2));
+    const int a = 2 * h;                                     // this thread's lattice pixels: a and a + 1
+    const int y = ry + (ty * kLatY + b) * s;
+    const int x0 = rx + (tx * kLatX + a) * s, x1 = x0 + s;
+    if (y >= (int)H || x0 >= (int)W) return;
+    const int tiles_x = (int)((W + kTile - 1) / kTile);
+    const int x1c = x1 < (int)W ? x1 : x0;
+    const float2 st0 = tile_stats(stats, (y / kTile) * tiles_x + x0 / kTile);
+    const float2 st1 = tile_stats(stats, (y / kTile) * tiles_x + x1c / kTile);
+    const float ip0 = __frcp_rn(__fmul_rn(st0.y, st0.y)), iw0 = __frcp_rn(__fmul_rn(st0.x, st0.x));
+    const float ip1 = __frcp_rn(__fmul_rn(st1.y, st1.y)), iw1 = __frcp_rn(__fmul_rn(st1.x, st1.x));
+    float c0[9], c1[9];
+    {
+        const int r0 = 3 * (((b + 2) * 2 + 0) * kHalfX + h + 1);   // column a + 2 (even)
+        const int r1 = 3 * (((b + 2) * 2 + 1) * kHalfX + h + 1);   // column a + 3 (odd)
+        const float4 p0 = rec[r0], p1 = rec[r0 + 1], p2 = rec[r0 + 2];
+        const float4 q0 = rec[r1], q1 = rec[r1 + 1], q2 = rec[r1 + 2];
+        c0[0] = p0.x; c0[1] = p0.y; c0[2] = p0.z; c0[3] = p0.w; c0[4] = p1.x; c0[5] = p1.y;
+        c0[6] = p1.z; c0[7] = p1.w; c0[8] = p2.x;
+        c1[0] = q0.x; c1[1] = q0.y; c1[2] = q0.z; c1[3] = q0.w; c1[4] = q1.x; c1[5] = q1.y;
+        c1[6] = q1.z; c1[7] = q1.w; c1[8] = q2.x;
+    }
+    float acc0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, acc1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {   // footprint column a + q
+            const int r = 3 * (((b + j) * 2 + (q & 1)) * kHalfX + h + (q >> 1));
+            const float4 t0 = rec[r], t1 = rec[r + 1], t2 = rec[r + 2];
+            if (q <= 4) blend_tap(t0, t1, t2, kAtrousWeights[j * 5 + q], c0, ip0, iw0, acc0);
+            if (q >= 1) blend_tap(t0, t1, t2, kAtrousWeights[j * 5 + q - 1], c1, ip1, iw1, acc1);
+        }
+    }
+    const Idx o0 = ((Idx)y * W + (Idx)x0) * 3;
+    dst[o0] = __fdiv_rn(acc0[0], acc0[3]);
+    dst[o0 + 1] = __fdiv_rn(acc0[1], acc0[3]);
+    dst[o0 + 2] = __fdiv_rn(acc0[2], acc0[3]);
+    if (x1 < (int)W) {
+        const Idx o1 = ((Idx)y * W + (Idx)x1) * 3;
+        dst[o1] = __fdiv_rn(acc1[0], acc1[3]);
+        dst[o1 + 1] = __fdiv_rn(acc1[1], acc1[3]);
+        dst[o1 + 2] = __fdiv_rn(acc1[2], acc1[3]);
+    }
+}
+
+// Spacings up to this use the tiled blend; wider ones gather their staged lattice
+// points from scattered sectors and run faster as the direct kernel.
+constexpr int kTiledMaxSpacing = 4;
+
 cudaError_t launch_atrous(const float* pixels, const float* normals, const float* positions, const float* diffuse,
                           uint32_t W, uint32_t H, float* scratch_a, float* scratch_b, float* tile_stats, float* out,
                           cudaStream_t st)
 {
     if (W == 0 || H == 0) return cudaSuccess;
     const uint32_t tiles = ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
-    float2* stats = reinterpret_cast<float2*>(tile_stats);
+    float4* stats = reinterpret_cast<float4*>(tile_stats);
     const float* src = pixels;
     for (int level = 0; level < 5; ++level) {
         // ping-pong: in -> A -> B -> A -> B -> out
         float* dst = level == 4 ? out : ((level % 2 == 0) ? scratch_a : scratch_b);
         const int s = 1 << level;
-        atrous_stats_kernel<<<tiles, kStatsThreads, 0, st>>>(src, positions, W, H, s, stats);
-        dim3 grid((W + 255) / 256, H);
-        if ((uint64_t)W * H * 3 < (1ull << 32))
-            atrous_blend_kernel<uint32_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats, dst);
-        else
-            atrous_blend_kernel<size_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats, dst);
+        atrous_stats_kernel<<<tiles * kStatsSplit, kStatsThreads, 0, st>>>(src, positions, W, H, s, stats);
+        const bool small = (uint64_t)W * H * 3 < (1ull << 32);
+        if (s <= kTiledMaxSpacing) {
+            // one CTA per kLatX x kLatY tile of each of the s x s sub-lattices
+            const uint32_t lw = (W + s - 1) / s, lh = (H + s - 1) / s;
+            dim3 grid(((lw + kLatX - 1) / kLatX) * s, ((lh + kLatY - 1) / kLatY) * s);
+            if (small)
+                atrous_blend_tiled_kernel<uint32_t><<<grid, kBlendThreads, 0, st>>>(src, normals, positions, diffuse,
+                                                                                   W, H, s, stats, dst);
+            else
+                atrous_blend_tiled_kernel<size_t><<<grid, kBlendThreads, 0, st>>>(src, normals, positions, diffuse, W,
+                                                                                 H, s, stats, dst);
+        } else {
+            dim3 grid((W + 255) / 256, H);
+            if (small)
+                atrous_blend_kernel<uint32_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats,
+                                                                    dst);
+            else
+                atrous_blend_kernel<size_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats,
+                                                                  dst);
+        }
         src = dst;
     }
     return cudaGetLastError();

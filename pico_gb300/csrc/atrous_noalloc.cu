@@ -17,7 +17,7 @@
 //   * at most kNoAllocMaxPixels = 2,097,152 pixels (1920 x 1080 fits) and
 //     65,535 rows per call; larger images are rejected with
 //     PICO_ERR_INVALID_ARG and a message in the context, before any launch;
-//   * the array takes 48 MiB + 288 KiB of device memory on each device;
+//   * the array takes 48 MiB + 2.25 MiB of device memory on each device;
 //   * every call on a device shares that one array, so calls whose kernels
 //     overlap on the GPU (different streams, or different host threads) race
 //     and corrupt each other's output: order them on one stream or with events;
@@ -38,12 +38,12 @@ constexpr size_t kNoAllocMaxPixels = size_t(1) << 21;
 constexpr uint32_t kNoAllocMaxRows = 65535;            // the blend kernel's grid.y
 constexpr size_t kNoAllocMaxTiles = 36864;             // 64 x 64 tiles; 2^21 pixels need at most 32,768
 constexpr size_t kNoAllocImageFloats = 3 * kNoAllocMaxPixels;
-constexpr size_t kNoAllocFloats = 2 * kNoAllocImageFloats + 2 * kNoAllocMaxTiles;
+constexpr size_t kNoAllocFloats = 2 * kNoAllocImageFloats + pico::kAtrousStatsFloatsPerTile * kNoAllocMaxTiles;
 constexpr int kNoAllocMaxDevices = 64;
 
 }  // namespace
 
-// Ping-pong image A, ping-pong image B, then the per-tile (float2) statistics.
+// Ping-pong image A, ping-pong image B, then the per-tile statistics records (float4).
 static __device__ __align__(256) float pico_atrous_noalloc_scratch[kNoAllocFloats];
 
 namespace {

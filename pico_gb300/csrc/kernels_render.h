@@ -41,6 +41,9 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
                                 DeviceStatus* status, int order, cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
+// Floats of a-trous scratch per 64 x 64 tile: four partial statistics records
+// (white point, min |position|, max |position|, unused) per level.
+constexpr size_t kAtrousStatsFloatsPerTile = 16;
 cudaError_t launch_atrous(const float* pixels, const float* normals, const float* positions, const float* diffuse,
                           uint32_t W, uint32_t H, float* scratch_a, float* scratch_b, float* tile_stats, float* out,
                           cudaStream_t st);

@@ -120,7 +120,7 @@ int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const fl
     const size_t tiles = (size_t)((W + 63) / 64) * ((H + 63) / 64);
     cudaError_t e = r.ga.reserve(n * sizeof(float));
     if (e == cudaSuccess) e = r.gb.reserve(n * sizeof(float));
-    if (e == cudaSuccess) e = r.stats.reserve(tiles * 2 * sizeof(float));
+    if (e == cudaSuccess) e = r.stats.reserve(tiles * kAtrousStatsFloatsPerTile * sizeof(float));
     if (e == cudaSuccess)
         e = launch_atrous(d_pix, d_n, d_p, d_d, W, H, as<float>(r.ga), as<float>(r.gb), as<float>(r.stats), d_out, st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous");
