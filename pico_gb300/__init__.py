@@ -150,11 +150,11 @@ class Context:
         """stbi_write_hdr's file image of `pixels` (no reversal)."""
         px = np.ascontiguousarray(pixels, dtype=np.float32)
         cap = self.lib.pico_gpu_hdr_bound(width, height)
-        buf = (C.c_ubyte * cap)()
+        buf = np.empty(cap, np.uint8)
         n = C.c_size_t(0)
-        self.check(self.lib.pico_gpu_encode_hdr(self.handle, _f32(px), width, height, buf, cap, C.byref(n)),
-                   "encode_hdr")
-        return bytes(buf[:n.value])
+        self.check(self.lib.pico_gpu_encode_hdr(self.handle, _f32(px), width, height, buf.ctypes.data, cap,
+                                                C.byref(n)), "encode_hdr")
+        return buf[:n.value].tobytes()
 
     def bsdf_eval(self, kinds, materials, V, N, H, xi):
         """Device BSRDF routines on given inputs: (pdf, L, P, energy, direct_pdf)."""

@@ -4,9 +4,9 @@
 // component on scanlines 8..32767 pixels wide.
 //
 // On the device: one thread per pixel encodes RGBE (frexp of the largest
-// component; mantissa scaled by 256 / max, truncated), then one thread per
-// (scanline, component) run-length codes that component's bytes into a slot
-// of W + ceil(W / 128) bytes (the worst case: all literals).  The host writes
+// component; mantissa scaled by 256 / max, truncated), then one CTA per
+// scanline run-length codes its four components, each into a slot of
+// W + ceil(W / 128) bytes (the worst case: all literals).  The host writes
 // the header and concatenates the slots.  NaN or negative components, whose
 // conversion to a byte is undefined in the reference, are written as 0.
 #include "capi_internal.h"
@@ -39,36 +39,46 @@ __global__ void rgbe_kernel(const float* __restrict__ pix, size_t npx, uchar4* _
     }
 }
 
-// One (scanline, component) per thread, the stbi_write_hdr run-length scheme.
-__global__ void rle_kernel(const uchar4* __restrict__ rgbe, uint32_t W, uint32_t H, size_t slot,
-                           unsigned char* __restrict__ out, uint32_t* __restrict__ lens)
+size_t rle_slot(uint32_t W) { return (size_t)W + (W + 127) / 128; }
+
+// The stbi_write_hdr run-length scheme, one CTA per scanline: the row's RGBE
+// texels are staged in shared memory with coalesced loads, then four threads
+// code the four components from shared memory (literal runs of up to 128
+// bytes until the next run of three or more equal bytes, which is coded in
+// pieces of up to 127).
+__global__ void rle_row_kernel(const uchar4* __restrict__ rgbe, uint32_t W, uint32_t H, size_t slot,
+                               unsigned char* __restrict__ out, uint32_t* __restrict__ lens)
 {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= 4 * H) return;
-    const uint32_t row = k / 4, c = k % 4;
+    extern __shared__ uchar4 row_px[];
+    const uint32_t row = blockIdx.x;
     const uchar4* line = rgbe + (size_t)row * W;
+    for (uint32_t x = threadIdx.x; x < W; x += blockDim.x) row_px[x] = line[x];
+    __syncthreads();
+    const uint32_t c = threadIdx.x;
+    if (c >= 4) return;
     auto at = [&](uint32_t x) -> unsigned char {
-        const uchar4 v = line[x];
+        const uchar4 v = row_px[x];
         return c == 0 ? v.x : (c == 1 ? v.y : (c == 2 ? v.z : v.w));
     };
+    const uint32_t k = row * 4 + c;
     unsigned char* o = out + slot * k;
     uint32_t n = 0, x = 0;
     while (x < W) {
-        uint32_t r = x;   // the first run of three equal bytes at or after x
+        uint32_t r = x;
         while (r + 2 < W) {
             const unsigned char a = at(r);
             if (a == at(r + 1) && a == at(r + 2)) break;
             ++r;
         }
         if (r + 2 >= W) r = W;
-        while (x < r) {   // literals up to the run, at most 128 at a time
+        while (x < r) {
             uint32_t len = r - x;
             if (len > 128) len = 128;
             o[n++] = (unsigned char)len;
             for (uint32_t i = 0; i < len; ++i) o[n++] = at(x + i);
             x += len;
         }
-        if (r + 2 < W) {   // the run, at most 127 at a time
+        if (r + 2 < W) {
             const unsigned char v = at(x);
             while (r < W && at(r) == v) ++r;
             while (x < r) {
@@ -82,8 +92,6 @@ __global__ void rle_kernel(const uchar4* __restrict__ rgbe, uint32_t W, uint32_t
     }
     lens[k] = n;
 }
-
-size_t rle_slot(uint32_t W) { return (size_t)W + (W + 127) / 128; }
 
 }  // namespace
 
@@ -112,9 +120,13 @@ int encode_hdr(pico_gpu_ctx* ctx, const float* d_pixels, uint32_t W, uint32_t H,
         rgbe_kernel<<<blocks, 256, 0, st>>>(d_pixels, npx, static_cast<uchar4*>(d_rgbe));
         e = cudaGetLastError();
         if (e == cudaSuccess && rle) {
-            rle_kernel<<<(4 * H + 127) / 128, 128, 0, st>>>(static_cast<uchar4*>(d_rgbe), W, H, slot,
-                                                           static_cast<unsigned char*>(d_rle),
-                                                           static_cast<uint32_t*>(d_lens));
+            // rows are staged in shared memory (W < 32768 texels of 4 bytes)
+            const size_t smem = (size_t)W * sizeof(uchar4);
+            e = cudaFuncSetAttribute(rle_row_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess)
+                rle_row_kernel<<<H, 128, smem, st>>>(static_cast<uchar4*>(d_rgbe), W, H, slot,
+                                                     static_cast<unsigned char*>(d_rle),
+                                                     static_cast<uint32_t*>(d_lens));
             e = cudaGetLastError();
             lens.resize(4 * (size_t)H);
             body.resize(slot * 4 * H);

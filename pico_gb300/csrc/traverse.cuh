@@ -150,7 +150,8 @@ __device__ __forceinline__ ObjectRay to_object(const GpuInstance* inst, const fl
     r.root_hi = __ldg(ip + 8);
     r.ox = row4(i0, o.x, o.y, o.z, o.w); r.oy = row4(i1, o.x, o.y, o.z, o.w); r.oz = row4(i2, o.x, o.y, o.z, o.w);
     r.dx = row3(i0, d.x, d.y, d.z); r.dy = row3(i1, d.x, d.y, d.z); r.dz = row3(i2, d.x, d.y, d.z);
-    r.ix = div(1.0f, r.dx); r.iy = div(1.0f, r.dy); r.iz = div(1.0f, r.dz);
+    // 1.0f / x correctly rounded (Core/AABB.cpp:48): the same bits as the IEEE division
+    r.ix = __frcp_rn(r.dx); r.iy = __frcp_rn(r.dy); r.iz = __frcp_rn(r.dz);
     return r;
 }
 
@@ -241,7 +242,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
     uint32_t stack[kTraceStack];
     int sp = 0;
     best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
-    const float wix = div(1.0f, d.x), wiy = div(1.0f, d.y), wiz = div(1.0f, d.z);
+    const float wix = __frcp_rn(d.x), wiy = __frcp_rn(d.y), wiz = __frcp_rn(d.z);
     // A triangle of an instance at object-space t lies at world distance t |D| up
     // to float error (relative ~1e-6, absolute ~1e-7 |O|); the BLAS bound adds
     // 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a triangle
@@ -389,7 +390,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
     StackEntry stack[kTraceStack];
     int sp = 0;
     best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
-    const float wix = div(1.0f, d.x), wiy = div(1.0f, d.y), wiz = div(1.0f, d.z);
+    const float wix = __frcp_rn(d.x), wiy = __frcp_rn(d.y), wiz = __frcp_rn(d.z);
     ObjectRay q{};
     float lt = kInf, lu = 0.0f, lv = 0.0f;
     uint32_t ltri = kNoHit, cur = 0;
