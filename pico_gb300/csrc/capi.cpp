@@ -168,7 +168,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     cudaError_t e = cudaSuccess;
     const GpuNode* nodes; const GpuTri* tris; const GpuTriShade* tshade; const GpuInstance* insts;
     const GpuInstanceShade* ishade; const uint32_t* irank; const GpuMaterial* mats; const GpuLight* lights;
-    const float* law; const uint32_t* lai; const float* lpos; const unsigned char* skypx;
+    const float* law; const uint32_t* lai; const float* lpos; const unsigned char* skypx; const uint32_t* titems;
     if (e == cudaSuccess) e = upload(fs.nodes, nodes);
     if (e == cudaSuccess) e = upload(fs.tris, tris);
     if (e == cudaSuccess) e = upload(fs.tri_shade, tshade);
@@ -181,12 +181,13 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     if (e == cudaSuccess) e = upload(fs.light_alias_index, lai);
     if (e == cudaSuccess) e = upload(fs.light_positions, lpos);
     if (e == cudaSuccess) e = upload(fs.sky_pixels, skypx);
+    if (e == cudaSuccess) e = upload(fs.tlas_items, titems);
     if (e != cudaSuccess) {
         pico_gpu_scene_free(s);
         return cuda_error(ctx, e, "scene upload");
     }
     v.nodes = nodes; v.tris = tris; v.tri_shade = tshade; v.insts = insts; v.inst_shade = ishade;
-    v.inst_rank = irank; v.materials = mats; v.lights = lights; v.light_alias_weight = law;
+    v.inst_rank = irank; v.tlas_items = titems; v.materials = mats; v.lights = lights; v.light_alias_weight = law;
     v.light_alias_index = lai; v.light_positions = lpos;
     v.nlights = (uint32_t)fs.lights.size();
     v.tlas_root_ref = fs.tlas_root_ref;

@@ -100,6 +100,7 @@ struct SceneView {
     const GpuTri* tris;
     const GpuTriShade* tri_shade;
     const GpuInstance* insts;          // indexed by TLAS rank
+    const uint32_t* tlas_items;         // TLAS leaf item -> instance rank
     const GpuInstanceShade* inst_shade; // indexed by original instance index
     const uint32_t* inst_rank;          // original instance index -> TLAS rank
     const GpuMaterial* materials;

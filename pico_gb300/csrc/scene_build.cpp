@@ -169,6 +169,94 @@ private:
     RefBvh& bvh_;
 };
 
+// A 32-bin SAH over the instances' tight boxes for the near-first walk: every
+// split is priced by area x count on both sides, leaves hold one instance
+// unless all centroids coincide.  Its topology is free (the walk breaks ties by
+// the reference's ranks), so it only has to prune well.
+class BinnedSahBuilder {
+public:
+    explicit BinnedSahBuilder(RefBvh& out) : bvh_(out) {}
+    void build(std::vector<Item>& items) { bvh_.root = split(items.begin(), items.end()); }
+
+private:
+    using It = std::vector<Item>::iterator;
+    static constexpr int kBins = 32;
+
+    static float centre(const Item& it, int a)
+    {
+        const V4 c = it.box.center();
+        return a == 0 ? c.x : (a == 1 ? c.y : c.z);
+    }
+
+    uint32_t split(It start, It end)
+    {
+        if (start == end) return kInvalid;
+        RefNode n;
+        float lo[3] = {kInf, kInf, kInf}, hi[3] = {-kInf, -kInf, -kInf};
+        for (It i = start; i != end; ++i) {
+            n.box.grow(i->box);
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], centre(*i, a));
+                hi[a] = std::max(hi[a], centre(*i, a));
+            }
+        }
+        const size_t count = (size_t)std::distance(start, end);
+        int best_axis = -1, best_bin = 0;
+        float best_cost = kInf;
+        if (count > 1) {
+            for (int a = 0; a < 3; ++a) {
+                const float extent = hi[a] - lo[a];
+                if (!(extent > 0.0f)) continue;
+                uint32_t cnt[kBins] = {};
+                Box bb[kBins];
+                for (It i = start; i != end; ++i) {
+                    const int b = std::min(kBins - 1, (int)((float)kBins * (centre(*i, a) - lo[a]) / extent));
+                    cnt[b]++;
+                    bb[b].grow(i->box);
+                }
+                float right_area[kBins];
+                uint32_t right_cnt[kBins];
+                Box r;
+                uint32_t rc = 0;
+                for (int b = kBins - 1; b > 0; --b) {
+                    r.grow(bb[b]);
+                    rc += cnt[b];
+                    right_area[b] = rc ? r.area() : 0.0f;
+                    right_cnt[b] = rc;
+                }
+                Box l;
+                uint32_t lc = 0;
+                for (int b = 0; b < kBins - 1; ++b) {
+                    l.grow(bb[b]);
+                    lc += cnt[b];
+                    if (lc == 0 || right_cnt[b + 1] == 0) continue;
+                    const float cost = l.area() * (float)lc + right_area[b + 1] * (float)right_cnt[b + 1];
+                    if (cost < best_cost) { best_cost = cost; best_axis = a; best_bin = b; }
+                }
+            }
+        }
+        It mid = end;
+        if (best_axis >= 0) {
+            const int a = best_axis;
+            const float extent = hi[a] - lo[a];
+            mid = std::partition(start, end, [&](const Item& it) {
+                return std::min(kBins - 1, (int)((float)kBins * (centre(it, a) - lo[a]) / extent)) <= best_bin;
+            });
+        }
+        if (mid == start || mid == end) {   // one instance, or all centroids in one place: a leaf
+            for (It i = start; i != end; ++i) n.values.push_back(i->value);
+            bvh_.nodes.push_back(std::move(n));
+            return (uint32_t)bvh_.nodes.size() - 1;
+        }
+        n.child[0] = split(start, mid);
+        n.child[1] = split(mid, end);
+        bvh_.nodes.push_back(std::move(n));
+        return (uint32_t)bvh_.nodes.size() - 1;
+    }
+
+    RefBvh& bvh_;
+};
+
 // Flattens a reference-topology BVH into GpuNodes; `place` appends a leaf's
 // items to the item array and returns the position of the first.
 template <class Place>
@@ -457,6 +545,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
             g.root_ref = mr.ref;
             g.inst_id = i;
             fs.inst_rank[i] = (uint32_t)fs.insts.size();
+            fs.tlas_items.push_back((uint32_t)fs.insts.size());   // the reference tree's items are its ranks
             fs.insts.push_back(g);
         }
         return first;
@@ -508,23 +597,20 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         tight[i].lo = {(float)(e[0] - pad), (float)(e[1] - pad), (float)(e[2] - pad), 1.0f};
         tight[i].hi = {(float)(e[3] + pad), (float)(e[4] + pad), (float)(e[5] + pad), 1.0f};
     }
-    RefBvh refit = tlas;
-    for (RefNode& n : refit.nodes) {   // post-order: children before parents
-        n.box = Box{};
-        if (!n.values.empty()) {
-            for (uint32_t v : n.values) n.box.grow(tight[v]);
-        } else {
-            for (int c = 0; c < 2; ++c)
-                if (n.child[c] != kInvalid) n.box.grow(refit.nodes[n.child[c]].box);
-        }
+    // the near-first TLAS: a fresh SAH over the tight boxes, leaves listing ranks
+    RefBvh refit;
+    {
+        std::vector<Item> titems(desc.ninstances);
+        for (uint32_t i = 0; i < desc.ninstances; ++i) titems[i] = Item{tight[i], fs.inst_rank[i]};
+        BinnedSahBuilder(refit).build(titems);
     }
-    uint32_t rank_cursor = 0;   // leaves come in the same depth-first order as above
-    auto replace = [&](const std::vector<uint32_t>& values) -> uint32_t {
-        const uint32_t first = rank_cursor;
-        rank_cursor += (uint32_t)values.size();
+    auto list_ranks = [&](const std::vector<uint32_t>& ranks) -> uint32_t {
+        const uint32_t first = (uint32_t)fs.tlas_items.size();
+        fs.tlas_items.insert(fs.tlas_items.end(), ranks.begin(), ranks.end());
         return first;
     };
-    fs.tlas_fast_root_ref = flatten(refit, fs.nodes, replace);
+    fs.tlas_fast_root_ref = flatten(refit, fs.nodes, list_ranks);
+    if (fs.tlas_items.size() > PICO_FIRST_MAX) return "too many instances";
     if (refit.root != kInvalid) {
         const Box& b = refit.nodes[refit.root].box;
         fs.tlas_fast_lo[0] = b.lo.x; fs.tlas_fast_lo[1] = b.lo.y; fs.tlas_fast_lo[2] = b.lo.z;

@@ -16,6 +16,7 @@ struct FlatScene {
     std::vector<GpuTri> tris;
     std::vector<GpuTriShade> tri_shade;
     std::vector<GpuInstance> insts;       // TLAS rank order
+    std::vector<uint32_t> tlas_items;     // TLAS leaf items -> instance rank (identity for the reference tree)
     std::vector<GpuInstanceShade> inst_shade;
     std::vector<uint32_t> inst_rank;      // original index -> rank
     std::vector<GpuMaterial> materials;

@@ -340,23 +340,24 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             ref = stack[--sp];   // the END_BLAS sentinel is below, so sp > 0 here
             continue;
         }
-        // TLAS leaf: search instance `first`; the rest of the leaf waits on the stack.
+        // TLAS leaf: search the instance of item `first`; the rest of the leaf waits on the stack.
         if (count > 1) {
             if (sp >= kTraceStack) return kTraceStackOverflow;
             stack[sp++] = pico_leaf_ref(first + 1, count - 1);
         }
+        const uint32_t rank = __ldg(sc.tlas_items + first);
         if (kCount) cnt->insts++;
-        if (kImplicit && is_implicit_root(sc.insts + first)) {
+        if (kImplicit && is_implicit_root(sc.insts + rank)) {
             // an implicit shape: one candidate, no BLAS and no root box test
             float tw, t;
-            if (implicit_candidate(sc.insts + first, o, d, tw, t) &&
-                (tw < best.t || (tw == best.t && first < best.rank))) {
-                best.t = tw; best.rank = first; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+            if (implicit_candidate(sc.insts + rank, o, d, tw, t) &&
+                (tw < best.t || (tw == best.t && rank < best.rank))) {
+                best.t = tw; best.rank = rank; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
             }
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
         }
-        q = to_object(sc.insts + first, o, d);
+        q = to_object(sc.insts + rank, o, d);
         gl = (best.t * 1.001f + omag) * inv_len;
         bool h;
         const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
@@ -369,7 +370,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         stack[sp++] = PICO_REF_END_BLAS;
         in_blas = true;
         qfast = sc.finite_boxes && all_finite(q.ox, q.oy, q.oz, q.ix, q.iy, q.iz);
-        cur = first;
+        cur = rank;
         lt = kInf; ltri = kNoHit;
         ref = __float_as_uint(q.root_lo.w);
     }
@@ -464,16 +465,17 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             if (sp >= kTraceStack) return kTraceStackOverflow;
             stack[sp++] = StackEntry{pico_leaf_ref(first + 1, count - 1), -kInf};
         }
+        const uint32_t rank = __ldg(sc.tlas_items + first);   // the identity on the reference's tree
         if (kCount) cnt->insts++;
-        if (kImplicit && is_implicit_root(sc.insts + first)) {
+        if (kImplicit && is_implicit_root(sc.insts + rank)) {
             float tw, t;
-            if (implicit_candidate(sc.insts + first, o, d, tw, t) && tw < best.t) {
-                best.t = tw; best.rank = first; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+            if (implicit_candidate(sc.insts + rank, o, d, tw, t) && tw < best.t) {
+                best.t = tw; best.rank = rank; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
             }
             ref = pop();
             continue;
         }
-        q = to_object(sc.insts + first, o, d);
+        q = to_object(sc.insts + rank, o, d);
         bool h;
         const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
                               q.oy, q.oz, q.ix, q.iy, q.iz, h);
@@ -484,7 +486,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
         if (sp >= kTraceStack) return kTraceStackOverflow;
         stack[sp++] = StackEntry{PICO_REF_END_BLAS, -kInf};
         in_blas = true;
-        cur = first;
+        cur = rank;
         lt = kInf; ltri = kNoHit;
         ref = __float_as_uint(q.root_lo.w);
     }
