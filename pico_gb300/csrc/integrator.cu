@@ -98,7 +98,7 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 }
 
 template <int kOrder>
-__global__ void __launch_bounds__(128, 8) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
+__global__ void __launch_bounds__(128, 7) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                        const uint32_t* count, unsigned long long* work, int* err,
                                                        bool shadow, unsigned long long* tally)
 {

@@ -34,7 +34,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
     trace_kernel(SceneView sc, const float4* __restrict__ rays, uint64_t n, pico_hit* __restrict__ hits,
                  DeviceStatus* status)
 {
-    TraceCounters cnt{0, 0, 0};
+    TraceCounters cnt{0, 0, 0, 0};
     const unsigned lane = threadIdx.x & 31u;
     for (;;) {
         unsigned long long base = 0;
@@ -56,11 +56,13 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
             cnt.nodes += __shfl_down_sync(0xffffffffu, cnt.nodes, off);
             cnt.tris += __shfl_down_sync(0xffffffffu, cnt.tris, off);
             cnt.insts += __shfl_down_sync(0xffffffffu, cnt.insts, off);
+            cnt.blas_nodes += __shfl_down_sync(0xffffffffu, cnt.blas_nodes, off);
         }
         if (lane == 0) {
             atomicAdd(&status->counters[0], cnt.nodes);
             atomicAdd(&status->counters[1], cnt.tris);
             atomicAdd(&status->counters[2], cnt.insts);
+            atomicAdd(&status->counters[3], cnt.blas_nodes);
         }
     }
 }

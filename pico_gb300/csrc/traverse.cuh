@@ -40,7 +40,7 @@ struct TraceHit {
 };
 
 struct TraceCounters {
-    unsigned long long nodes, tris, insts;
+    unsigned long long nodes, tris, insts, blas_nodes;   // blas_nodes: the part of nodes inside instances
 };
 
 // AABB::intersection_distance; `hit` is false where the reference returns INFINITY.
@@ -239,29 +239,30 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 {
     using namespace ex;
     const float kInf = __int_as_float(0x7f800000);
+    const float kMaxFinite = __int_as_float(0x7f7fffff);
     uint32_t stack[kTraceStack];
     int sp = 0;
     best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
     const float wix = __frcp_rn(d.x), wiy = __frcp_rn(d.y), wiz = __frcp_rn(d.z);
-    // A triangle of an instance at object-space t lies at world distance t |D| up
-    // to float error (relative ~1e-6, absolute ~1e-7 |O|); the BLAS bound adds
-    // 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a triangle
-    // that could beat or tie the best world distance.
-    const float inv_len = rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
-    const float omag = 1e-4f * (fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) + 1.0f);
-    ObjectRay q{};
+    // node tests take the NaN-free form when the ray (world or object space) and the boxes are finite
+    const bool wfast = sc.finite_boxes && all_finite(o.x, o.y, o.z, wix, wiy, wiz);
+    // The ray the node tests use: the world ray in the TLAS, the object-space ray
+    // inside an instance; switched on entering and leaving an instance.  `limit`
+    // is the distance a child box may not exceed (the best world distance in the
+    // TLAS, min(object-space best, BLAS bound) inside), clamped to the largest
+    // finite float so that one comparison also rejects boxes at +inf.
+    float cx = o.x, cy = o.y, cz = o.z, cix = wix, ciy = wiy, ciz = wiz;
+    bool cfast = wfast;
+    float limit = kMaxFinite;
+    float qdx = 0.0f, qdy = 0.0f, qdz = 0.0f;   // object-space direction of the instance being searched
     float gl = kInf, lt = kInf, lu = 0.0f, lv = 0.0f;
     uint32_t ltri = kNoHit, cur = 0;
     bool in_blas = false;
-    // node tests take the NaN-free form when the ray (world or object space) and the boxes are finite
-    const bool wfast = sc.finite_boxes && all_finite(o.x, o.y, o.z, wix, wiy, wiz);
-    bool qfast = false;
 
     // A ray with a zero direction component whose origin lies on a box plane gets
     // a NaN slab distance there, and the reference skips that box.  Such rays walk
     // the reference's own TLAS boxes so those decisions stay the reference's; every
-    // other ray walks the refitted TLAS (same topology, same leaf ranks), where no
-    // slab distance can be NaN.
+    // other ray walks the near-first TLAS, where no slab distance can be NaN.
     uint32_t ref = PICO_REF_DONE;
     {
         const bool axis = d.x == 0.0f || d.y == 0.0f || d.z == 0.0f;
@@ -281,21 +282,22 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
             const float4 n0 = __ldg(np), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
             const uint4 n3 = __ldg(reinterpret_cast<const uint4*>(np) + 3);
-            if (kCount) cnt->nodes++;
-            const float rx = in_blas ? q.ox : o.x, ry = in_blas ? q.oy : o.y, rz = in_blas ? q.oz : o.z;
-            const float rix = in_blas ? q.ix : wix, riy = in_blas ? q.iy : wiy, riz = in_blas ? q.iz : wiz;
-            const float limit = in_blas ? fminf(lt, gl) : best.t;
+            if (kCount) {
+                cnt->nodes++;
+                if (in_blas) cnt->blas_nodes++;
+            }
             bool h0, h1;
             float t0, t1;
-            if (in_blas ? qfast : wfast) {
-                t0 = slab_fast(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-                t1 = slab_fast(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            if (cfast) {
+                t0 = slab_fast(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, cx, cy, cz, cix, ciy, ciz, h0);
+                t1 = slab_fast(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, cx, cy, cz, cix, ciy, ciz, h1);
             } else {
-                t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-                t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+                t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, cx, cy, cz, cix, ciy, ciz, h0);
+                t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, cx, cy, cz, cix, ciy, ciz, h1);
             }
-            const bool v0 = h0 && t0 <= limit && t0 < kInf;
-            const bool v1 = h1 && t1 <= limit && t1 < kInf;
+            // t <= limit (finite) also rejects t = +inf and NaN, like "t <= best && t < inf"
+            const bool v0 = h0 && t0 <= limit;
+            const bool v1 = h1 && t1 <= limit;
             if (v0 && v1) {
                 const bool swap = t1 < t0;
                 if (sp >= kTraceStack) return kTraceStackOverflow;
@@ -319,6 +321,11 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
                 }
             }
             in_blas = false;
+            // back to the world ray (its reciprocals recomputed rather than kept in registers)
+            cx = o.x; cy = o.y; cz = o.z;
+            cix = __frcp_rn(d.x); ciy = __frcp_rn(d.y); ciz = __frcp_rn(d.z);
+            cfast = wfast;
+            limit = fminf(best.t, kMaxFinite);
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
         }
@@ -332,11 +339,12 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
                 const uint32_t tri = first + k;
                 float t, u, v;
                 if (kCount) cnt->tris++;
-                if (intersect_triangle(sc.tris + tri, q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, t, u, v) &&
+                if (intersect_triangle(sc.tris + tri, cx, cy, cz, qdx, qdy, qdz, t, u, v) &&
                     (t < lt || (t == lt && tri < ltri))) {
                     lt = t; ltri = tri; lu = u; lv = v;
                 }
             }
+            limit = fminf(limit, lt);
             ref = stack[--sp];   // the END_BLAS sentinel is below, so sp > 0 here
             continue;
         }
@@ -353,12 +361,21 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             if (implicit_candidate(sc.insts + rank, o, d, tw, t) &&
                 (tw < best.t || (tw == best.t && rank < best.rank))) {
                 best.t = tw; best.rank = rank; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+                limit = fminf(best.t, kMaxFinite);
             }
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
         }
-        q = to_object(sc.insts + rank, o, d);
-        gl = (best.t * 1.001f + omag) * inv_len;
+        const ObjectRay q = to_object(sc.insts + rank, o, d);
+        {
+            // A triangle of an instance at object-space t lies at world distance t |D|
+            // up to float error (relative ~1e-6, absolute ~1e-7 |O|); the BLAS bound
+            // adds 0.1 % and 1e-4 (|O| + 1), far above that error, so it never cuts a
+            // triangle that could beat or tie the best world distance.
+            const float inv_len = rsqrtf(d.x * d.x + d.y * d.y + d.z * d.z);
+            const float omag = 1e-4f * (fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)) + 1.0f);
+            gl = (best.t * 1.001f + omag) * inv_len;
+        }
         bool h;
         const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
                               q.oy, q.oz, q.ix, q.iy, q.iz, h);
@@ -369,7 +386,10 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         if (sp >= kTraceStack) return kTraceStackOverflow;
         stack[sp++] = PICO_REF_END_BLAS;
         in_blas = true;
-        qfast = sc.finite_boxes && all_finite(q.ox, q.oy, q.oz, q.ix, q.iy, q.iz);
+        cx = q.ox; cy = q.oy; cz = q.oz; cix = q.ix; ciy = q.iy; ciz = q.iz;
+        qdx = q.dx; qdy = q.dy; qdz = q.dz;
+        cfast = sc.finite_boxes && all_finite(q.ox, q.oy, q.oz, q.ix, q.iy, q.iz);
+        limit = fminf(gl, kMaxFinite);   // lt starts at +inf
         cur = rank;
         lt = kInf; ltri = kNoHit;
         ref = __float_as_uint(q.root_lo.w);
