@@ -283,7 +283,10 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
     if (!ctx || !scene || (n && (!rays || !hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     cudaSetDevice(ctx->device);
     if (n == 0) return PICO_OK;
-    const uint64_t chunk = n < (1ull << 22) ? n : (1ull << 22);
+    // 1M-ray chunks alternate between two streams: each chunk's copies overlap the
+    // other stream's traversal, and only the first upload and the last download
+    // (32 MB / 20 MB) stay exposed
+    const uint64_t chunk = n < (1ull << 20) ? n : (1ull << 20);
     cudaError_t e = ctx->buf_a.reserve(chunk * sizeof(pico_ray));
     if (e == cudaSuccess) e = ctx->buf_b.reserve(chunk * sizeof(pico_ray));
     if (e == cudaSuccess) e = ctx->buf_c.reserve(chunk * sizeof(pico_hit));
