@@ -222,10 +222,44 @@ def bench_render(ctx, args, torch, local):
            "rays": {k: st[k] for k in ("camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
            "timing": "wall clock around pico_gpu_render, host buffers in and out",
            "clocks": clocks.summary()}
+    conv = convergence(ctx, gs, scene, cam, args, pix)
+    if conv:
+        out["relmse"] = conv
     if not args.no_cpu and args.render_cpu_pixels > 0:
         out["cpu_baseline"] = cpu_render(scene, cam, args)
     gs.free()
     return out
+
+
+def convergence(ctx, gs, scene, cam, args, timed_image):
+    """relMSE against the converged judge of the lit field (FP64 mean of 4096 reference samples
+    on 1024 seeded pixels): of the timed render, and of plain renders at 64 and 256 spp without
+    the early exit (noisy, and after the a-trous pass), each with its wall time."""
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from judge import Judge
+    try:
+        j = Judge("lit")
+        j.check_scene(scene)
+    except (OSError, KeyError, ValueError):
+        return None
+    if (j.width, j.height) != tuple(cam.resolution) or j.depth != args.render_depth:
+        return None
+    W, H = cam.resolution
+    nrm, pos, dif = gs.denoiser_inputs(cam)
+    series = []
+    for spp in (64, 256):
+        t0 = time.perf_counter()
+        pix, _, _ = gs.render(cam, args.render_depth, spp, seed=500 + spp, max_variance=-1.0)
+        secs = time.perf_counter() - t0
+        den, bad = j.relmse_finite(ctx.atrous(pix, nrm, pos, dif, W, H))
+        series.append({"spp": spp, "seconds": secs, "relmse": j.relmse(pix), "relmse_denoised": den,
+                       "denoised_nan_pixels": bad})
+    timed = j.relmse_finite(timed_image)
+    return {"judge": f"FP64 mean of {j.spp} reference samples (Integrators.cpp:130-154) on "
+                     f"{len(j.pixels)} seeded pixels", "eps": 0.01,
+            "timed_render": timed[0], "timed_render_nan_pixels": timed[1],
+            "timed_render_note": "denoised, reference early exit; relMSE over the finite judged pixels",
+            "plain_no_early_exit": series}
 
 
 def cpu_render(scene, cam, args):

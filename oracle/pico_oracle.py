@@ -388,6 +388,8 @@ class Reference(_SceneLib):
             "ref_integrate": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _u32, _u64, _u32, _fp]),
             "ref_render_pixels": (C.c_double, [_vp, C.POINTER(CCamera), _u32, _u32, C.c_float, _up,
                                                C.POINTER(_u64), _u32, _fp, _up, _fp, _i32]),
+            "ref_render_mean64": (C.c_double, [_vp, C.POINTER(CCamera), _u32, _u32, _up, C.POINTER(_u64), _u32,
+                                               C.POINTER(C.c_double), C.POINTER(C.c_double), _i32]),
             "ref_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "ref_atrous": (C.c_double, [_fp, _fp, _fp, _fp, _u32, _u32, _fp, _i32]),
             "ref_reinhard": (None, [_fp, _u32, _u32]),
@@ -468,6 +470,18 @@ class ReferenceScene:
                                           pixels.ctypes.data_as(_fp), counts.ctypes.data_as(_up),
                                           variance.ctypes.data_as(_fp), nthreads)
         return pixels, counts, variance, secs
+
+    def render_mean64(self, cam, max_depth, spp, pixel_index, seeds, nthreads=0):
+        """Plain FP64 mean and sample variance of `spp` reference samples per listed pixel."""
+        idx = np.ascontiguousarray(pixel_index, np.uint32)
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        mean, var = np.empty((len(idx), 3)), np.empty((len(idx), 3))
+        c = cam.to_c()
+        secs = self.lib.ref_render_mean64(self.handle, C.byref(c), max_depth, spp, idx.ctypes.data_as(_up),
+                                          sd.ctypes.data_as(C.POINTER(_u64)), len(idx),
+                                          mean.ctypes.data_as(C.POINTER(C.c_double)),
+                                          var.ctypes.data_as(C.POINTER(C.c_double)), nthreads)
+        return mean, var, secs
 
     def denoiser_inputs(self, cam):
         W, H = int(cam.resolution[0]), int(cam.resolution[1])

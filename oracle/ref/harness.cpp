@@ -655,6 +655,51 @@ double ref_render_pixels(const void* p, const po_camera* c, uint32_t max_depth, 
     return std::chrono::duration<double>(t1 - t0).count();
 }
 
+// A converged judge render: `spp` samples of the reference's own
+// Monte_Carlo_Integrator::integrate_ray (Render/Integrators.cpp:130-154) per listed
+// pixel, summed in double precision.  Writes per pixel and channel the plain mean
+// of all samples and their unbiased sample variance (not the running mean of
+// Scene.cpp:185-191, which drops the first sample).
+double ref_render_mean64(const void* p, const po_camera* c, uint32_t max_depth, uint32_t spp,
+                         const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, double* mean,
+                         double* var, int nthreads)
+{
+    auto* s = const_cast<RefScene*>(static_cast<const RefScene*>(p));
+    const Scene::Camera cam = to_camera(c);
+    const uint32_t W = c->resolution[0];
+    auto body = [&](uint32_t lo, uint32_t hi) -> bool {
+        for (uint32_t k = lo; k < hi; ++k) {
+            const uint32_t flat = pixel_index[k];
+            const glm::uvec2 pix(flat % W, flat / W);
+            Render::Monte_Carlo_Integrator integrator(s->tlas, s->materials, s->lights, s->sun, seeds[k]);
+            double sum[3] = {0.0, 0.0, 0.0}, sq[3] = {0.0, 0.0, 0.0};
+            for (uint32_t i = 0; i < spp; ++i) {
+                const glm::vec3 x = integrator.integrate_ray(cam, pix, max_depth);
+                for (int a = 0; a < 3; ++a) {
+                    sum[a] += (double)x[a];
+                    sq[a] += (double)x[a] * (double)x[a];
+                }
+            }
+            for (int a = 0; a < 3; ++a) {
+                const double m = sum[a] / spp;
+                mean[3 * k + a] = m;
+                var[3 * k + a] = spp > 1 ? (sq[a] - spp * m * m) / (spp - 1) : 0.0;
+            }
+        }
+        return true;
+    };
+    auto t0 = std::chrono::steady_clock::now();
+    {
+        ThreadPool pool(nthreads > 0 ? (uint32_t)nthreads : std::thread::hardware_concurrency());
+        std::vector<std::future<bool>> handles;
+        for (uint32_t lo = 0; lo < npixels; lo += 16)
+            handles.push_back(pool.add_task(body, lo, std::min(npixels, lo + 16)));
+        for (auto& h : handles) h.wait();
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+
 // Scene::generate_denoiser_inputs (Core/Scene.cpp:248-294), private there; the
 // per-pixel body is written against the reference's public routines.
 void ref_denoiser_inputs(const void* p, const po_camera* c, uint32_t W, uint32_t H, float* normals,

@@ -342,15 +342,43 @@ def shapes_fixtures(ref):
     np.savez_compressed(HERE / "shapes.npz", **out)
 
 
+def judge_fixtures(ref, spp: int = 4096):
+    """Converged judges: `spp` reference samples per pixel summed in FP64, on 4096 seeded
+    pixels of the 256 x 256 Cornell box (depth 5) and 1024 of the 1920 x 1080 lit field
+    (depth 8)."""
+    from judge import relmse, scene_digest
+    out = {}
+    cases = [("cornell", scenes.cornell_box(), scenes.cornell_camera(256, 256), 5, 4096, 601),
+             ("lit", scenes.lit_field(), scenes.lit_field_camera(1920, 1080), 8, 1024, 602)]
+    for name, scene, cam, depth, npix, seed in cases:
+        W, H = cam.resolution
+        rng = np.random.default_rng(seed)
+        idx = np.sort(rng.choice(W * H, npix, replace=False)).astype(np.uint32)
+        seeds = rng.integers(1, 2**63, npix, dtype=np.uint64)
+        rs = ref.scene(scene)
+        mean, var, secs = rs.render_mean64(cam, depth, spp, idx, seeds)
+        print(f"judge {name}: {npix} pixels x {spp} spp in {secs:.1f} s")
+        # the reference's own render loop at 64 spp with its default early exit
+        # (max_variance 0, Scene.cpp:185-191): pixels it stopped and its relMSE
+        pix, cnt, _, _ = rs.render_pixels(cam, depth, 64, idx, rng.integers(1, 2**63, npix, dtype=np.uint64))
+        out[f"{name}_ref64_exited"] = np.array(int((cnt.reshape(-1)[idx] < 64).sum()))
+        out[f"{name}_ref64_relmse"] = np.array(relmse(pix.reshape(-1, 3)[idx], mean))
+        out.update({f"{name}_idx": idx, f"{name}_mean": mean, f"{name}_var": var, f"{name}_spp": np.array(spp),
+                    f"{name}_depth": np.array(depth), f"{name}_res": np.array([W, H]),
+                    f"{name}_digest": np.array(scene_digest(scene))})
+    np.savez_compressed(HERE / "judge.npz", **out)
+
+
+FIXTURES = {"trace": trace_fixtures, "sampling": sampling_fixtures, "integrator": integrator_fixtures,
+            "atrous": atrous_fixtures, "sky": sky_fixtures, "shapes": shapes_fixtures, "judge": judge_fixtures}
+
+
 def main():
+    """python make_golden.py [fixture ...]: all fixtures, or the named ones."""
     pico_oracle.build_reference()
     ref = pico_oracle.Reference()
-    trace_fixtures(ref)
-    sampling_fixtures(ref)
-    integrator_fixtures(ref)
-    atrous_fixtures(ref)
-    sky_fixtures(ref)
-    shapes_fixtures(ref)
+    for name in (sys.argv[1:] or list(FIXTURES)):
+        FIXTURES[name](ref)
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 
