@@ -199,46 +199,51 @@ ATROUS_BYTES_PER_PIXEL_LEVEL = 60   # 4 x 12 B in (colour, normal, position, alb
 L2_FLUSH_BYTES = 512 << 20
 
 
-def bench_render(ctx, args, torch, local):
+def bench_render(ctx, args, torch, local, estimator=0):
     """1080p render of the lit field through pico_gpu_render (host buffers in and out, denoised):
-    wall time per render, samples added and rays traced (camera, bounce, shadow, G-buffer)."""
+    wall time per render, samples added and rays traced (camera, bounce, shadow, G-buffer).
+    estimator 0 is the reference's estimator, 1 the physical one (NEE + BSDF sampling with MIS)."""
     scene = scenes.lit_field()
     cam = scenes.lit_field_camera(1920, 1080)
     gs = ctx.upload(scene)
-    gs.render(cam, args.render_depth, 2, seed=99, denoise=True)          # warm-up
+    gs.render(cam, args.render_depth, 2, seed=99, denoise=True, estimator=estimator)          # warm-up
     runs = []
     with ClockSampler(local) as clocks:
         for k in range(2):
             t0 = time.perf_counter()
-            pix, cnt, var = gs.render(cam, args.render_depth, args.render_spp, seed=1 + k, denoise=True)
+            pix, cnt, var = gs.render(cam, args.render_depth, args.render_spp, seed=1 + k, denoise=True,
+                                      estimator=estimator)
             runs.append((time.perf_counter() - t0, ctx.render_stats()))
     secs = float(np.mean([r[0] for r in runs]))
     st = runs[-1][1]
     rays = st["camera_paths"] + st["bounce_rays"] + st["shadow_rays"] + st["gbuffer_rays"]
+    name = "physical estimator (GGX, NEE + BSDF sampling with MIS, RR from depth 3)" if estimator else \
+        "reference estimator"
     out = {"workload": f"lit field (4096 level-4 icospheres, ground quad, 8 quad lights), 1920x1080, "
-                       f"{args.render_spp} spp, depth {args.render_depth}, a-trous denoise, reference estimator",
+                       f"{args.render_spp} spp, depth {args.render_depth}, a-trous denoise, {name}",
            "Msamples_per_s": st["samples"] / secs / 1e6, "Mrays_per_s": rays / secs / 1e6,
            "ms_per_render": secs * 1e3, "samples": st["samples"], "camera_paths": st["camera_paths"],
            "rays": {k: st[k] for k in ("camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
            "timing": "wall clock around pico_gpu_render, host buffers in and out",
            "clocks": clocks.summary()}
-    conv = convergence(ctx, gs, scene, cam, args, pix)
+    conv = convergence(ctx, gs, scene, cam, args, pix, estimator)
     if conv:
         out["relmse"] = conv
-    if not args.no_cpu and args.render_cpu_pixels > 0:
+    if not args.no_cpu and args.render_cpu_pixels > 0 and estimator == 0:
         out["cpu_baseline"] = cpu_render(scene, cam, args)
     gs.free()
     return out
 
 
-def convergence(ctx, gs, scene, cam, args, timed_image):
-    """relMSE against the converged judge of the lit field (FP64 mean of 4096 reference samples
-    on 1024 seeded pixels): of the timed render, and of plain renders at 64 and 256 spp without
-    the early exit (noisy, and after the a-trous pass), each with its wall time."""
+def convergence(ctx, gs, scene, cam, args, timed_image, estimator=0):
+    """relMSE against the converged judge of the lit field (FP64 mean of 4096 samples on 1024
+    seeded pixels, of the reference's integrator or, for the physical estimator, of its FP64
+    oracle): of the timed render, and of plain renders at 64 and 256 spp (the reference
+    estimator without its early exit), noisy and after the a-trous pass, with their wall time."""
     sys.path.insert(0, str(ROOT / "tests" / "golden"))
     from judge import Judge
     try:
-        j = Judge("lit")
+        j = Judge("lit_phys" if estimator else "lit")
         j.check_scene(scene)
     except (OSError, KeyError, ValueError):
         return None
@@ -249,16 +254,18 @@ def convergence(ctx, gs, scene, cam, args, timed_image):
     series = []
     for spp in (64, 256):
         t0 = time.perf_counter()
-        pix, _, _ = gs.render(cam, args.render_depth, spp, seed=500 + spp, max_variance=-1.0)
+        pix, _, _ = gs.render(cam, args.render_depth, spp, seed=500 + spp, max_variance=-1.0, estimator=estimator)
         secs = time.perf_counter() - t0
         den, bad = j.relmse_finite(ctx.atrous(pix, nrm, pos, dif, W, H))
         series.append({"spp": spp, "seconds": secs, "relmse": j.relmse(pix), "relmse_denoised": den,
                        "denoised_nan_pixels": bad})
     timed = j.relmse_finite(timed_image)
-    return {"judge": f"FP64 mean of {j.spp} reference samples (Integrators.cpp:130-154) on "
-                     f"{len(j.pixels)} seeded pixels", "eps": 0.01,
+    source = "samples of the FP64 oracle of the physical estimator" if estimator else \
+        "reference samples (Integrators.cpp:130-154)"
+    return {"judge": f"FP64 mean of {j.spp} {source} on {len(j.pixels)} seeded pixels", "eps": 0.01,
             "timed_render": timed[0], "timed_render_nan_pixels": timed[1],
-            "timed_render_note": "denoised, reference early exit; relMSE over the finite judged pixels",
+            "timed_render_note": ("denoised" if estimator else "denoised, reference early exit") +
+                                 "; relMSE over the finite judged pixels",
             "plain_no_early_exit": series}
 
 
@@ -496,10 +503,11 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
-    render = atrous = tonemap = hdr = None
+    render = render_physical = atrous = tonemap = hdr = None
     if not args.no_render:
         gs.free()
         render = bench_render(ctx, args, torch, local)
+        render_physical = bench_render(ctx, args, torch, local, estimator=1)
         atrous = bench_atrous(ctx, args, torch, local)
         tonemap, hdr = bench_tonemap_and_hdr(ctx, args, torch, local)
 
@@ -507,7 +515,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clocks.summary(), "scene": info, "render_1080p": render, "atrous_1080p": atrous,
+            "clocks": clocks.summary(), "scene": info, "render_1080p": render,
+            "render_1080p_physical": render_physical, "atrous_1080p": atrous,
             "tonemap_1080p": tonemap, "hdr_1080p": hdr}
     print(json.dumps(line), flush=True)
     if dist:

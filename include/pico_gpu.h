@@ -137,14 +137,29 @@ typedef struct {
 } pico_camera;
 
 /* Scene::RenderParams (Core/Scene.hpp:30-43) without the buffers, plus the seed
- * that replaces the reference's std::random_device draw. */
+ * that replaces the reference's std::random_device draw and the estimator.
+ *
+ * PICO_ESTIMATOR_REFERENCE (0) is Monte_Carlo_Integrator (Render/Integrators.cpp:
+ * 46-209) with the render loop of Scene.cpp:164-198, quirks included.
+ * PICO_ESTIMATOR_PHYSICAL (1) has no counterpart in the reference: Lambert plus
+ * GGX microfacet reflection (alpha = roughness^2, Smith height-correlated
+ * masking, Schlick Fresnel with F0 = specular) sampled through the GGX
+ * visible-normal distribution, next-event estimation on the triangle lights and
+ * the sun combined with BSDF sampling by the power heuristic, Russian roulette
+ * from the fourth vertex, a jitter over the whole pixel and a plain running mean
+ * (every sample counts; max_variance is ignored and no pixel stops early).
+ * Diffuse, Specular, Dielectric, Light and Specular_Delta (a mirror with Schlick
+ * reflectance) instances are supported; a scene with Transparent or Fresnel
+ * instances returns PICO_ERR_UNSUPPORTED.  Emitters are two-sided; the sun is a
+ * directional light whose colour is its irradiance. */
+enum pico_estimator { PICO_ESTIMATOR_REFERENCE = 0, PICO_ESTIMATOR_PHYSICAL = 1 };
 typedef struct {
     uint32_t max_ray_depth;
     uint32_t max_samples;
     float max_variance;
     uint32_t height, width;
     int32_t tonemap, denoise;
-    uint32_t reserved;
+    uint32_t estimator;       /* pico_estimator */
     uint64_t seed;
 } pico_render_config;
 
@@ -250,6 +265,15 @@ int pico_gpu_encode_hdr(pico_gpu_ctx* ctx, const float* pixels, uint32_t width, 
 int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, const pico_material* mats,
                        const float* V, const float* N, const float* H, const float* xi, float* pdf,
                        float* L, float* P, float* energy, float* direct_pdf);
+/* No counterpart in the reference: the physical estimator's BSDF (see
+ * pico_render_config) for n tuples of a Diffuse, Specular or Dielectric kind,
+ * unit V, N, L [n*3] and uniforms u [n*3]: f(V, L) [n*3] and the sampling
+ * density of L [n], and one sample from u: its direction [n*3], density [n],
+ * throughput weight f (N.L) / pdf [n*3] and whether it stays above the surface
+ * [n].  Other kinds return PICO_ERR_INVALID_ARG. */
+int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, const pico_material* mats,
+                            const float* V, const float* N, const float* L, const float* u, float* f, float* pdf,
+                            float* sample_L, float* sample_pdf, float* sample_weight, uint32_t* sample_ok);
 
 #ifdef __cplusplus
 }

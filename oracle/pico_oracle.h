@@ -152,6 +152,18 @@ void po_render_pixels(const po_scene* s, const po_camera* cam, uint32_t max_dept
                       uint32_t max_samples, float max_variance,
                       const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels,
                       float* pixels, uint32_t* sample_count, float* variance, int nthreads);
+/* The physical estimator (no reference counterpart; po_physical.c): the BSDF at
+ * unit V, N, L (double), a sample from three uniforms (returns 0 when it leaves
+ * below the surface), and the plain FP64 mean and sample variance of `spp` paths
+ * per listed pixel with both light strategies (0), light sampling alone (1) or
+ * BSDF sampling alone (2). */
+void po_phys_bsdf_eval(int bsdf, const po_material* m, const double* V, const double* N, const double* L,
+                       double* f_rgb, double* pdf);
+int po_phys_bsdf_sample(int bsdf, const po_material* m, const double* V, const double* N, const double* u3,
+                        double* L, double* pdf, double* weight_rgb);
+void po_phys_render_mean(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
+                         const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, int strategy,
+                         double* mean_rgb, double* var_rgb, int nthreads);
 /* Mean/variance recurrence alone, applied to a given sample sequence per pixel. */
 void po_accumulate(const float* samples /* n * 3 */, uint32_t n, uint32_t max_samples,
                    float max_variance, float* pixel, uint32_t* count, float* variance);

@@ -30,6 +30,7 @@ FRAG_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("u", "<f
 
 _vp, _u32, _u64, _i32 = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int
 _fp, _up = C.POINTER(C.c_float), C.POINTER(C.c_uint32)
+_dp = C.POINTER(C.c_double)
 
 
 def build_oracle() -> Path:
@@ -125,6 +126,10 @@ class Oracle(_SceneLib):
             "po_render_pixels": (None, [_vp, C.POINTER(CCamera), _u32, _u32, C.c_float, _up, C.POINTER(_u64),
                                         _u32, _fp, _up, _fp, _i32]),
             "po_accumulate": (None, [_fp, _u32, _u32, C.c_float, _fp, _up, _fp]),
+            "po_phys_bsdf_eval": (None, [_i32, C.POINTER(CMaterial), _dp, _dp, _dp, _dp, _dp]),
+            "po_phys_bsdf_sample": (_i32, [_i32, C.POINTER(CMaterial), _dp, _dp, _dp, _dp, _dp, _dp]),
+            "po_phys_render_mean": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _up, C.POINTER(_u64), _u32, _i32,
+                                           _dp, _dp, _i32]),
             "po_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "po_view_matrix": (None, [C.POINTER(CCamera), _fp]),
             "po_atrous_denoise": (None, [_fp, _fp, _fp, _fp, _u32, _u32, _fp]),
@@ -213,6 +218,25 @@ class Oracle(_SceneLib):
     def direct_lighting_pdf(self, kind, material: Material, N, wi, wo) -> float:
         m = _mat(material)
         return self.lib.po_direct_lighting_pdf(kind, C.byref(m), _f(N), _f(wi), _f(wo))
+
+    def phys_bsdf_eval(self, kind, material: Material, V, N, L):
+        """Physical estimator's BSDF (FP64): (f rgb, pdf) for unit V, N, L."""
+        v, n, l = (np.ascontiguousarray(a, np.float64) for a in (V, N, L))
+        f, pdf = np.empty(3), np.empty(1)
+        m = _mat(material)
+        self.lib.po_phys_bsdf_eval(kind, C.byref(m), v.ctypes.data_as(_dp), n.ctypes.data_as(_dp),
+                                   l.ctypes.data_as(_dp), f.ctypes.data_as(_dp), pdf.ctypes.data_as(_dp))
+        return f, float(pdf[0])
+
+    def phys_bsdf_sample(self, kind, material: Material, V, N, u):
+        """Physical estimator's BSDF sample (FP64) from three uniforms: (ok, L, pdf, weight rgb)."""
+        v, n, uu = (np.ascontiguousarray(a, np.float64) for a in (V, N, u))
+        L, pdf, w = np.empty(3), np.empty(1), np.empty(3)
+        m = _mat(material)
+        ok = self.lib.po_phys_bsdf_sample(kind, C.byref(m), v.ctypes.data_as(_dp), n.ctypes.data_as(_dp),
+                                          uu.ctypes.data_as(_dp), L.ctypes.data_as(_dp), pdf.ctypes.data_as(_dp),
+                                          w.ctypes.data_as(_dp))
+        return bool(ok), L, float(pdf[0]), w
 
     def alias_build(self, weights) -> tuple[np.ndarray, np.ndarray]:
         w = np.ascontiguousarray(weights, np.float32)
@@ -335,6 +359,18 @@ class OracleScene:
                                   pixels.ctypes.data_as(_fp), counts.ctypes.data_as(_up),
                                   variance.ctypes.data_as(_fp), nthreads)
         return pixels, counts, variance
+
+    def phys_render_mean(self, cam, max_depth, spp, pixel_index, seeds, strategy=0, nthreads=0):
+        """Physical estimator: FP64 mean and sample variance of `spp` paths per listed pixel;
+        strategy 0 combines light and BSDF sampling, 1 samples lights alone, 2 the BSDF alone."""
+        idx = np.ascontiguousarray(pixel_index, np.uint32)
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        mean, var = np.empty((len(idx), 3)), np.empty((len(idx), 3))
+        c = cam.to_c()
+        self.lib.po_phys_render_mean(self.handle, C.byref(c), max_depth, spp, idx.ctypes.data_as(_up),
+                                     sd.ctypes.data_as(C.POINTER(_u64)), len(idx), strategy,
+                                     mean.ctypes.data_as(_dp), var.ctypes.data_as(_dp), nthreads)
+        return mean, var
 
     def denoiser_inputs(self, cam):
         W, H = int(cam.resolution[0]), int(cam.resolution[1])

@@ -60,6 +60,8 @@ SIGNATURES = {
     "pico_gpu_hdr_bound": (C.c_size_t, [_u32, _u32]),
     "pico_gpu_encode_hdr": (C.c_int, [_vp, _fp, _u32, _u32, _vp, C.c_size_t, C.POINTER(C.c_size_t)]),
     "pico_gpu_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "pico_gpu_phys_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                          _vp]),
 }
 
 _lib = None
@@ -156,6 +158,25 @@ class Context:
                                                 C.byref(n)), "encode_hdr")
         return buf[:n.value].tobytes()
 
+    def phys_bsdf_eval(self, kinds, materials, V, N, L, u):
+        """The physical estimator's device BSDF: (f, pdf, sample L, sample pdf, sample weight, sample ok)."""
+        from .types import CMaterial
+        n = len(kinds)
+        k = np.ascontiguousarray(kinds, np.uint32)
+        mats = (CMaterial * max(n, 1))()
+        for i, m in enumerate(materials):
+            mats[i].diffuse[:] = list(m.diffuse)
+            mats[i].specular[:] = list(m.specular)
+            mats[i].roughness = m.roughness
+        arr = [np.ascontiguousarray(a, np.float32).reshape(n, 3) for a in (V, N, L, u)]
+        f, sl, sw = (np.empty((n, 3), np.float32) for _ in range(3))
+        pdf, spdf = np.empty(n, np.float32), np.empty(n, np.float32)
+        ok = np.empty(n, np.uint32)
+        self.check(self.lib.pico_gpu_phys_bsdf_eval(self.handle, n, k.ctypes.data, mats, *[a.ctypes.data for a in arr],
+                                                    f.ctypes.data, pdf.ctypes.data, sl.ctypes.data, spdf.ctypes.data,
+                                                    sw.ctypes.data, ok.ctypes.data), "phys_bsdf_eval")
+        return f, pdf, sl, spdf, sw, ok.astype(bool)
+
     def bsdf_eval(self, kinds, materials, V, N, H, xi):
         """Device BSRDF routines on given inputs: (pdf, L, P, energy, direct_pdf)."""
         from .types import CMaterial
@@ -246,8 +267,9 @@ class GpuScene:
 
     def render(self, camera: Camera, max_depth: int, max_samples: int, seed: int = 1, pixels=None,
                sample_count=None, variance=None, max_variance: float = 0.0, denoise: bool = False,
-               tonemap: bool = False, should_quit=None):
-        """Scene::render_scene_to_memory into (H, W, 3) buffers that are updated in place."""
+               tonemap: bool = False, should_quit=None, estimator: int = 0):
+        """Scene::render_scene_to_memory into (H, W, 3) buffers that are updated in place;
+        estimator 1 (ESTIMATOR_PHYSICAL) selects the physical estimator of pico_gpu.h."""
         W, H = int(camera.resolution[0]), int(camera.resolution[1])
         if pixels is None:
             pixels = np.zeros((H, W, 3), np.float32)
@@ -255,7 +277,8 @@ class GpuScene:
             sample_count = np.zeros((H, W), np.uint32)
         if variance is None:
             variance = np.zeros((H, W, 3), np.float32)
-        cfg = CRenderConfig(max_depth, max_samples, max_variance, H, W, int(tonemap), int(denoise), 0, seed)
+        cfg = CRenderConfig(max_depth, max_samples, max_variance, H, W, int(tonemap), int(denoise), int(estimator),
+                            seed)
         cam = camera.to_c()
         quit_flag = should_quit if should_quit is not None else C.c_int32(0)
         self.ctx.check(self.lib.pico_gpu_render(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),

@@ -3,6 +3,7 @@
 // on caller-supplied inputs, so the shading code the integrator runs can be
 // checked against the reference value by value.
 #include "capi_internal.h"
+#include "physical.cuh"
 #include "shade.cuh"
 
 namespace pico {
@@ -35,9 +36,81 @@ __global__ void bsdf_eval_kernel(uint64_t n, const uint32_t* kinds, const GpuMat
     dl_pdf[i] = direct_lighting_pdf(kind, m, nn, v, s.L);
 }
 
+// The physical estimator's BSDF on caller-supplied inputs, through the same
+// device routines the physical shade kernel runs: f and pdf of (V, L) and one
+// sample from three uniforms.
+__global__ void phys_bsdf_kernel(uint64_t n, const uint32_t* kinds, const GpuMaterial* mats, const float* V,
+                                 const float* N, const float* L, const float* u, float* f, float* pdf, float* sl,
+                                 float* spdf, float* sw, uint32_t* sok)
+{
+    using namespace phys;
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Lobes lb = lobes_of(kinds[i], mats[i]);
+    const Frame fr = frame_of(make_float3(N[3 * i], N[3 * i + 1], N[3 * i + 2]));
+    const float3 vl = to_local(fr, make_float3(V[3 * i], V[3 * i + 1], V[3 * i + 2]));
+    float3 fv;
+    eval(lb, vl, to_local(fr, make_float3(L[3 * i], L[3 * i + 1], L[3 * i + 2])), fv, pdf[i]);
+    f[3 * i] = fv.x; f[3 * i + 1] = fv.y; f[3 * i + 2] = fv.z;
+    const Sample s = phys::sample(lb, vl, u[3 * i], u[3 * i + 1], u[3 * i + 2]);
+    const float3 w = to_world(fr, s.l);
+    sl[3 * i] = w.x; sl[3 * i + 1] = w.y; sl[3 * i + 2] = w.z;
+    spdf[i] = s.pdf;
+    sw[3 * i] = s.weight.x; sw[3 * i + 1] = s.weight.y; sw[3 * i + 2] = s.weight.z;
+    sok[i] = s.ok ? 1u : 0u;
+}
+
 }  // namespace pico
 
 using namespace pico;
+
+extern "C" int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds,
+                                       const pico_material* mats, const float* V, const float* N, const float* L,
+                                       const float* u, float* f, float* pdf, float* sample_L, float* sample_pdf,
+                                       float* sample_weight, uint32_t* sample_ok)
+{
+    if (!ctx || (n && (!kinds || !mats || !V || !N || !L || !u || !f || !pdf || !sample_L || !sample_pdf ||
+                       !sample_weight || !sample_ok)))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (n == 0) return PICO_OK;
+    for (uint64_t i = 0; i < n; ++i)
+        if (kinds[i] != PICO_BSDF_DIFFUSE && kinds[i] != PICO_BSDF_SPECULAR && kinds[i] != PICO_BSDF_DIELECTRIC)
+            return set_error(ctx, PICO_ERR_INVALID_ARG, "the physical BSDF covers Diffuse, Specular and Dielectric");
+    cudaSetDevice(ctx->device);
+    std::vector<GpuMaterial> gm(n);
+    for (uint64_t i = 0; i < n; ++i) {
+        GpuMaterial g{};
+        for (int a = 0; a < 3; ++a) {
+            g.diffuse[a] = mats[i].diffuse[a]; g.specular[a] = mats[i].specular[a];
+        }
+        g.roughness = mats[i].roughness;
+        gm[i] = g;
+    }
+    // one device block: [kinds | mats | V | N | L | u | f | pdf | sL | spdf | sw | sok]
+    const size_t fl = sizeof(float);
+    const size_t sizes[] = {n * 4, n * sizeof(GpuMaterial), n * 3 * fl, n * 3 * fl, n * 3 * fl, n * 3 * fl,
+                            n * 3 * fl, n * fl, n * 3 * fl, n * fl, n * 3 * fl, n * 4};
+    size_t off[13] = {0};
+    for (int k = 0; k < 12; ++k) off[k + 1] = off[k] + ((sizes[k] + 255) & ~size_t(255));
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, off[12]);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "bsdf eval buffers");
+    char* b = static_cast<char*>(base);
+    const void* src[] = {kinds, gm.data(), V, N, L, u};
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaMemcpy(b + off[k], src[k], sizes[k], cudaMemcpyHostToDevice);
+    auto F = [&](int k) { return reinterpret_cast<float*>(b + off[k]); };
+    if (e == cudaSuccess) {
+        phys_bsdf_kernel<<<(unsigned)((n + 127) / 128), 128>>>(
+            n, reinterpret_cast<uint32_t*>(b + off[0]), reinterpret_cast<GpuMaterial*>(b + off[1]), F(2), F(3),
+            F(4), F(5), F(6), F(7), F(8), F(9), F(10), reinterpret_cast<uint32_t*>(b + off[11]));
+        e = cudaGetLastError();
+    }
+    void* dst[] = {f, pdf, sample_L, sample_pdf, sample_weight, sample_ok};
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaMemcpy(dst[k], b + off[6 + k], sizes[6 + k], cudaMemcpyDeviceToHost);
+    cudaFree(base);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "physical bsdf eval");
+    return PICO_OK;
+}
 
 extern "C" int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, const pico_material* mats,
                                   const float* V, const float* N, const float* H, const float* xi, float* pdf,

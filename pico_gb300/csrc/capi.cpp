@@ -144,6 +144,8 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
         const uint32_t shape = desc->meshes[desc->instances[i].mesh].shape;
         if (shape == PICO_SHAPE_SPHERE) s->needs_reference_order = true;
         if (shape != PICO_SHAPE_TRIANGLES) implicit = true;
+        const uint32_t kind = desc->instances[i].bsdf;
+        if (kind == PICO_BSDF_BTDF || kind == PICO_BSDF_FRESNEL) s->has_btdf = true;
     }
     s->light_inst_host.reserve(fs.lights.size());
     for (const GpuLight& l : fs.lights) s->light_inst_host.push_back(l.inst);
@@ -169,6 +171,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     const GpuNode* nodes; const GpuTri* tris; const GpuTriShade* tshade; const GpuInstance* insts;
     const GpuInstanceShade* ishade; const uint32_t* irank; const GpuMaterial* mats; const GpuLight* lights;
     const float* law; const uint32_t* lai; const float* lpos; const unsigned char* skypx; const uint32_t* titems;
+    const float* lgeo; const uint32_t* lofi;
     if (e == cudaSuccess) e = upload(fs.nodes, nodes);
     if (e == cudaSuccess) e = upload(fs.tris, tris);
     if (e == cudaSuccess) e = upload(fs.tri_shade, tshade);
@@ -180,6 +183,8 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     if (e == cudaSuccess) e = upload(fs.light_alias_weight, law);
     if (e == cudaSuccess) e = upload(fs.light_alias_index, lai);
     if (e == cudaSuccess) e = upload(fs.light_positions, lpos);
+    if (e == cudaSuccess) e = upload(fs.light_tri_geo, lgeo);
+    if (e == cudaSuccess) e = upload(fs.light_of_inst, lofi);
     if (e == cudaSuccess) e = upload(fs.sky_pixels, skypx);
     if (e == cudaSuccess) e = upload(fs.tlas_items, titems);
     if (e != cudaSuccess) {
@@ -188,7 +193,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     }
     v.nodes = nodes; v.tris = tris; v.tri_shade = tshade; v.insts = insts; v.inst_shade = ishade;
     v.inst_rank = irank; v.tlas_items = titems; v.materials = mats; v.lights = lights; v.light_alias_weight = law;
-    v.light_alias_index = lai; v.light_positions = lpos;
+    v.light_alias_index = lai; v.light_positions = lpos; v.light_tri_geo = lgeo; v.light_of_inst = lofi;
     v.nlights = (uint32_t)fs.lights.size();
     v.tlas_root_ref = fs.tlas_root_ref;
     v.tlas_fast_root_ref = fs.tlas_fast_root_ref;

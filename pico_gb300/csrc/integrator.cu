@@ -17,7 +17,11 @@
 // light hit by the shadow ray counts, Russian roulette runs from depth 0 with
 // survival max(throughput), throughput is multiplied by the sample pdf, and
 // rays leave surfaces 0.01 along the normal (or the light direction).
+//
+// The physical estimator (PICO_ESTIMATOR_PHYSICAL, physical.cuh) shares the
+// batch, queues and extension kernels and replaces shade and the running mean.
 #include "kernels_render.h"
+#include "physical.cuh"
 #include "shade.cuh"
 #include "traverse.cuh"
 
@@ -35,7 +39,8 @@ __device__ __forceinline__ uint32_t warp_append(bool take, uint32_t* counter)
     return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, CameraView cam, unsigned long long seed)
+__global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, CameraView cam, unsigned long long seed,
+                                                               bool physical)
 {
     // whole warps iterate together so the queue append can use warp collectives
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -49,7 +54,13 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
             live = b.done[pixel] == 0;
             Pcg32 rng = path_rng(seed, pixel, b.count[pixel] + s);
             float x0, x1;
-            hammersley(rng, x0, x1);
+            if (physical) {
+                // camera_ray halves its jitter (Camera.cpp:14-15): this covers the whole pixel
+                x0 = 2.0f * rng.uniform();
+                x1 = 2.0f * rng.uniform();
+            } else {
+                hammersley(rng, x0, x1);
+            }
             float4 o, d;
             camera_ray(cam, x0, x1, pixel % b.width, pixel / b.width, o, d);
             b.org[i] = o;
@@ -72,7 +83,15 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
                                               int s, bool shadow)
 {
     const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
-    if (shadow) {
+    if (shadow && b.senergy[i].w == 2.0f) {
+        // physical estimator: the contribution counts unless something lies nearer than scontrib.w
+        const float4 c = b.scontrib[i];
+        if (s == kTraceOk && (rank == kNoHit || h.t >= c.w)) {
+            float4 p = b.pay[i];
+            p.x += c.x; p.y += c.y; p.z += c.z;
+            b.pay[i] = p;
+        }
+    } else if (shadow) {
         // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176);
         // a sun ray (senergy.w = 1) adds the sun colour when it escapes (Integrators.cpp:60-76)
         const float4 e = b.senergy[i];
@@ -258,6 +277,181 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
     }
 }
 
+// The physical estimator's shade step.  Path state: thr.w is the density with
+// which the current ray's direction was sampled (0 for camera rays and mirror
+// bounces, whose emission is not weighted); a shadow record carries its finished
+// contribution in scontrib.xyz, the distance from which a hit no longer occludes
+// in scontrib.w, and senergy.w = 2.
+__global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneView sc, PathBatch b, int cur,
+                                                                       uint32_t depth, uint32_t max_depth)
+{
+    using namespace phys;
+    const uint32_t n = b.counters[cur];
+    const uint32_t nxt = cur ^ 1;
+    const uint32_t nl = sc.nlights + (sc.use_sun ? 1u : 0u);
+    const float4* light_geo = reinterpret_cast<const float4*>(sc.light_tri_geo);
+    // whole warps iterate together so the queue appends can use warp collectives
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t k = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool cont = false, shadow = false;
+        uint32_t i = 0;
+        if (k < n) {
+            i = b.queue[cur][k];
+            const float4 hit = b.hit[i];
+            const uint32_t rank = __float_as_uint(hit.w);
+            float4 thr = b.thr[i], pay = b.pay[i];
+            const float4 dir = b.dir[i];
+            if (rank == kNoHit) {
+                const float3 sk = sky_radiance(sc, dir.x, dir.y, dir.z);
+                pay.x += thr.x * sk.x; pay.y += thr.y * sk.y; pay.z += thr.z * sk.z;
+                b.pay[i] = pay;
+            } else {
+                const uint32_t inst = sc.insts[rank].inst_id;
+                const GpuInstanceShade is = sc.inst_shade[inst];
+                const GpuMaterial m = sc.materials[is.material];
+                if (is.bsdf == PICO_BSDF_LIGHT) {
+                    // emission, weighted against the light sample that could have reached this point
+                    float w = 1.0f;
+                    const uint32_t li = sc.light_of_inst[inst];
+                    const uint32_t tri = b.hit_tri[i];
+                    if (thr.w > 0.0f && li != ~0u && tri != kImplicitTri &&
+                        sc.lights[li].shape == PICO_SHAPE_TRIANGLES) {
+                        const float4 g = light_geo[sc.lights[li].tri_base + sc.tris[tri].prim];
+                        const float cl = fabsf(g.x * dir.x + g.y * dir.y + g.z * dir.z);
+                        const float pl = g.w * hit.x * hit.x / (cl * (float)nl);   // +inf at cl = 0
+                        w = mis_weight(thr.w, pl);
+                    }
+                    pay.x += thr.x * m.emissive[0] * w;
+                    pay.y += thr.y * m.emissive[1] * w;
+                    pay.z += thr.z * m.emissive[2] * w;
+                    b.pay[i] = pay;
+                } else if (depth < max_depth) {
+                    Pcg32 rng{b.rng[i]};
+                    const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z, b.org[i], dir);
+                    float3 nrm = normalize3(make_float3(f.n.x, f.n.y, f.n.z));
+                    const float3 v = make_float3(-dir.x, -dir.y, -dir.z);
+                    if (dot3(nrm, v) < 0.0f) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+                    const float eps = ray_offset(f.px, f.py, f.pz);
+                    const float4 org = make_float4(f.px + eps * nrm.x, f.py + eps * nrm.y, f.pz + eps * nrm.z, f.pw);
+                    float3 L, weight;
+                    float pdf_next = 0.0f;
+                    bool ok;
+                    if (is.bsdf == PICO_BSDF_DELTA) {
+                        // a mirror with Schlick reflectance; its emission is not weighted
+                        const float c = dot3(nrm, v);
+                        L = make_float3(2.0f * c * nrm.x - v.x, 2.0f * c * nrm.y - v.y, 2.0f * c * nrm.z - v.z);
+                        weight = make_float3(schlick(m.specular[0], c), schlick(m.specular[1], c),
+                                             schlick(m.specular[2], c));
+                        ok = c > 0.0f;
+                    } else {
+                        const Frame fr = frame_of(nrm);
+                        const float3 vl = to_local(fr, v);
+                        const Lobes lb = lobes_of(is.bsdf, m);
+                        // next-event estimation towards one uniformly chosen light (the sun last)
+                        if (nl > 0) {
+                            uint32_t li = (uint32_t)(rng.uniform() * (float)nl);
+                            if (li >= nl) li = nl - 1;
+                            float3 wi = make_float3(0.0f, 0.0f, 0.0f), c = wi;
+                            float reach = 0.0f;
+                            if (sc.use_sun && li == nl - 1) {
+                                wi = normalize3(make_float3(-sc.sun_dir[0], -sc.sun_dir[1], -sc.sun_dir[2]));
+                                const float3 wl = to_local(fr, wi);
+                                if (wl.z > 0.0f) {
+                                    float3 fv;
+                                    float pb;
+                                    eval(lb, vl, wl, fv, pb);
+                                    const float kk = wl.z * (float)nl;
+                                    c = make_float3(thr.x * fv.x * sc.sun_col[0] * kk, thr.y * fv.y * sc.sun_col[1] * kk,
+                                                    thr.z * fv.z * sc.sun_col[2] * kk);
+                                    reach = __int_as_float(0x7f800000);   // only an escaping ray sees the sun
+                                    shadow = true;
+                                }
+                            } else if (sc.lights[li].shape == PICO_SHAPE_TRIANGLES) {
+                                const GpuLight Lt = sc.lights[li];
+                                const uint32_t bucket = rng.next() % Lt.ntris;
+                                const float coin = (float)rng.next() / 4294967296.0f;
+                                const uint32_t t = coin <= sc.light_alias_weight[Lt.tri_base + bucket]
+                                                       ? bucket
+                                                       : sc.light_alias_index[Lt.tri_base + bucket];
+                                const float su0 = sqrtf(rng.uniform()), x1 = rng.uniform();
+                                const float bx = 1.0f - su0, by = x1 * su0, w0 = 1.0f - bx - by;
+                                const float* lp = sc.light_positions + 9 * (size_t)(Lt.tri_base + t);
+                                const float sx = w0 * lp[0] + bx * lp[3] + by * lp[6];
+                                const float sy = w0 * lp[1] + bx * lp[4] + by * lp[7];
+                                const float sz = w0 * lp[2] + bx * lp[5] + by * lp[8];
+                                const float4* lip = reinterpret_cast<const float4*>(sc.insts + sc.inst_rank[Lt.inst]);
+                                const float4 r0 = __ldg(lip + 3), r1 = __ldg(lip + 4), r2 = __ldg(lip + 5);
+                                const float yx = r0.x * sx + r0.y * sy + r0.z * sz + r0.w;
+                                const float yy = r1.x * sx + r1.y * sy + r1.z * sz + r1.w;
+                                const float yz = r2.x * sx + r2.y * sy + r2.z * sz + r2.w;
+                                const float3 dd = make_float3(yx - org.x, yy - org.y, yz - org.z);
+                                const float dist2 = dot3(dd, dd), dist = sqrtf(dist2);
+                                wi = make_float3(dd.x / dist, dd.y / dist, dd.z / dist);
+                                const float4 g = light_geo[Lt.tri_base + t];
+                                const float cl = fabsf(g.x * wi.x + g.y * wi.y + g.z * wi.z);
+                                const float3 wl = to_local(fr, wi);
+                                if (wl.z > 0.0f && cl > 0.0f && g.w > 0.0f && dist > 0.0f) {
+                                    const float pl = g.w * dist2 / (cl * (float)nl);
+                                    float3 fv;
+                                    float pb;
+                                    eval(lb, vl, wl, fv, pb);
+                                    const float kk = wl.z * mis_weight(pl, pb) / pl;
+                                    const float* le = sc.materials[sc.inst_shade[Lt.inst].material].emissive;
+                                    c = make_float3(thr.x * fv.x * le[0] * kk, thr.y * fv.y * le[1] * kk,
+                                                    thr.z * fv.z * le[2] * kk);
+                                    reach = dist * (1.0f - 1e-4f);
+                                    shadow = true;
+                                }
+                            }
+                            if (shadow) {
+                                b.sorg[i] = org;
+                                b.sdir[i] = make_float4(wi.x, wi.y, wi.z, 10000.0f);
+                                b.scontrib[i] = make_float4(c.x, c.y, c.z, reach);
+                                b.senergy[i] = make_float4(0.0f, 0.0f, 0.0f, 2.0f);
+                            }
+                        }
+                        const float u0 = rng.uniform(), u1 = rng.uniform(), u2 = rng.uniform();
+                        const Sample smp = phys::sample(lb, vl, u0, u1, u2);
+                        ok = smp.ok;
+                        L = to_world(fr, smp.l);
+                        weight = smp.weight;
+                        pdf_next = smp.pdf;
+                    }
+                    if (ok) {
+                        thr.x *= weight.x; thr.y *= weight.y; thr.z *= weight.z;
+                        bool live = true;
+                        if (depth >= 3) {   // Russian roulette from the fourth vertex
+                            const float q = fminf(0.95f, fmaxf(thr.x, fmaxf(thr.y, thr.z)));
+                            live = rng.uniform() < q;
+                            if (live) { thr.x /= q; thr.y /= q; thr.z /= q; }
+                        }
+                        if (!(isfinite(thr.x) && isfinite(thr.y) && isfinite(thr.z))) {
+                            pay.x = __int_as_float(0x7fffffff);   // shows as pink
+                            b.pay[i] = pay;
+                            live = false;
+                        }
+                        if (live) {
+                            thr.w = pdf_next;
+                            b.thr[i] = thr;
+                            b.org[i] = org;
+                            b.dir[i] = make_float4(L.x, L.y, L.z, dir.w);
+                            b.depth[i] = depth + 1;
+                            cont = true;
+                        }
+                    }
+                    b.rng[i] = rng.state;
+                }
+            }
+        }
+        const uint32_t at = warp_append(cont, &b.counters[nxt]);
+        if (cont) b.queue[nxt][at] = i;
+        const uint32_t sat = warp_append(shadow, &b.counters[2]);
+        if (shadow) b.shadow_queue[sat] = i;
+    }
+}
+
 __global__ void __launch_bounds__(kRenderThreads) finish_kernel(PathBatch b)
 {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < b.n; i += gridDim.x * blockDim.x) {
@@ -268,8 +462,9 @@ __global__ void __launch_bounds__(kRenderThreads) finish_kernel(PathBatch b)
 }
 
 // Scene.cpp:173-198 for each pixel of the batch, samples in order, exact float ops.
+// The physical estimator keeps a plain running mean (1 / (n + 1)) and never stops early.
 __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b, uint32_t spb, uint32_t max_samples,
-                                                                   float max_variance)
+                                                                   float max_variance, bool physical)
 {
     using namespace ex;
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < b.npix; slot += gridDim.x * blockDim.x) {
@@ -288,7 +483,8 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
                 cnt = 1;
                 var[0] = var[1] = var[2] = 0.0f;
             } else {
-                const float f = div(1.0f, (float)prev), g = div(1.0f, (float)(prev + 1));
+                const float g = div(1.0f, (float)(prev + 1));
+                const float f = physical ? g : div(1.0f, (float)prev);
                 for (int c = 0; c < 3; ++c) {
                     const float pp = px[c];
                     const float np = add(pp, mul(sub(x[c], pp), f));
@@ -298,7 +494,8 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
                 cnt = prev + 1;
             }
             px[0] = x[0]; px[1] = x[1]; px[2] = x[2];
-            if (prev > 4 && var[0] <= max_variance && var[1] <= max_variance && var[2] <= max_variance) {
+            if (!physical && prev > 4 && var[0] <= max_variance && var[1] <= max_variance &&
+                var[2] <= max_variance) {
                 b.done[pixel] = 1;
                 break;
             }
@@ -375,11 +572,12 @@ static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, 
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                DeviceStatus* status, int order, cudaStream_t st)
+                                int estimator, DeviceStatus* status, int order, cudaStream_t st)
 {
+    const bool physical = estimator == PICO_ESTIMATOR_PHYSICAL;
     cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed);
+    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
     const bool trace_last =
         sc.sky_kind != PICO_SKY_CONSTANT || sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
     int cur = 0;
@@ -393,8 +591,12 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
-        shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
-                                                                                trace_last);
+        if (physical)
+            shade_physical_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth,
+                                                                                         max_depth);
+        else
+            shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
+                                                                                    trace_last);
         if (depth < max_depth) {
             e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
             if (e != cudaSuccess) return e;
@@ -406,7 +608,8 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         cur ^= 1;
     }
     finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
-    accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance);
+    accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,
+                                                                                    physical);
     return cudaGetLastError();
 }
 

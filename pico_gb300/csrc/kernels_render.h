@@ -38,7 +38,7 @@ struct PathBatch {
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                DeviceStatus* status, int order, cudaStream_t st);
+                                int estimator, DeviceStatus* status, int order, cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
 // Floats of a-trous scratch per 64 x 64 tile: four partial statistics records

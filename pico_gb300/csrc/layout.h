@@ -108,6 +108,8 @@ struct SceneView {
     const float* light_alias_weight;    // per light triangle
     const uint32_t* light_alias_index;  // per light triangle (alias, local index)
     const float* light_positions;       // per light triangle: v0, v1, v2 (9 floats)
+    const float* light_tri_geo;         // per light triangle: world unit normal, area pdf (4 floats)
+    const uint32_t* light_of_inst;      // original instance index -> light index, or ~0u
     uint32_t nlights;
     uint32_t tlas_root_ref;             // the reference's TLAS boxes
     float tlas_lo[3], tlas_hi[3];

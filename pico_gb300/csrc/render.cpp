@@ -141,6 +141,10 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (cfg->width != camera->resolution[0] || cfg->height != camera->resolution[1])
         return set_error(ctx, PICO_ERR_INVALID_ARG, "render size differs from the camera resolution");
+    if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && cfg->estimator != PICO_ESTIMATOR_PHYSICAL)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "unknown estimator");
+    if (cfg->estimator == PICO_ESTIMATOR_PHYSICAL && scene->has_btdf)
+        return set_error(ctx, PICO_ERR_UNSUPPORTED, "the physical estimator has no Transparent or Fresnel lobes");
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
@@ -199,7 +203,8 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
                 b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
                 b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
                 e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
-                                        cfg->max_variance, ctx->status, scene_order(ctx, scene), st);
+                                        cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene),
+                                        st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
                 if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
             }

@@ -435,6 +435,42 @@ void mat4_inverse(const float* mf, float* out)
         for (int r = 0; r < 4; ++r) out[c * 4 + r] = inv[c][r] * o;
 }
 
+// For the physical estimator: per light triangle its world-space unit normal and
+// the area density of a light sample, p(triangle) / world area, where p is the
+// probability with which the alias table (sampled as AliasTable::sample,
+// Util/AliasTable.cpp:89-104: a uniform bucket, then the bucket or its alias by
+// a coin against the bucket's weight) returns the triangle.
+static void light_triangle_geometry(const pico_mesh& m, const float* T, const std::vector<float>& bw,
+                                    const std::vector<uint32_t>& ba, std::vector<float>& out)
+{
+    const size_t n = bw.size();
+    std::vector<double> p(n, 0.0);
+    for (size_t b = 0; b < n; ++b) {
+        const double keep = std::min(1.0, std::max(0.0, (double)bw[b]));
+        p[b] += keep / (double)n;
+        if (ba[b] < n) p[ba[b]] += (1.0 - keep) / (double)n;
+    }
+    for (size_t t = 0; t < n; ++t) {
+        double e[2][3];
+        const float* a = m.positions + 3 * m.indices[3 * t];
+        for (int k = 0; k < 2; ++k) {
+            const float* q = m.positions + 3 * m.indices[3 * t + 1 + k];
+            for (int r = 0; r < 3; ++r)
+                e[k][r] = (double)T[0 * 4 + r] * ((double)q[0] - a[0]) + (double)T[1 * 4 + r] * ((double)q[1] - a[1]) +
+                          (double)T[2 * 4 + r] * ((double)q[2] - a[2]);
+        }
+        const double c[3] = {e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                             e[0][0] * e[1][1] - e[0][1] * e[1][0]};
+        const double len = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        const double area = 0.5 * len;
+        if (area > 0.0 && std::isfinite(area)) {
+            out.insert(out.end(), {(float)(c[0] / len), (float)(c[1] / len), (float)(c[2] / len), (float)(p[t] / area)});
+        } else {
+            out.insert(out.end(), {0.0f, 0.0f, 1.0f, 0.0f});
+        }
+    }
+}
+
 std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
 {
     if (desc.nmeshes && !desc.meshes) return "meshes is NULL";
@@ -644,10 +680,12 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
     }
 
     // ---- NEE lights (Scene.cpp:406-412: every "Light" instance, in order) -----
+    fs.light_of_inst.assign(desc.ninstances, ~0u);
     for (uint32_t i = 0; i < desc.ninstances; ++i) {
         const pico_instance& in = desc.instances[i];
         if (in.bsdf != PICO_BSDF_LIGHT) continue;
         const pico_mesh& m = desc.meshes[in.mesh];
+        fs.light_of_inst[i] = (uint32_t)fs.lights.size();
         if (m.shape != PICO_SHAPE_TRIANGLES) {   // sampled by the shape itself (sample_geometry)
             fs.lights.push_back(GpuLight{i, 0, 0, m.shape});
             continue;
@@ -665,6 +703,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         std::vector<float> bw;
         std::vector<uint32_t> ba;
         alias_build(w, bw, ba);
+        light_triangle_geometry(m, in.transform, bw, ba, fs.light_tri_geo);
         fs.light_alias_weight.insert(fs.light_alias_weight.end(), bw.begin(), bw.end());
         fs.light_alias_index.insert(fs.light_alias_index.end(), ba.begin(), ba.end());
         fs.lights.push_back(l);

@@ -24,6 +24,8 @@ struct FlatScene {
     std::vector<float> light_alias_weight;
     std::vector<uint32_t> light_alias_index;
     std::vector<float> light_positions;
+    std::vector<float> light_tri_geo;     // per light triangle: world unit normal, area pdf (4 floats)
+    std::vector<uint32_t> light_of_inst;  // original instance index -> NEE light index, or ~0u
     uint32_t tlas_root_ref = PICO_REF_EMPTY;
     float tlas_lo[3] = {0, 0, 0}, tlas_hi[3] = {0, 0, 0};
     uint32_t tlas_fast_root_ref = PICO_REF_EMPTY;   // refitted TLAS for the near-first walk

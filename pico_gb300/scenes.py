@@ -21,8 +21,8 @@ from __future__ import annotations
 
 import numpy as np
 
-from .types import (BTDF, DELTA, DIELECTRIC, DIFFUSE, FRESNEL, LIGHT, RAY_DTYPE, SHAPE_CUBE, SHAPE_SPHERE, Camera,
-                    Instance, Material, Mesh, SceneData)
+from .types import (BTDF, DELTA, DIELECTRIC, DIFFUSE, FRESNEL, LIGHT, RAY_DTYPE, SHAPE_CUBE, SHAPE_SPHERE, SKY_CONSTANT,
+                    Camera, Instance, Material, Mesh, SceneData, Sky)
 
 
 # ----------------------------------------------------------------------------- matrices
@@ -259,6 +259,26 @@ def cornell_shapes() -> SceneData:
                     Instance(sph, place((0.2, 0.8, 0.7), 0.1), LIGHT, lamp),
                     Instance(cub, place((0.8, 0.85, 0.3), 0.08), LIGHT, lamp)]
     return s
+
+
+def glossy_field(n_instances: int = 48, level: int = 2, seed: int = 21) -> SceneData:
+    """A small lit field for the physical estimator: metalness-roughness spheres, one of
+    them a Specular_Delta mirror, a Lambert ground, three quad lights, a constant blue sky
+    and a sun."""
+    s = lit_field(n_instances=n_instances, level=level, seed=seed, n_lights=3, extent=8.0)
+    mirror = len(s.materials)
+    s.materials.append(Material(specular=(0.9, 0.9, 0.9)))
+    s.instances[0].bsdf = DELTA
+    s.instances[0].material = mirror
+    s.sky = (0.10, 0.15, 0.25)
+    d = np.array([0.3, -1.0, 0.2])
+    s.sky_image = Sky(SKY_CONSTANT, None, True, tuple(d / np.linalg.norm(d)), (2.0, 1.8, 1.5))
+    return s
+
+
+def glossy_field_camera(width: int = 64, height: int = 48) -> Camera:
+    return Camera(position=(0.0, 4.0, -24.0), direction=(0.0, -0.12, 1.0), resolution=(width, height),
+                  aspect=width / height)
 
 
 def lit_field_camera(width: int = 1920, height: int = 1080) -> Camera:

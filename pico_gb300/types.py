@@ -16,6 +16,8 @@ import numpy as np
 DIFFUSE, SPECULAR, DIELECTRIC, BTDF, LIGHT, FRESNEL, DELTA = 0, 1, 2, 3, 4, 5, 6
 # Mesh shapes (pico_shape).
 SHAPE_TRIANGLES, SHAPE_SPHERE, SHAPE_CUBE = 0, 1, 2
+# Render estimators (pico_estimator).
+ESTIMATOR_REFERENCE, ESTIMATOR_PHYSICAL = 0, 1
 
 RAY_DTYPE = np.dtype([("org", "<f4", (4,)), ("dir", "<f4", (4,))])
 HIT_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -65,7 +67,7 @@ class CCamera(C.Structure):
 class CRenderConfig(C.Structure):
     _fields_ = [("max_ray_depth", C.c_uint32), ("max_samples", C.c_uint32), ("max_variance", C.c_float),
                 ("height", C.c_uint32), ("width", C.c_uint32), ("tonemap", C.c_int32),
-                ("denoise", C.c_int32), ("reserved", C.c_uint32), ("seed", C.c_uint64)]
+                ("denoise", C.c_int32), ("estimator", C.c_uint32), ("seed", C.c_uint64)]
 
 
 @dataclass

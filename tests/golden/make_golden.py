@@ -345,7 +345,8 @@ def shapes_fixtures(ref):
 def judge_fixtures(ref, spp: int = 4096):
     """Converged judges: `spp` reference samples per pixel summed in FP64, on 4096 seeded
     pixels of the 256 x 256 Cornell box (depth 5) and 1024 of the 1920 x 1080 lit field
-    (depth 8)."""
+    (depth 8); and for the physical estimator, which the reference lacks, `spp` samples of
+    the FP64 oracle on the same lit-field pixels."""
     from judge import relmse, scene_digest
     out = {}
     cases = [("cornell", scenes.cornell_box(), scenes.cornell_camera(256, 256), 5, 4096, 601),
@@ -366,6 +367,18 @@ def judge_fixtures(ref, spp: int = 4096):
         out.update({f"{name}_idx": idx, f"{name}_mean": mean, f"{name}_var": var, f"{name}_spp": np.array(spp),
                     f"{name}_depth": np.array(depth), f"{name}_res": np.array([W, H]),
                     f"{name}_digest": np.array(scene_digest(scene))})
+    # the physical estimator has no reference counterpart: its judge is the FP64 oracle
+    oracle = pico_oracle.Oracle()
+    scene, cam = scenes.lit_field(), scenes.lit_field_camera(1920, 1080)
+    rng = np.random.default_rng(603)
+    idx = out["lit_idx"]
+    mean, var = oracle.scene(scene).phys_render_mean(cam, 8, spp, idx,
+                                                     rng.integers(1, 2**63, len(idx), dtype=np.uint64))
+    print(f"judge lit_phys: {len(idx)} pixels x {spp} spp (oracle)")
+    out.update({"lit_phys_idx": idx, "lit_phys_mean": mean, "lit_phys_var": var, "lit_phys_spp": np.array(spp),
+                "lit_phys_depth": np.array(8), "lit_phys_res": np.array([1920, 1080]),
+                "lit_phys_digest": out["lit_digest"], "lit_phys_ref64_exited": np.array(0),
+                "lit_phys_ref64_relmse": np.array(np.nan)})
     np.savez_compressed(HERE / "judge.npz", **out)
 
 
