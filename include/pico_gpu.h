@@ -152,7 +152,16 @@ typedef struct {
  * reflectance) instances are supported; a scene with Transparent or Fresnel
  * instances returns PICO_ERR_UNSUPPORTED.  Emitters are two-sided; the sun is a
  * directional light whose colour is its irradiance. */
-enum pico_estimator { PICO_ESTIMATOR_REFERENCE = 0, PICO_ESTIMATOR_PHYSICAL = 1 };
+enum pico_estimator {
+    PICO_ESTIMATOR_REFERENCE = 0,
+    PICO_ESTIMATOR_PHYSICAL = 1,
+    /* No counterpart in the reference: the physical estimator whose camera paths
+     * end after one bounce (two when the first vertex has roughness < 0.1) in the
+     * context's neural radiance cache (pico_gpu_set_radiance_cache), which every
+     * sample pass first trains on full-depth physical paths.  See the radiance
+     * cache section below. */
+    PICO_ESTIMATOR_RADIANCE_CACHE = 2
+};
 typedef struct {
     uint32_t max_ray_depth;
     uint32_t max_samples;
@@ -274,6 +283,81 @@ int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, con
 int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds, const pico_material* mats,
                             const float* V, const float* N, const float* L, const float* u, float* f, float* pdf,
                             float* sample_L, float* sample_pdf, float* sample_weight, uint32_t* sample_ok);
+
+/* ---- neural radiance cache ------------------------------------------------
+ * No counterpart in the reference (Mueller et al. 2021, "Real-time neural
+ * radiance caching for path tracing").  A cache maps a surface point to the
+ * radiance it reflects towards a direction (its own emission excluded):
+ *
+ *   inputs   position in the cache's box through a 16-level multiresolution
+ *            hash grid (Mueller et al. 2022; 2 fp16 features per level,
+ *            2^log2_table_size entries per level, resolutions from
+ *            base_resolution to max_resolution in geometric steps, dense
+ *            indexing where a level fits its table), the direction through
+ *            real spherical harmonics of degrees 0-3 (16 values), the normal,
+ *            roughness and albedo (diffuse + specular colour), a constant 1
+ *            and zero padding: 64 values;
+ *   network  5 hidden layers of 64 ReLU units and 3 linear outputs, bf16
+ *            weights and activations, fp32 accumulation on the tensor cores;
+ *   training relative L2 loss sum_c (y_c - t_c)^2 / (y_c^2 + 0.01), the
+ *            denominator held constant, averaged over the batch and channels;
+ *            Adam over the fp32 master weights and grid features.
+ *
+ * Parameters for pico_gpu_nrc_get_params / set_params: the network as
+ * 6 x 64 x 64 floats (layer, output, input; layer 5 uses outputs 0-2, the
+ * other rows are ignored and kept 0) and the grid as levels x entries x 2
+ * floats (16 x 2^log2_table_size x 2). */
+typedef struct pico_gpu_nrc pico_gpu_nrc;
+
+typedef struct {
+    float position[3];
+    float direction[3];             /* unit, towards the viewer */
+    float normal[3];
+    float roughness;
+    float albedo[3];
+    uint32_t payload;               /* carried through, unused by the network */
+    uint32_t pad[2];
+} pico_nrc_query;                   /* 64 bytes */
+
+typedef struct {
+    uint32_t log2_table_size;       /* [10, 22]; 19 */
+    float base_resolution, max_resolution;   /* 16, 4096 */
+    float aabb_min[3], aabb_max[3]; /* the box the grid covers; a render with an empty box uses the scene's bounds */
+    float learning_rate, beta1, beta2, epsilon;   /* 1e-2, 0.9, 0.99, 1e-15 */
+    uint32_t train_paths;           /* training paths per sample pass of a render: 65536 */
+    uint32_t train_batch;           /* records per optimiser step: 65536, at most 2^20 */
+    uint32_t max_train_steps;       /* optimiser steps per sample pass: 4 */
+    uint32_t warmup_frames;         /* training-only passes before a render's first sample: 0 */
+    uint64_t seed;                  /* initial weights and training-path streams */
+} pico_nrc_config;
+
+int pico_gpu_nrc_default_config(pico_nrc_config* out);
+int pico_gpu_nrc_create(pico_gpu_ctx* ctx, const pico_nrc_config* config, pico_gpu_nrc** out);
+void pico_gpu_nrc_free(pico_gpu_nrc* cache);
+int pico_gpu_nrc_get_params(pico_gpu_nrc* cache, float* mlp, float* grid);
+/* Replaces the parameters and resets the optimiser state. */
+int pico_gpu_nrc_set_params(pico_gpu_nrc* cache, const float* mlp, const float* grid);
+int pico_gpu_nrc_set_bounds(pico_gpu_nrc* cache, const float* aabb_min, const float* aabb_max);
+/* [0] optimiser steps, [1] grid entries, [2] network parameters (incl. padding), [3] frames rendered. */
+int pico_gpu_nrc_info(const pico_gpu_nrc* cache, uint64_t* out4);
+/* The 64 network inputs of n queries (n * 64 floats, before their bf16 rounding). */
+int pico_gpu_nrc_encode(pico_gpu_nrc* cache, const pico_nrc_query* queries, uint64_t n, float* out);
+/* Network outputs (n * 3 floats) of n <= 2^26 queries. */
+int pico_gpu_nrc_infer(pico_gpu_nrc* cache, const pico_nrc_query* queries, uint64_t n, float* rgb);
+int pico_gpu_nrc_infer_device(pico_gpu_nrc* cache, const pico_nrc_query* d_queries, uint64_t n, float* d_rgb,
+                              void* stream);
+/* One optimiser step on n <= 2^20 records (targets: n * 3 floats; the device
+ * variant takes n * 4 floats, the fourth unused); with apply = 0 only the
+ * gradients are computed (pico_gpu_nrc_gradients reads them).  *loss receives
+ * the batch's mean loss. */
+int pico_gpu_nrc_train(pico_gpu_nrc* cache, const pico_nrc_query* queries, const float* targets, uint64_t n,
+                       int apply, float* loss);
+int pico_gpu_nrc_train_device(pico_gpu_nrc* cache, const pico_nrc_query* d_queries, const float* d_targets,
+                              uint64_t n, int apply, void* stream);
+/* Gradients of the last training call: network (6 x 64 x 64) and grid (levels x entries x 2). */
+int pico_gpu_nrc_gradients(pico_gpu_nrc* cache, float* mlp_grad, float* grid_grad);
+/* The cache PICO_ESTIMATOR_RADIANCE_CACHE renders of this context use (NULL: none). */
+int pico_gpu_set_radiance_cache(pico_gpu_ctx* ctx, pico_gpu_nrc* cache);
 
 #ifdef __cplusplus
 }

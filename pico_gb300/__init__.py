@@ -20,7 +20,7 @@ import numpy as np
 
 from .types import (SKY_CONSTANT, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF, Sky, SHAPE_TRIANGLES, SHAPE_SPHERE,  # noqa: F401
                     SHAPE_CUBE, BTDF, FRESNEL, DELTA,  # noqa: F401
-                    CCamera, CRenderConfig, CSceneDesc, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
+                    CCamera, CNrcConfig, CRenderConfig, CSceneDesc, NRC_QUERY_DTYPE, ESTIMATOR_RADIANCE_CACHE, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
                     MarshalledScene, Material, Mesh, SceneData, DIFFUSE, SPECULAR, DIELECTRIC, LIGHT, MISS)
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpico_gpu.so"
@@ -62,6 +62,20 @@ SIGNATURES = {
     "pico_gpu_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "pico_gpu_phys_bsdf_eval": (C.c_int, [_vp, _u64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                           _vp]),
+    "pico_gpu_nrc_default_config": (C.c_int, [C.POINTER(CNrcConfig)]),
+    "pico_gpu_nrc_create": (C.c_int, [_vp, C.POINTER(CNrcConfig), C.POINTER(_vp)]),
+    "pico_gpu_nrc_free": (None, [_vp]),
+    "pico_gpu_nrc_get_params": (C.c_int, [_vp, _vp, _vp]),
+    "pico_gpu_nrc_set_params": (C.c_int, [_vp, _vp, _vp]),
+    "pico_gpu_nrc_set_bounds": (C.c_int, [_vp, _fp, _fp]),
+    "pico_gpu_nrc_info": (C.c_int, [_vp, C.POINTER(_u64)]),
+    "pico_gpu_nrc_encode": (C.c_int, [_vp, _vp, _u64, _vp]),
+    "pico_gpu_nrc_infer": (C.c_int, [_vp, _vp, _u64, _vp]),
+    "pico_gpu_nrc_infer_device": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "pico_gpu_nrc_train": (C.c_int, [_vp, _vp, _vp, _u64, C.c_int, _fp]),
+    "pico_gpu_nrc_train_device": (C.c_int, [_vp, _vp, _vp, _u64, C.c_int, _vp]),
+    "pico_gpu_nrc_gradients": (C.c_int, [_vp, _vp, _vp]),
+    "pico_gpu_set_radiance_cache": (C.c_int, [_vp, _vp]),
 }
 
 _lib = None
@@ -307,3 +321,100 @@ class GpuScene:
         self.ctx.check(self.lib.pico_gpu_denoiser_inputs(self.ctx.handle, self.handle, C.byref(cam), _f32(n),
                                                          _f32(p), _f32(d)), "denoiser_inputs")
         return n, p, d
+
+
+class RadianceCache:
+    """pico_gpu_nrc: a neural radiance cache on the context's device (see pico_gpu.h)."""
+
+    LEVELS, WIDTH, LAYERS = 16, 64, 6
+
+    def __init__(self, ctx: Context, **overrides):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        cfg = CNrcConfig()
+        self.lib.pico_gpu_nrc_default_config(C.byref(cfg))
+        for k, v in overrides.items():
+            if k in ("aabb_min", "aabb_max"):
+                getattr(cfg, k)[:] = [float(x) for x in v]
+            else:
+                setattr(cfg, k, v)
+        self.config = cfg
+        h = _vp()
+        ctx.check(self.lib.pico_gpu_nrc_create(ctx.handle, C.byref(cfg), C.byref(h)), "nrc_create")
+        self.handle = h
+        self.table_size = 1 << cfg.log2_table_size
+
+    def free(self):
+        if getattr(self, "handle", None):
+            self.lib.pico_gpu_nrc_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def params(self):
+        """(network (6, 64, 64) float32, grid (16, T, 2) float32) master parameters."""
+        mlp = np.empty((self.LAYERS, self.WIDTH, self.WIDTH), np.float32)
+        grid = np.empty((self.LEVELS, self.table_size, 2), np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_get_params(self.handle, mlp.ctypes.data, grid.ctypes.data), "nrc_params")
+        return mlp, grid
+
+    def set_params(self, mlp, grid):
+        m = np.ascontiguousarray(mlp, np.float32)
+        g = np.ascontiguousarray(grid, np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_set_params(self.handle, m.ctypes.data, g.ctypes.data), "nrc_set_params")
+
+    def set_bounds(self, lo, hi):
+        a = np.ascontiguousarray(lo, np.float32)
+        b = np.ascontiguousarray(hi, np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_set_bounds(self.handle, _f32(a), _f32(b)), "nrc_set_bounds")
+
+    def info(self) -> dict:
+        out = (C.c_uint64 * 4)()
+        self.ctx.check(self.lib.pico_gpu_nrc_info(self.handle, out), "nrc_info")
+        return dict(zip(["steps", "grid_entries", "mlp_params", "frames"], [int(x) for x in out]))
+
+    def encode(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, NRC_QUERY_DTYPE)
+        out = np.empty((len(q), self.WIDTH), np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_encode(self.handle, q.ctypes.data, len(q), out.ctypes.data),
+                       "nrc_encode")
+        return out
+
+    def infer(self, queries: np.ndarray) -> np.ndarray:
+        q = np.ascontiguousarray(queries, NRC_QUERY_DTYPE)
+        out = np.empty((len(q), 3), np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_infer(self.handle, q.ctypes.data, len(q), out.ctypes.data), "nrc_infer")
+        return out
+
+    def infer_device(self, d_queries: int, n: int, d_rgb: int, stream: int = 0):
+        self.ctx.check(self.lib.pico_gpu_nrc_infer_device(self.handle, d_queries, n, d_rgb, stream or None),
+                       "nrc_infer_device")
+
+    def train(self, queries: np.ndarray, targets: np.ndarray, apply: bool = True) -> float:
+        """One optimiser step (or, with apply=False, only the gradients); returns the batch loss."""
+        q = np.ascontiguousarray(queries, NRC_QUERY_DTYPE)
+        t = np.ascontiguousarray(targets, np.float32).reshape(-1, 3)
+        loss = C.c_float(0.0)
+        self.ctx.check(self.lib.pico_gpu_nrc_train(self.handle, q.ctypes.data, t.ctypes.data, len(q), int(apply),
+                                                   C.byref(loss)), "nrc_train")
+        return float(loss.value)
+
+    def train_device(self, d_queries: int, d_targets: int, n: int, apply: bool = True, stream: int = 0):
+        self.ctx.check(self.lib.pico_gpu_nrc_train_device(self.handle, d_queries, d_targets, n, int(apply),
+                                                          stream or None), "nrc_train_device")
+
+    def gradients(self):
+        """Gradients of the last train call: (network (6, 64, 64), grid (16, T, 2))."""
+        mlp = np.empty((self.LAYERS, self.WIDTH, self.WIDTH), np.float32)
+        grid = np.empty((self.LEVELS, self.table_size, 2), np.float32)
+        self.ctx.check(self.lib.pico_gpu_nrc_gradients(self.handle, mlp.ctypes.data, grid.ctypes.data),
+                       "nrc_gradients")
+        return mlp, grid
+
+    def attach(self):
+        """Makes this the cache of the context's ESTIMATOR_RADIANCE_CACHE renders."""
+        self.ctx.check(self.lib.pico_gpu_set_radiance_cache(self.ctx.handle, self.handle), "set_radiance_cache")

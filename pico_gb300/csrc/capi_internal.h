@@ -14,6 +14,7 @@
 #include <vector>
 
 struct RenderBuffers;
+struct pico_gpu_nrc;
 
 namespace pico {
 
@@ -37,6 +38,7 @@ struct pico_gpu_ctx {
     RenderBuffers* render = nullptr;            // wavefront path state and image buffers
     int order = PICO_ORDER_NEAR_FIRST;          // traversal order of every trace in this context
     uint64_t render_stats[5] = {0, 0, 0, 0, 0}; // tallies of the last pico_gpu_render call
+    pico_gpu_nrc* cache = nullptr;              // radiance cache of PICO_ESTIMATOR_RADIANCE_CACHE renders
     pico::DeviceStatus* status2() { return status + 1; }
 };
 

@@ -17,7 +17,7 @@ DIFFUSE, SPECULAR, DIELECTRIC, BTDF, LIGHT, FRESNEL, DELTA = 0, 1, 2, 3, 4, 5, 6
 # Mesh shapes (pico_shape).
 SHAPE_TRIANGLES, SHAPE_SPHERE, SHAPE_CUBE = 0, 1, 2
 # Render estimators (pico_estimator).
-ESTIMATOR_REFERENCE, ESTIMATOR_PHYSICAL = 0, 1
+ESTIMATOR_REFERENCE, ESTIMATOR_PHYSICAL, ESTIMATOR_RADIANCE_CACHE = 0, 1, 2
 
 RAY_DTYPE = np.dtype([("org", "<f4", (4,)), ("dir", "<f4", (4,))])
 HIT_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
@@ -62,6 +62,20 @@ class CCamera(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("up", C.c_float * 3),
                 ("resolution", C.c_uint32 * 2), ("aspect", C.c_float), ("near_plane", C.c_float),
                 ("far_plane", C.c_float), ("fov", C.c_float)]
+
+
+class CNrcConfig(C.Structure):
+    """pico_nrc_config: the radiance cache's encoding, optimiser and per-frame training budget."""
+    _fields_ = [("log2_table_size", C.c_uint32), ("base_resolution", C.c_float), ("max_resolution", C.c_float),
+                ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("learning_rate", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float), ("train_paths", C.c_uint32),
+                ("train_batch", C.c_uint32), ("max_train_steps", C.c_uint32), ("warmup_frames", C.c_uint32),
+                ("seed", C.c_uint64)]
+
+
+# pico_nrc_query: 16 x 4 bytes.
+NRC_QUERY_DTYPE = np.dtype([("position", "<f4", (3,)), ("direction", "<f4", (3,)), ("normal", "<f4", (3,)),
+                            ("roughness", "<f4"), ("albedo", "<f4", (3,)), ("payload", "<u4"), ("pad", "<u4", (2,))])
 
 
 class CRenderConfig(C.Structure):
