@@ -340,6 +340,9 @@ int pico_gpu_nrc_set_params(pico_gpu_nrc* cache, const float* mlp, const float* 
 int pico_gpu_nrc_set_bounds(pico_gpu_nrc* cache, const float* aabb_min, const float* aabb_max);
 /* [0] optimiser steps, [1] grid entries, [2] network parameters (incl. padding), [3] frames rendered. */
 int pico_gpu_nrc_info(const pico_gpu_nrc* cache, uint64_t* out4);
+/* Render work with this cache since its creation: [0] training paths traced,
+ * [1] training records, [2] optimiser steps, [3] cache queries of camera paths. */
+int pico_gpu_nrc_stats(const pico_gpu_nrc* cache, uint64_t* out4);
 /* The 64 network inputs of n queries (n * 64 floats, before their bf16 rounding). */
 int pico_gpu_nrc_encode(pico_gpu_nrc* cache, const pico_nrc_query* queries, uint64_t n, float* out);
 /* Network outputs (n * 3 floats) of n <= 2^26 queries. */

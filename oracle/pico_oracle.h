@@ -164,6 +164,12 @@ int po_phys_bsdf_sample(int bsdf, const po_material* m, const double* V, const d
 void po_phys_render_mean(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
                          const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, int strategy,
                          double* mean_rgb, double* var_rgb, int nthreads);
+/* The radiance-cache form of the physical estimator with a cache answering the
+ * constant cache_rgb: paths end after one bounce (two behind a first vertex of
+ * roughness < 0.1) with throughput * cache_rgb. */
+void po_phys_render_mean_cached(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
+                                const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels,
+                                const double* cache_rgb, double* mean_rgb, double* var_rgb, int nthreads);
 /* Mean/variance recurrence alone, applied to a given sample sequence per pixel. */
 void po_accumulate(const float* samples /* n * 3 */, uint32_t n, uint32_t max_samples,
                    float max_variance, float* pixel, uint32_t* count, float* variance);

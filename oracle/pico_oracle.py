@@ -130,6 +130,8 @@ class Oracle(_SceneLib):
             "po_phys_bsdf_sample": (_i32, [_i32, C.POINTER(CMaterial), _dp, _dp, _dp, _dp, _dp, _dp]),
             "po_phys_render_mean": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _up, C.POINTER(_u64), _u32, _i32,
                                            _dp, _dp, _i32]),
+            "po_phys_render_mean_cached": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _up, C.POINTER(_u64), _u32,
+                                                  _dp, _dp, _dp, _i32]),
             "po_denoiser_inputs": (None, [_vp, C.POINTER(CCamera), _u32, _u32, _fp, _fp, _fp]),
             "po_view_matrix": (None, [C.POINTER(CCamera), _fp]),
             "po_atrous_denoise": (None, [_fp, _fp, _fp, _fp, _u32, _u32, _fp]),
@@ -370,6 +372,19 @@ class OracleScene:
         self.lib.po_phys_render_mean(self.handle, C.byref(c), max_depth, spp, idx.ctypes.data_as(_up),
                                      sd.ctypes.data_as(C.POINTER(_u64)), len(idx), strategy,
                                      mean.ctypes.data_as(_dp), var.ctypes.data_as(_dp), nthreads)
+        return mean, var
+
+    def phys_render_mean_cached(self, cam, max_depth, spp, pixel_index, seeds, cache_rgb, nthreads=0):
+        """The radiance-cache form of the physical estimator with a cache answering the constant
+        cache_rgb (FP64 mean and sample variance of `spp` paths per listed pixel)."""
+        idx = np.ascontiguousarray(pixel_index, np.uint32)
+        sd = np.ascontiguousarray(seeds, np.uint64)
+        k = np.ascontiguousarray(cache_rgb, np.float64)
+        mean, var = np.empty((len(idx), 3)), np.empty((len(idx), 3))
+        c = cam.to_c()
+        self.lib.po_phys_render_mean_cached(self.handle, C.byref(c), max_depth, spp, idx.ctypes.data_as(_up),
+                                            sd.ctypes.data_as(C.POINTER(_u64)), len(idx), k.ctypes.data_as(_dp),
+                                            mean.ctypes.data_as(_dp), var.ctypes.data_as(_dp), nthreads)
         return mean, var
 
     def denoiser_inputs(self, cam):

@@ -285,9 +285,15 @@ static double light_pdf(const phys_scene* ps, const double* g, double t, d3 d)
     return g[3] * t * t / (cl * ps->nl);
 }
 
+/* One path of the physical estimator.  With `cache` (the radiance-cache form,
+ * pico_gpu.h PICO_ESTIMATOR_RADIANCE_CACHE, here with a cache that answers the
+ * constant radiance cache[0..2]): a path ends at its non-emitting vertex after
+ * one bounce, or after two when the first vertex has roughness < 0.1 (a mirror
+ * counts as roughness 0), adding throughput * cache there. */
 static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uint32_t py, uint32_t max_depth,
-                    int strategy, prng* rng)
+                    int strategy, const double* cache, prng* rng)
 {
+    double prev_rough = 0.0;
     const po_scene* s = ps->s;
     po_ray r;
     const float jx = (float)(2.0 * rnd(rng)), jy = (float)(2.0 * rnd(rng));
@@ -318,7 +324,12 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
             rad = d3_add(rad, d3_scale(d3_mul(thr, d3_of(m->emissive)), w));
             break;
         }
+        if (cache && (depth >= 2 || (depth == 1 && prev_rough >= 0.1))) {
+            rad = d3_add(rad, d3_mul(thr, d3v(cache[0], cache[1], cache[2])));
+            break;
+        }
         if (depth >= max_depth) break;
+        prev_rough = in->bsdf == PO_DELTA ? 0.0 : m->roughness;   /* a mirror is glossy */
         d3 n = d3_norm(d3_of(f.normal));
         const d3 v = d3_scale(d, -1.0);
         if (d3_dot(n, v) < 0.0) n = d3_scale(n, -1.0);
@@ -412,6 +423,7 @@ typedef struct {
     const po_camera* cam;
     uint32_t max_depth, spp, pixel;
     int strategy;
+    const double* cache;
     uint64_t seed;
     double *mean, *var;
 } phys_job;
@@ -423,7 +435,7 @@ static void phys_job_run(void* p)
     prng rng = {j->seed};
     double sum[3] = {0, 0, 0}, sq[3] = {0, 0, 0};
     for (uint32_t i = 0; i < j->spp; ++i) {
-        const d3 x = phys_path(j->ps, j->cam, j->pixel % W, j->pixel / W, j->max_depth, j->strategy, &rng);
+        const d3 x = phys_path(j->ps, j->cam, j->pixel % W, j->pixel / W, j->max_depth, j->strategy, j->cache, &rng);
         const double c[3] = {x.x, x.y, x.z};
         for (int a = 0; a < 3; ++a) { sum[a] += c[a]; sq[a] += c[a] * c[a]; }
     }
@@ -434,9 +446,9 @@ static void phys_job_run(void* p)
     }
 }
 
-void po_phys_render_mean(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
-                         const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, int strategy,
-                         double* mean, double* var, int nthreads)
+static void render_mean(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
+                        const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, int strategy,
+                        const double* cache, double* mean, double* var, int nthreads)
 {
     phys_scene ps;
     phys_prepare(&ps, s);
@@ -444,9 +456,24 @@ void po_phys_render_mean(const po_scene* s, const po_camera* cam, uint32_t max_d
     for (uint32_t i = 0; i < npixels; ++i) {
         phys_job* j = &jobs[i];
         j->ps = &ps; j->cam = cam; j->max_depth = max_depth; j->spp = spp; j->pixel = pixel_index[i];
-        j->strategy = strategy; j->seed = seeds[i]; j->mean = mean + 3 * (size_t)i; j->var = var + 3 * (size_t)i;
+        j->strategy = strategy; j->cache = cache; j->seed = seeds[i]; j->mean = mean + 3 * (size_t)i;
+        j->var = var + 3 * (size_t)i;
     }
     po_parallel_for(npixels, jobs, sizeof(phys_job), phys_job_run, nthreads);
     free(jobs);
     phys_release(&ps);
+}
+
+void po_phys_render_mean(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
+                         const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels, int strategy,
+                         double* mean, double* var, int nthreads)
+{
+    render_mean(s, cam, max_depth, spp, pixel_index, seeds, npixels, strategy, NULL, mean, var, nthreads);
+}
+
+void po_phys_render_mean_cached(const po_scene* s, const po_camera* cam, uint32_t max_depth, uint32_t spp,
+                                const uint32_t* pixel_index, const uint64_t* seeds, uint32_t npixels,
+                                const double* cache_rgb, double* mean, double* var, int nthreads)
+{
+    render_mean(s, cam, max_depth, spp, pixel_index, seeds, npixels, 0, cache_rgb, mean, var, nthreads);
 }

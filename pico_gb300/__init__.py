@@ -69,6 +69,7 @@ SIGNATURES = {
     "pico_gpu_nrc_set_params": (C.c_int, [_vp, _vp, _vp]),
     "pico_gpu_nrc_set_bounds": (C.c_int, [_vp, _fp, _fp]),
     "pico_gpu_nrc_info": (C.c_int, [_vp, C.POINTER(_u64)]),
+    "pico_gpu_nrc_stats": (C.c_int, [_vp, C.POINTER(_u64)]),
     "pico_gpu_nrc_encode": (C.c_int, [_vp, _vp, _u64, _vp]),
     "pico_gpu_nrc_infer": (C.c_int, [_vp, _vp, _u64, _vp]),
     "pico_gpu_nrc_infer_device": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
@@ -376,6 +377,12 @@ class RadianceCache:
         out = (C.c_uint64 * 4)()
         self.ctx.check(self.lib.pico_gpu_nrc_info(self.handle, out), "nrc_info")
         return dict(zip(["steps", "grid_entries", "mlp_params", "frames"], [int(x) for x in out]))
+
+    def stats(self) -> dict:
+        """Cumulative render work with this cache."""
+        out = (C.c_uint64 * 4)()
+        self.ctx.check(self.lib.pico_gpu_nrc_stats(self.handle, out), "nrc_stats")
+        return dict(zip(["train_paths", "train_records", "train_steps", "queries"], [int(x) for x in out]))
 
     def encode(self, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, NRC_QUERY_DTYPE)

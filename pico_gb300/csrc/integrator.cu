@@ -282,8 +282,29 @@ __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, Pat
 // bounces, whose emission is not weighted); a shadow record carries its finished
 // contribution in scontrib.xyz, the distance from which a hit no longer occludes
 // in scontrib.w, and senergy.w = 2.
+// The radiance-cache query of a shading point (pico_nrc_query layout): position,
+// direction towards the viewer, shading normal, roughness, albedo (diffuse +
+// specular colour, at most 1), the path index as payload.
+__device__ __forceinline__ void nrc_query(const Fragment& f, float3 nrm, float3 v, const GpuMaterial& m,
+                                          uint32_t kind, uint32_t path, float4 (&q)[4])
+{
+    float a[3];
+    if (kind == PICO_BSDF_DELTA) {
+        for (int c = 0; c < 3; ++c) a[c] = m.specular[c];
+    } else {
+        const phys::Lobes lb = phys::lobes_of(kind, m);
+        a[0] = lb.diffuse.x + lb.f0.x; a[1] = lb.diffuse.y + lb.f0.y; a[2] = lb.diffuse.z + lb.f0.z;
+    }
+    for (int c = 0; c < 3; ++c) a[c] = fminf(fmaxf(a[c], 0.0f), 1.0f);
+    q[0] = make_float4(f.px, f.py, f.pz, v.x);
+    q[1] = make_float4(v.y, v.z, nrm.x, nrm.y);
+    q[2] = make_float4(nrm.z, kind == PICO_BSDF_DELTA ? 0.0f : m.roughness, a[0], a[1]);
+    q[3] = make_float4(a[2], __uint_as_float(path), 0.0f, 0.0f);
+}
+
 __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneView sc, PathBatch b, int cur,
-                                                                       uint32_t depth, uint32_t max_depth)
+                                                                       uint32_t depth, uint32_t max_depth,
+                                                                       NrcShadeArgs nrc)
 {
     using namespace phys;
     const uint32_t n = b.counters[cur];
@@ -295,7 +316,8 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
     const uint32_t rounds = (n + stride - 1) / stride;
     for (uint32_t r = 0; r < rounds; ++r) {
         const uint32_t k = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        bool cont = false, shadow = false;
+        bool cont = false, shadow = false, emit = false;
+        float4 eq[4], et = make_float4(0.0f, 0.0f, 0.0f, 0.0f), ep = et;   // radiance-cache entry
         uint32_t i = 0;
         if (k < n) {
             i = b.queue[cur][k];
@@ -303,10 +325,23 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
             const uint32_t rank = __float_as_uint(hit.w);
             float4 thr = b.thr[i], pay = b.pay[i];
             const float4 dir = b.dir[i];
+            const bool terminal = nrc.mode == kNrcTerminate && rank != kNoHit &&
+                                  (depth >= 2 || (depth == 1 && nrc.prev_rough[i] >= 0.1f));
             if (rank == kNoHit) {
                 const float3 sk = sky_radiance(sc, dir.x, dir.y, dir.z);
                 pay.x += thr.x * sk.x; pay.y += thr.y * sk.y; pay.z += thr.z * sk.z;
                 b.pay[i] = pay;
+            } else if (terminal && sc.inst_shade[sc.insts[rank].inst_id].bsdf != PICO_BSDF_LIGHT) {
+                // the path ends here in the radiance cache: query what this point reflects towards v
+                const uint32_t inst = sc.insts[rank].inst_id;
+                const GpuInstanceShade is = sc.inst_shade[inst];
+                const GpuMaterial m = sc.materials[is.material];
+                const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z, b.org[i], dir);
+                float3 nrm = normalize3(make_float3(f.n.x, f.n.y, f.n.z));
+                const float3 v = make_float3(-dir.x, -dir.y, -dir.z);
+                if (dot3(nrm, v) < 0.0f) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+                nrc_query(f, nrm, v, m, is.bsdf, i, eq);
+                emit = true;
             } else {
                 const uint32_t inst = sc.insts[rank].inst_id;
                 const GpuInstanceShade is = sc.inst_shade[inst];
@@ -333,6 +368,14 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                     float3 nrm = normalize3(make_float3(f.n.x, f.n.y, f.n.z));
                     const float3 v = make_float3(-dir.x, -dir.y, -dir.z);
                     if (dot3(nrm, v) < 0.0f) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+                    if (nrc.mode == kNrcRecord) {
+                        nrc_query(f, nrm, v, m, is.bsdf, i, eq);
+                        et = thr;
+                        ep = pay;
+                        emit = true;
+                    } else if (nrc.mode == kNrcTerminate) {
+                        nrc.prev_rough[i] = is.bsdf == PICO_BSDF_DELTA ? 0.0f : m.roughness;   // a mirror is glossy
+                    }
                     const float eps = ray_offset(f.px, f.py, f.pz);
                     const float4 org = make_float4(f.px + eps * nrm.x, f.py + eps * nrm.y, f.pz + eps * nrm.z, f.pw);
                     float3 L, weight;
@@ -449,6 +492,69 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
         if (cont) b.queue[nxt][at] = i;
         const uint32_t sat = warp_append(shadow, &b.counters[2]);
         if (shadow) b.shadow_queue[sat] = i;
+        if (nrc.mode != kNrcOff) {
+            const uint32_t ea = warp_append(emit, nrc.count);
+            if (emit && ea < nrc.capacity) {
+                float4* q = nrc.queries + 4 * (size_t)ea;
+                q[0] = eq[0]; q[1] = eq[1]; q[2] = eq[2]; q[3] = eq[3];
+                if (nrc.mode == kNrcRecord) {
+                    nrc.rec_tp[2 * (size_t)ea] = et;
+                    nrc.rec_tp[2 * (size_t)ea + 1] = ep;
+                }
+            }
+        }
+    }
+}
+
+// Pixel-pseudo-random camera paths that train the radiance cache: path j of pass
+// `frame` starts at a uniformly drawn pixel with a jitter over the whole pixel.
+__global__ void __launch_bounds__(kRenderThreads) train_raygen_kernel(PathBatch b, CameraView cam,
+                                                                     unsigned long long seed, uint32_t frame,
+                                                                     uint32_t W, uint32_t npx)
+{
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (b.n + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool live = i < b.n;
+        if (live) {
+            Pcg32 rng = path_rng(seed, i, frame);
+            const uint32_t pixel = rng.next() % npx;
+            const float x0 = 2.0f * rng.uniform(), x1 = 2.0f * rng.uniform();
+            float4 o, d;
+            camera_ray(cam, x0, x1, pixel % W, pixel / W, o, d);
+            b.org[i] = o;
+            b.dir[i] = d;
+            b.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            b.pay[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            b.rng[i] = rng.state;
+            b.depth[i] = 0;
+        }
+        const uint32_t at = warp_append(live, &b.counters[0]);
+        if (live) b.queue[0][at] = i;
+    }
+}
+
+// Target of each training record: (final payload - payload on arrival) / throughput
+// on arrival, per channel (0 where the throughput is 0); NaN for a path whose
+// payload is not finite, which training skips.
+__global__ void __launch_bounds__(kRenderThreads) nrc_targets_kernel(const float4* __restrict__ queries,
+                                                                    const float4* __restrict__ rec_tp,
+                                                                    const float4* __restrict__ pay,
+                                                                    const uint32_t* count, uint32_t capacity,
+                                                                    float4* targets)
+{
+    const uint32_t n = min(*count, capacity);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t path = __float_as_uint(queries[4 * (size_t)j + 3].y);
+        const float4 T = rec_tp[2 * (size_t)j], P = rec_tp[2 * (size_t)j + 1], F = pay[path];
+        float4 t;
+        t.x = T.x > 0.0f ? (F.x - P.x) / T.x : 0.0f;
+        t.y = T.y > 0.0f ? (F.y - P.y) / T.y : 0.0f;
+        t.z = T.z > 0.0f ? (F.z - P.z) / T.z : 0.0f;
+        t.w = 0.0f;
+        if (!(isfinite(F.x) && isfinite(F.y) && isfinite(F.z))) t.x = __int_as_float(0x7fc00000);
+        targets[j] = t;
     }
 }
 
@@ -570,14 +676,11 @@ static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, 
                                                                   &status->trace_error, shadow, tally);
 }
 
-cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
-                                uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                int estimator, DeviceStatus* status, int order, cudaStream_t st)
+// The extend / shade / shadow loop of one batch whose camera rays are queued.
+static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t max_depth, bool physical,
+                                  const NrcShadeArgs& nrc, DeviceStatus* status, int order, cudaStream_t st)
 {
-    const bool physical = estimator == PICO_ESTIMATOR_PHYSICAL;
-    cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
+    cudaError_t e = cudaSuccess;
     const bool trace_last =
         sc.sky_kind != PICO_SKY_CONSTANT || sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
     int cur = 0;
@@ -593,7 +696,7 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
         if (e != cudaSuccess) return e;
         if (physical)
             shade_physical_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth,
-                                                                                         max_depth);
+                                                                                         max_depth, nrc);
         else
             shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
                                                                                     trace_last);
@@ -606,6 +709,47 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
             });
         }
         cur ^= 1;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
+                                  uint32_t frame, uint32_t n, uint32_t W, uint32_t H, uint32_t max_depth,
+                                  const NrcShadeArgs& nrc, float4* targets, DeviceStatus* status, int order,
+                                  cudaStream_t st)
+{
+    PathBatch t = b;
+    t.n = n;
+    cudaError_t e = cudaMemsetAsync(t.counters, 0, 4 * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(nrc.count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    train_raygen_kernel<<<grid_for(n, kRenderThreads), kRenderThreads, 0, st>>>(t, cam, seed, frame, W, W * H);
+    e = run_depth_loop(sc, t, max_depth, true, nrc, status, order, st);
+    if (e != cudaSuccess) return e;
+    nrc_targets_kernel<<<grid_for(nrc.capacity, kRenderThreads), kRenderThreads, 0, st>>>(
+        nrc.queries, nrc.rec_tp, t.pay, nrc.count, nrc.capacity, targets);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
+                                uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
+                                int estimator, DeviceStatus* status, int order, cudaStream_t st,
+                                const NrcShadeArgs* nrc)
+{
+    const bool physical = estimator != PICO_ESTIMATOR_REFERENCE;
+    NrcShadeArgs off{};
+    off.mode = kNrcOff;
+    const NrcShadeArgs& na = nrc ? *nrc : off;
+    cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
+    if (e == cudaSuccess && na.mode != kNrcOff) e = cudaMemsetAsync(na.count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
+    e = run_depth_loop(sc, b, max_depth, physical, na, status, order, st);
+    if (e != cudaSuccess) return e;
+    if (na.mode == kNrcTerminate) {
+        e = nrc::launch_infer(na.geo, na.table, na.weights, na.queries, na.capacity, nullptr, b.thr, b.pay, na.err, st,
+                              na.count);
+        if (e != cudaSuccess) return e;
     }
     finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
     accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,

@@ -3,7 +3,9 @@
 
 #include "kernels.h"
 #include "layout.h"
+#include "nrc.h"
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -36,9 +38,43 @@ struct PathBatch {
     float* pixels; float* variance; uint32_t* count; uint32_t* taken; uint32_t* done;
 };
 
+// What the physical shade step does for the radiance cache.
+//   kNrcRecord     every shaded vertex of a training path appends a record: the
+//                  cache query (4 float4), then the path throughput and payload
+//                  on arrival (2 float4 in rec_tp), from which the radiance the
+//                  rest of the path reflects there is (final payload - payload)
+//                  / throughput;
+//   kNrcTerminate  a camera path stops at its vertex after one bounce (after two
+//                  when the first vertex has roughness < 0.1) and appends that
+//                  vertex's query; the cache's answer times the throughput is
+//                  added to the payload after the depth loop.
+enum NrcMode { kNrcOff = 0, kNrcRecord = 1, kNrcTerminate = 2 };
+struct NrcShadeArgs {
+    int mode;
+    uint32_t capacity;        // entries of queries / rec_tp
+    float4* queries;          // 4 float4 per entry (pico_nrc_query)
+    float4* rec_tp;           // kNrcRecord: 2 float4 per entry
+    uint32_t* count;          // entries appended
+    float* prev_rough;        // kNrcTerminate: per path, roughness of its previous vertex
+    // the cache the terminating paths query
+    nrc::GridGeometry geo;
+    const __half2* table;
+    const uint8_t* weights;
+    int* err;
+};
+
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
-                                int estimator, DeviceStatus* status, int order, cudaStream_t st);
+                                int estimator, DeviceStatus* status, int order, cudaStream_t st,
+                                const NrcShadeArgs* nrc = nullptr);
+// The radiance cache's training paths of one sample pass: n full-depth physical
+// paths from pseudo-random pixels of the W x H image (path slots 0 .. n-1 of b),
+// recording every shaded vertex (kNrcRecord), then the records' targets
+// (4 floats each) in `targets`.
+cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
+                                  uint32_t frame, uint32_t n, uint32_t W, uint32_t H, uint32_t max_depth,
+                                  const NrcShadeArgs& nrc, float4* targets, DeviceStatus* status, int order,
+                                  cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
 // Floats of a-trous scratch per 64 x 64 tile: four partial statistics records

@@ -89,6 +89,7 @@ struct InferArgs {
     const float4* thr;
     float4* pay;
     int* err;
+    const uint32_t* n_dev;
 };
 
 __global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
@@ -122,10 +123,11 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
     uint32_t phase = 0;
     const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
     const uint32_t x_addr = smem_addr(X), w_addr = smem_addr(W);
-    const uint32_t ntiles = (a.n + kRows - 1) / kRows;
+    const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
+    const uint32_t ntiles = (n + kRows - 1) / kRows;
     for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint32_t row = t * kRows + tid;
-        const bool valid = row < a.n;
+        const bool valid = row < n;
         uint32_t payload = 0;
         {
             float in[kWidth];
@@ -471,7 +473,8 @@ cudaError_t launch_encode(const GridGeometry& g, const __half2* table, const flo
 }
 
 cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint8_t* weights, const float4* queries,
-                         uint32_t n, float* out_rgb, const float4* thr, float4* pay, int* err, cudaStream_t st)
+                         uint32_t n, float* out_rgb, const float4* thr, float4* pay, int* err, cudaStream_t st,
+                         const uint32_t* n_dev)
 {
     if (n == 0) return cudaSuccess;
     static bool configured = false;
@@ -486,7 +489,7 @@ cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint
     }
     const uint32_t tiles = (n + kRows - 1) / kRows;
     const uint32_t cap = (uint32_t)(sm_count() * per_sm);
-    InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err};
+    InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev};
     infer_kernel<<<tiles < cap ? tiles : cap, kThreads, kInferSmem, st>>>(a);
     return cudaGetLastError();
 }

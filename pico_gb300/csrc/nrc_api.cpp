@@ -268,6 +268,13 @@ int pico_gpu_nrc_info(const pico_gpu_nrc* c, uint64_t* out4)
     return PICO_OK;
 }
 
+int pico_gpu_nrc_stats(const pico_gpu_nrc* c, uint64_t* out4)
+{
+    if (!c || !out4) return PICO_ERR_INVALID_ARG;
+    for (int k = 0; k < 4; ++k) out4[k] = c->render_stats[k];
+    return PICO_OK;
+}
+
 int pico_gpu_nrc_encode(pico_gpu_nrc* c, const pico_nrc_query* q, uint64_t n, float* out)
 {
     if (!c || (n && (!q || !out))) return PICO_ERR_INVALID_ARG;

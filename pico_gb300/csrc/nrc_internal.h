@@ -15,6 +15,7 @@ struct pico_gpu_nrc {
     uint32_t max_parts = 0;            // weight-gradient partials (one per training CTA)
     uint64_t step = 0;                 // optimiser steps taken
     uint64_t frames = 0;               // frames rendered with the cache
+    uint64_t train_passes = 0;         // training-path passes traced (selects their random streams)
     // network: fp32 master weights (layer, out, in), Adam moments, last gradient,
     // per-CTA gradient partials, swizzled bf16 image the kernels load
     float *master = nullptr, *adam_m = nullptr, *adam_v = nullptr, *grad = nullptr, *partial = nullptr;
@@ -27,7 +28,8 @@ struct pico_gpu_nrc {
     std::vector<void*> allocations;
     // render-time buffers: training path state and records
     std::vector<void*> render_allocations;
-    uint64_t render_stats[6] = {0, 0, 0, 0, 0, 0};
+    // cumulative render work: training paths, training records, optimiser steps, cache queries
+    uint64_t render_stats[4] = {0, 0, 0, 0};
 };
 
 namespace pico {

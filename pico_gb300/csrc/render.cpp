@@ -11,6 +11,7 @@
 // then runs on the result and replaces it (Scene.cpp:212-234).
 #include "capi_internal.h"
 #include "kernels_render.h"
+#include "nrc_internal.h"
 
 #include <cmath>
 #include <cstring>
@@ -75,12 +76,16 @@ struct RenderBuffers {
         q0, q1, sq, counters, samples;
     DeviceBuffer pixels, variance, count, taken, done, pix_list;
     DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
+    // radiance cache: terminal queries / training records, record throughput and
+    // payload, targets, previous roughness per path, entry counters
+    DeviceBuffer nrc_q, nrc_tp, nrc_tgt, nrc_prev, nrc_count;
     ~RenderBuffers()
     {
         for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
                                 &sorg, &sdir, &scontrib,
                                 &senergy, &q0, &q1, &sq, &counters, &samples, &pixels, &variance, &count, &taken,
-                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out, &tonemap})
+                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out, &tonemap, &nrc_q, &nrc_tp,
+                                &nrc_tgt, &nrc_prev, &nrc_count})
             b->release();
     }
 };
@@ -129,6 +134,119 @@ int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const fl
 
 bool valid_camera(const pico_camera* c) { return c && c->resolution[0] > 0 && c->resolution[1] > 0; }
 
+// The path state of a batch of n paths over npix listed pixels, in the context's buffers.
+PathBatch make_batch(RenderBuffers& r, uint32_t n, uint32_t npix, uint32_t W, const uint32_t* pix_list)
+{
+    PathBatch b{};
+    b.n = n; b.npix = npix; b.width = W;
+    b.pix_list = pix_list;
+    b.org = as<float4>(r.org); b.dir = as<float4>(r.dir); b.thr = as<float4>(r.thr);
+    b.pay = as<float4>(r.pay); b.hit = as<float4>(r.hit); b.hit_tri = as<uint32_t>(r.hit_tri);
+    b.rng = as<unsigned long long>(r.rng); b.depth = as<uint32_t>(r.depth);
+    b.ior_n = as<uint32_t>(r.ior_n); b.ior_lo = as<float4>(r.ior_lo); b.ior_hi = as<float4>(r.ior_hi);
+    b.sorg = as<float4>(r.sorg); b.sdir = as<float4>(r.sdir); b.scontrib = as<float4>(r.scontrib);
+    b.senergy = as<float4>(r.senergy); b.queue[0] = as<uint32_t>(r.q0); b.queue[1] = as<uint32_t>(r.q1);
+    b.shadow_queue = as<uint32_t>(r.sq); b.counters = as<uint32_t>(r.counters);
+    b.samples = as<float4>(r.samples);
+    b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
+    b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
+    return b;
+}
+
+// PICO_ESTIMATOR_RADIANCE_CACHE: warmup_frames training-only passes, then per
+// sample pass the cache trains on train_paths full-depth physical paths (at most
+// max_train_steps optimiser steps of at most train_batch records, spread over all
+// records of the pass) and every active pixel takes one sample whose path ends
+// in the cache.  The pixel list is on the device already.
+int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_nrc* c, const pico_render_config* cfg,
+                      const CameraView& cam, RenderBuffers& r, size_t nactive, const volatile int32_t* should_quit,
+                      bool& cancelled)
+{
+    cudaStream_t st = ctx->stream;
+    const uint32_t W = cfg->width, H = cfg->height;
+    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, kMaxPaths);
+    const uint32_t ntrain = std::min<uint32_t>(c->cfg.train_paths, kMaxPaths);
+    const uint32_t max_depth = cfg->max_ray_depth;
+    const size_t rec_cap = (size_t)ntrain * std::max(max_depth, 1u);
+    const size_t q_cap = std::max<size_t>(chunk_pix, rec_cap);
+    const size_t slots = std::max<size_t>(chunk_pix, ntrain);
+    cudaError_t e = reserve_paths(r, slots);
+    if (e == cudaSuccess) e = r.nrc_q.reserve(q_cap * sizeof(pico_nrc_query));
+    if (e == cudaSuccess) e = r.nrc_tp.reserve(rec_cap * 2 * sizeof(float4));
+    if (e == cudaSuccess) e = r.nrc_tgt.reserve(rec_cap * sizeof(float4));
+    if (e == cudaSuccess) e = r.nrc_prev.reserve(slots * sizeof(float));
+    if (e == cudaSuccess) e = r.nrc_count.reserve(4 * sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "radiance cache render buffers");
+    if (!(c->hi[0] > c->lo[0] || c->hi[1] > c->lo[1] || c->hi[2] > c->lo[2]))
+        nrc::set_geometry(c, scene->view.tlas_fast_lo, scene->view.tlas_fast_hi);
+
+    NrcShadeArgs na{};
+    na.queries = as<float4>(r.nrc_q);
+    na.rec_tp = as<float4>(r.nrc_tp);
+    na.count = as<uint32_t>(r.nrc_count);
+    na.prev_rough = as<float>(r.nrc_prev);
+    na.geo = c->geo;
+    na.table = c->table;
+    na.weights = c->image;
+    na.err = c->err;
+    const unsigned long long train_seed = c->cfg.seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    const int order = scene_order(ctx, scene);
+    const bool training = ntrain > 0 && c->cfg.max_train_steps > 0;
+    // training paths of one pass, then at most max_train_steps optimiser steps over their records
+    auto train_pass = [&]() -> int {
+        na.mode = kNrcRecord;
+        na.capacity = (uint32_t)rec_cap;
+        PathBatch tb = make_batch(r, ntrain, 0, W, nullptr);
+        cudaError_t te = launch_training_paths(scene->view, tb, cam, train_seed, (uint32_t)c->train_passes, ntrain,
+                                               W, H, max_depth, na, as<float4>(r.nrc_tgt), ctx->status, order, st);
+        uint32_t nrec = 0;
+        if (te == cudaSuccess) te = cudaMemcpyAsync(&nrec, na.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+        if (te == cudaSuccess) te = cudaStreamSynchronize(st);
+        if (te != cudaSuccess) return cuda_error(ctx, te, "radiance cache training paths");
+        nrec = std::min<uint32_t>(nrec, (uint32_t)rec_cap);
+        ++c->train_passes;
+        c->render_stats[0] += ntrain;
+        c->render_stats[1] += nrec;
+        if (nrec == 0) return PICO_OK;
+        const uint32_t batch = c->cfg.train_batch;
+        const uint32_t steps =
+            std::max<uint32_t>(1u, std::min<uint32_t>(c->cfg.max_train_steps, (nrec + batch - 1) / batch));
+        const uint32_t per = steps * ((nrec + steps * batch - 1) / (steps * batch));   // record stride
+        for (uint32_t s = 0; s < steps && s < nrec; ++s) {
+            const nrc::TrainBatch b{na.queries, as<float4>(r.nrc_tgt), (nrec - s + per - 1) / per, s, per};
+            const int status = nrc::train_step(c, b, true, st);
+            if (status != PICO_OK) return status;
+            c->render_stats[2] += 1;
+        }
+        return PICO_OK;
+    };
+    const uint32_t passes = c->cfg.warmup_frames + cfg->max_samples;
+    for (uint32_t pass = 0; pass < passes; ++pass) {
+        if (should_quit && *should_quit) { cancelled = true; break; }
+        if (training) {
+            const int status = train_pass();
+            if (status != PICO_OK) return status;
+        }
+        if (pass < c->cfg.warmup_frames) continue;
+        // one sample per active pixel, ending in the cache
+        na.mode = kNrcTerminate;
+        na.capacity = chunk_pix;
+        for (size_t p0 = 0; p0 < nactive; p0 += chunk_pix) {
+            const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, nactive - p0);
+            PathBatch b = make_batch(r, npix, npix, W, as<uint32_t>(r.pix_list) + p0);
+            e = launch_render_batch(scene->view, b, cam, cfg->seed, 1, max_depth, cfg->max_samples,
+                                    cfg->max_variance, PICO_ESTIMATOR_RADIANCE_CACHE, ctx->status, order, st, &na);
+            uint32_t nq = 0;
+            if (e == cudaSuccess) e = cudaMemcpyAsync(&nq, na.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "radiance cache render batch");
+            c->render_stats[3] += nq;
+        }
+        ++c->frames;
+    }
+    return nrc::take_status(c, st);
+}
+
 }  // namespace
 
 extern "C" {
@@ -141,10 +259,13 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (cfg->width != camera->resolution[0] || cfg->height != camera->resolution[1])
         return set_error(ctx, PICO_ERR_INVALID_ARG, "render size differs from the camera resolution");
-    if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && cfg->estimator != PICO_ESTIMATOR_PHYSICAL)
+    if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && cfg->estimator != PICO_ESTIMATOR_PHYSICAL &&
+        cfg->estimator != PICO_ESTIMATOR_RADIANCE_CACHE)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "unknown estimator");
-    if (cfg->estimator == PICO_ESTIMATOR_PHYSICAL && scene->has_btdf)
+    if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && scene->has_btdf)
         return set_error(ctx, PICO_ERR_UNSUPPORTED, "the physical estimator has no Transparent or Fresnel lobes");
+    if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE && !ctx->cache)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "no radiance cache attached (pico_gpu_set_radiance_cache)");
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
@@ -179,7 +300,13 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
 
     const CameraView cam = make_camera_view(*camera);
     bool cancelled = false;
-    if (!active.empty() && cfg->max_samples > 0) {
+    if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE) {
+        if (!active.empty() && cfg->max_samples > 0) {
+            const int status = render_with_cache(ctx, scene, ctx->cache, cfg, cam, r, active.size(), should_quit,
+                                                 cancelled);
+            if (status != PICO_OK) return status;
+        }
+    } else if (!active.empty() && cfg->max_samples > 0) {
         const uint32_t chunk_pix = (uint32_t)std::min<size_t>(active.size(), kMaxPaths);
         const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, kMaxPaths / chunk_pix));
         e = reserve_paths(r, (size_t)chunk_pix * spb_max);
@@ -189,19 +316,7 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
             for (uint32_t s0 = 0; s0 < cfg->max_samples; s0 += spb_max) {
                 if (should_quit && *should_quit) { cancelled = true; break; }
                 const uint32_t spb = std::min(spb_max, cfg->max_samples - s0);
-                PathBatch b{};
-                b.n = npix * spb; b.npix = npix; b.width = W;
-                b.pix_list = as<uint32_t>(r.pix_list) + p0;
-                b.org = as<float4>(r.org); b.dir = as<float4>(r.dir); b.thr = as<float4>(r.thr);
-                b.pay = as<float4>(r.pay); b.hit = as<float4>(r.hit); b.hit_tri = as<uint32_t>(r.hit_tri);
-                b.rng = as<unsigned long long>(r.rng); b.depth = as<uint32_t>(r.depth);
-                b.ior_n = as<uint32_t>(r.ior_n); b.ior_lo = as<float4>(r.ior_lo); b.ior_hi = as<float4>(r.ior_hi);
-                b.sorg = as<float4>(r.sorg); b.sdir = as<float4>(r.sdir); b.scontrib = as<float4>(r.scontrib);
-                b.senergy = as<float4>(r.senergy); b.queue[0] = as<uint32_t>(r.q0); b.queue[1] = as<uint32_t>(r.q1);
-                b.shadow_queue = as<uint32_t>(r.sq); b.counters = as<uint32_t>(r.counters);
-                b.samples = as<float4>(r.samples);
-                b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
-                b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
+                PathBatch b = make_batch(r, npix * spb, npix, W, as<uint32_t>(r.pix_list) + p0);
                 e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
                                         cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene),
                                         st);
