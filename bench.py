@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--render-spp", type=int, default=64)
     ap.add_argument("--render-depth", type=int, default=8)
     ap.add_argument("--render-cpu-pixels", type=int, default=8192)
+    ap.add_argument("--nrc-passes", type=int, nargs="*", default=[16, 32, 64, 96, 128])
     return ap.parse_args()
 
 
@@ -267,6 +268,124 @@ def convergence(ctx, gs, scene, cam, args, timed_image, estimator=0):
             "timed_render_note": ("denoised" if estimator else "denoised, reference early exit") +
                                  "; relMSE over the finite judged pixels",
             "plain_no_early_exit": series}
+
+
+NRC_FLOPS_PER_QUERY = 2 * (5 * 64 * 64 + 64 * 3)   # five 64x64 layers and the 64 -> 3 output
+
+
+def bench_radiance_cache(ctx, args, torch, local, plain_series):
+    """The radiance-cache form on the lit field at 1920x1080, depth 8: wall time and relMSE
+    (against the FP64 judge of the physical estimator) of renders of N passes from a fresh
+    cache, next to the plain physical tracer's relMSE at 256 spp; plus the inference and
+    training kernels timed alone with CUDA events (tensor roofline of the inference)."""
+    from pico_gb300 import RadianceCache
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from judge import Judge
+    scene = scenes.lit_field()
+    cam = scenes.lit_field_camera(1920, 1080)
+    gs = ctx.upload(scene)
+    try:
+        j = Judge("lit_phys")
+        j.check_scene(scene)
+    except (OSError, KeyError, ValueError):
+        j = None
+    cfg = dict(seed=3)
+    warm = RadianceCache(ctx, **cfg)
+    warm.attach()
+    gs.render(cam, args.render_depth, 2, seed=98, estimator=2)
+    warm.free()
+    series = []
+    with ClockSampler(local) as clocks:
+        for n in args.nrc_passes:
+            c = RadianceCache(ctx, **cfg)
+            c.attach()
+            t0 = time.perf_counter()
+            pix, cnt, _ = gs.render(cam, args.render_depth, n, seed=700 + n, estimator=2)
+            secs = time.perf_counter() - t0
+            st, rs = c.stats(), ctx.render_stats()
+            rays = rs["camera_paths"] + rs["bounce_rays"] + rs["shadow_rays"]
+            series.append({"passes": n, "seconds": secs, "relmse": j.relmse(pix) if j else None,
+                           "Msamples_per_s": rs["samples"] / secs / 1e6, "Mrays_per_s": rays / secs / 1e6,
+                           "train_paths": st["train_paths"], "train_records": st["train_records"],
+                           "train_steps": st["train_steps"], "cache_queries": st["queries"]})
+            c.free()
+    out = {"workload": f"lit field 1920x1080, depth {args.render_depth}, radiance cache (16-level hash grid 2^19, "
+                       f"SH4, 5 x 64 ReLU, bf16 tcgen05), 65536 training paths and up to 4 Adam steps of 65536 "
+                       f"records per pass, paths end after 1 bounce (2 behind roughness < 0.1)",
+           "timing": "wall clock around pico_gpu_render (host buffers in and out), fresh cache per render",
+           "series": series, "clocks": clocks.summary()}
+    plain = {p["spp"]: p for p in plain_series or []}
+    if j is not None and 256 in plain:
+        target, budget = plain[256]["relmse"], plain[256]["seconds"]
+        reached = [s for s in series if s["relmse"] is not None and s["relmse"] <= target]
+        out["target"] = {"plain_256spp_relmse": target, "plain_256spp_seconds": budget,
+                         "cache_seconds_to_target": min((s["seconds"] for s in reached), default=None),
+                         "best_cache_relmse": min(s["relmse"] for s in series),
+                         "cache_relmse_within_a_third": min((s["relmse"] for s in series
+                                                             if s["seconds"] <= budget / 3), default=None)}
+        if 64 in plain:
+            eq = [s for s in series if s["seconds"] <= plain[64]["seconds"] * 1.05]
+            out["target"]["equal_time_vs_plain_64spp"] = {
+                "plain_relmse": plain[64]["relmse"], "plain_seconds": plain[64]["seconds"],
+                "cache_relmse": min((s["relmse"] for s in eq), default=None)}
+    out["kernels"] = bench_cache_kernels(ctx, torch, local)
+    gs.free()
+    return out
+
+
+def bench_cache_kernels(ctx, torch, local):
+    """Inference over 2^21 queries and one training step over 2^16 records, device buffers."""
+    from pico_gb300 import RadianceCache
+    from pico_gb300.types import NRC_QUERY_DTYPE
+    lo, hi = (-200.0, -60.0, -200.0), (200.0, 65.0, 200.0)
+    c = RadianceCache(ctx, seed=3, aabb_min=lo, aabb_max=hi)
+    n = 1 << 21
+    rng = np.random.default_rng(5)
+    q = np.zeros(n, NRC_QUERY_DTYPE)
+    q["position"] = np.asarray(lo) + (np.asarray(hi) - np.asarray(lo)) * rng.random((n, 3))
+    for k in ("direction", "normal"):
+        d = rng.normal(size=(n, 3))
+        q[k] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    q["roughness"] = rng.random(n)
+    q["albedo"] = rng.random((n, 3))
+    dev = f"cuda:{local}"
+    dq = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
+    dout = torch.empty((n, 3), dtype=torch.float32, device=dev)
+    s = torch.cuda.current_stream()
+
+    def timed(fn, reps=20):
+        for _ in range(3):
+            fn()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        for _ in range(reps):
+            fn()
+        b.record(s)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    ms_inf = timed(lambda: c.infer_device(dq.data_ptr(), n, dout.data_ptr(), s.cuda_stream))
+    nt = 1 << 16
+    tt = torch.from_numpy(np.random.default_rng(1).gamma(1.0, 1.0, (nt, 4)).astype(np.float32)).to(dev)
+    ms_train = timed(lambda: c.train_device(dq.data_ptr(), tt.data_ptr(), nt, True, s.cuda_stream))
+    c.free()
+    peak = measured_bf16_peak()
+    ach = NRC_FLOPS_PER_QUERY * n / (ms_inf / 1e3) / 1e12
+    return {"inference": {"queries": n, "ms": ms_inf, "Mqueries_per_s": n / ms_inf / 1e3,
+                          "roofline": {"bound": "tensor", "achieved": ach, "peak": peak[0], "unit": "TFLOP/s",
+                                       "frac": ach / peak[0], "peak_source": peak[1],
+                                       "algorithmic_flops_per_query": NRC_FLOPS_PER_QUERY},
+                          "encoding_bytes_per_query": 16 * 8 * 4},
+            "training_step": {"records": nt, "ms": ms_train,
+                              "note": "grid-gradient clear, fused forward+backward, weight-gradient reduction and "
+                                      "Adam over the network and all 16 x 2^19 x 2 grid features"}}
+
+
+def measured_bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+    return 1900.0, "fallback"
 
 
 def cpu_render(scene, cam, args):
@@ -503,11 +622,14 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
-    render = render_physical = atrous = tonemap = hdr = None
+    render = render_physical = atrous = tonemap = hdr = cache = None
     if not args.no_render:
         gs.free()
         render = bench_render(ctx, args, torch, local)
         render_physical = bench_render(ctx, args, torch, local, estimator=1)
+        if args.nrc_passes:
+            plain = (render_physical.get("relmse") or {}).get("plain_no_early_exit")
+            cache = bench_radiance_cache(ctx, args, torch, local, plain)
         atrous = bench_atrous(ctx, args, torch, local)
         tonemap, hdr = bench_tonemap_and_hdr(ctx, args, torch, local)
 
@@ -516,7 +638,7 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clocks.summary(), "scene": info, "render_1080p": render,
-            "render_1080p_physical": render_physical, "atrous_1080p": atrous,
+            "render_1080p_physical": render_physical, "render_1080p_radiance_cache": cache, "atrous_1080p": atrous,
             "tonemap_1080p": tonemap, "hdr_1080p": hdr}
     print(json.dumps(line), flush=True)
     if dist:

@@ -284,6 +284,53 @@ int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds
                             const float* V, const float* N, const float* L, const float* u, float* f, float* pdf,
                             float* sample_L, float* sample_pdf, float* sample_weight, uint32_t* sample_ok);
 
+/* ---- batched rendering ------------------------------------------------------
+ * No counterpart in the reference, which renders one scene at a time.  Many
+ * independent renders, each what pico_gpu_render does for one (scene, camera,
+ * config, progressive buffers) with the REFERENCE or PHYSICAL estimator and
+ * no denoise / tone map, run as one CUDA graph: every render's batches are
+ * captured on its own branch (streams), the graph is instantiated and launched
+ * once, and the branches share the GPU.  The cancel flag is not polled.  Each
+ * render keeps its own path state (at most `wavefront` paths), so device
+ * memory grows with the number of renders. */
+typedef struct {
+    const pico_gpu_scene* scene;
+    pico_camera camera;
+    pico_render_config config;
+    float* pixels_rgb;              /* W*H*3, in/out, as pico_gpu_render */
+    uint32_t* sample_count;         /* W*H, in/out */
+    float* variance_rgb;            /* W*H*3, in/out */
+} pico_render_item;
+
+typedef struct {
+    uint32_t wavefront;             /* paths per batch of one render; 0: 2^20 */
+    uint32_t extend_ctas_per_sm;    /* persistent CTAs per SM of each closest-hit launch; 0: as many as fit */
+    uint32_t branches;              /* graph branches the renders are spread over; 0: one per render */
+    uint32_t reserved;
+} pico_launch_params;
+
+typedef struct {
+    double build_ms;                /* capture and instantiation of the graph */
+    double run_ms;                  /* graph launch to completion (host clock) */
+    uint64_t graph_nodes;
+    uint64_t samples;               /* samples added over all renders */
+    uint64_t rays;                  /* camera, bounce and shadow rays over all renders */
+} pico_batch_report;
+
+/* completion_ms (n entries, may be NULL): each render's finish time after the
+ * graph started, from device timestamps. */
+int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items,
+                         const pico_launch_params* params, double* completion_ms, pico_batch_report* report);
+/* Chooses launch parameters for a set of renders by timing short renders of the
+ * same items (trial_samples samples per pixel into scratch buffers; the items'
+ * buffers are not touched): the wavefront size, then the closest-hit CTAs per SM,
+ * then the number of branches, each by the highest samples per second.
+ * trials_out / trial_msamples_per_s (may be NULL) receive up to max_trials tried
+ * settings and their millions of samples per second; *ntrials the count. */
+int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, uint32_t trial_samples,
+                            pico_launch_params* best, pico_launch_params* trials_out, double* trial_msamples_per_s,
+                            uint32_t max_trials, uint32_t* ntrials);
+
 /* ---- neural radiance cache ------------------------------------------------
  * No counterpart in the reference (Mueller et al. 2021, "Real-time neural
  * radiance caching for path tracing").  A cache maps a surface point to the
@@ -329,6 +376,9 @@ typedef struct {
     uint32_t max_train_steps;       /* optimiser steps per sample pass: 4 */
     uint32_t warmup_frames;         /* training-only passes before a render's first sample: 0 */
     uint64_t seed;                  /* initial weights and training-path streams */
+    uint32_t bounces;               /* camera paths query the cache after this many bounces, one more
+                                     * behind a vertex of roughness < 0.1 (a mirror counts as 0): 1 */
+    uint32_t infer_groups;          /* 128-query tiles each inference CTA keeps in flight: 1, 2 or 4; 0: 2 */
 } pico_nrc_config;
 
 int pico_gpu_nrc_default_config(pico_nrc_config* out);

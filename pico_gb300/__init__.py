@@ -20,7 +20,7 @@ import numpy as np
 
 from .types import (SKY_CONSTANT, SKY_CUBE_RGBA8, SKY_EQUIRECT_RGBAF, Sky, SHAPE_TRIANGLES, SHAPE_SPHERE,  # noqa: F401
                     SHAPE_CUBE, BTDF, FRESNEL, DELTA,  # noqa: F401
-                    CCamera, CNrcConfig, CRenderConfig, CSceneDesc, NRC_QUERY_DTYPE, ESTIMATOR_RADIANCE_CACHE, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
+                    CCamera, CNrcConfig, CRenderConfig, CSceneDesc, CRenderItem, CLaunchParams, CBatchReport, NRC_QUERY_DTYPE, ESTIMATOR_RADIANCE_CACHE, HIT_DTYPE, RAY_DTYPE, Camera, Instance,  # noqa: F401
                     MarshalledScene, Material, Mesh, SceneData, DIFFUSE, SPECULAR, DIELECTRIC, LIGHT, MISS)
 
 LIB_PATH = Path(__file__).resolve().parent / "_build" / "libpico_gpu.so"
@@ -77,6 +77,10 @@ SIGNATURES = {
     "pico_gpu_nrc_train_device": (C.c_int, [_vp, _vp, _vp, _u64, C.c_int, _vp]),
     "pico_gpu_nrc_gradients": (C.c_int, [_vp, _vp, _vp]),
     "pico_gpu_set_radiance_cache": (C.c_int, [_vp, _vp]),
+    "pico_gpu_render_many": (C.c_int, [_vp, _u32, _vp, C.POINTER(CLaunchParams), C.POINTER(C.c_double),
+                                       C.POINTER(CBatchReport)]),
+    "pico_gpu_autotune_batch": (C.c_int, [_vp, _u32, _vp, _u32, C.POINTER(CLaunchParams), C.POINTER(CLaunchParams),
+                                          C.POINTER(C.c_double), _u32, C.POINTER(_u32)]),
 }
 
 _lib = None
@@ -150,6 +154,53 @@ class Context:
 
     def upload(self, scene: SceneData) -> "GpuScene":
         return GpuScene(self, scene)
+
+    @staticmethod
+    def _items(renders):
+        """pico_render_item array for renders given as dicts: gpu_scene, camera, max_depth, max_samples, and
+        optionally seed, estimator, max_variance, pixels, sample_count, variance (allocated when absent)."""
+        arr = (CRenderItem * max(len(renders), 1))()
+        for k, r in enumerate(renders):
+            cam = r["camera"]
+            W, H = int(cam.resolution[0]), int(cam.resolution[1])
+            r.setdefault("pixels", np.zeros((H, W, 3), np.float32))
+            r.setdefault("sample_count", np.zeros((H, W), np.uint32))
+            r.setdefault("variance", np.zeros((H, W, 3), np.float32))
+            it = arr[k]
+            it.scene = r["gpu_scene"].handle
+            it.camera = cam.to_c()
+            it.config = CRenderConfig(r["max_depth"], r["max_samples"], r.get("max_variance", 0.0), H, W, 0, 0,
+                                      r.get("estimator", 1), r.get("seed", 1))
+            it.pixels_rgb = _f32(r["pixels"])
+            it.sample_count = r["sample_count"].ctypes.data_as(C.POINTER(C.c_uint32))
+            it.variance_rgb = _f32(r["variance"])
+        return arr
+
+    def render_many(self, renders, wavefront: int = 0, extend_ctas_per_sm: int = 0, branches: int = 0):
+        """pico_gpu_render_many: all renders in one CUDA graph launch; their buffers are updated in place.
+        Returns (per-render completion times in ms, report dict)."""
+        arr = self._items(renders)
+        params = CLaunchParams(wavefront, extend_ctas_per_sm, branches, 0)
+        done = (C.c_double * max(len(renders), 1))()
+        rep = CBatchReport()
+        self.check(self.lib.pico_gpu_render_many(self.handle, len(renders), arr, C.byref(params), done,
+                                                 C.byref(rep)), "render_many")
+        report = {k: getattr(rep, k) for k in ("build_ms", "run_ms", "graph_nodes", "samples", "rays")}
+        return np.array(done[:len(renders)]), report
+
+    def autotune_batch(self, renders, trial_samples: int = 1):
+        """pico_gpu_autotune_batch: (best launch parameters, [(parameters, Msamples/s) per trial])."""
+        arr = self._items(renders)
+        best = CLaunchParams()
+        trials = (CLaunchParams * 16)()
+        rates = (C.c_double * 16)()
+        nt = C.c_uint32(0)
+        self.check(self.lib.pico_gpu_autotune_batch(self.handle, len(renders), arr, trial_samples, C.byref(best),
+                                                    trials, rates, 16, C.byref(nt)), "autotune_batch")
+
+        def as_dict(p):
+            return {"wavefront": p.wavefront, "extend_ctas_per_sm": p.extend_ctas_per_sm, "branches": p.branches}
+        return as_dict(best), [(as_dict(trials[i]), rates[i]) for i in range(nt.value)]
 
     def atrous(self, pixels, normals, positions, diffuse, width: int, height: int) -> np.ndarray:
         arrs = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (pixels, normals, positions, diffuse)]

@@ -90,6 +90,7 @@ void pico_gpu_shutdown(pico_gpu_ctx* ctx)
     cudaSetDevice(ctx->device);
     for (DeviceBuffer* b : {&ctx->buf_a, &ctx->buf_b, &ctx->buf_c, &ctx->buf_d, &ctx->buf_e}) b->release();
     free_render_buffers(ctx);
+    free_batch_state(ctx);
     if (ctx->status) cudaFree(ctx->status);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->stream2) cudaStreamDestroy(ctx->stream2);

@@ -14,6 +14,7 @@
 #include <vector>
 
 struct RenderBuffers;
+struct BatchState;
 struct pico_gpu_nrc;
 
 namespace pico {
@@ -39,6 +40,7 @@ struct pico_gpu_ctx {
     int order = PICO_ORDER_NEAR_FIRST;          // traversal order of every trace in this context
     uint64_t render_stats[5] = {0, 0, 0, 0, 0}; // tallies of the last pico_gpu_render call
     pico_gpu_nrc* cache = nullptr;              // radiance cache of PICO_ESTIMATOR_RADIANCE_CACHE renders
+    BatchState* batch = nullptr;                // per-render state and streams of pico_gpu_render_many
     pico::DeviceStatus* status2() { return status + 1; }
 };
 
@@ -70,4 +72,5 @@ int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what);
 int take_device_status(pico_gpu_ctx* ctx, cudaStream_t stream);
 RenderBuffers* render_buffers(pico_gpu_ctx* ctx);
 void free_render_buffers(pico_gpu_ctx* ctx);
+void free_batch_state(pico_gpu_ctx* ctx);
 }  // namespace pico

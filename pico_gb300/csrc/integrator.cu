@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
             float4 thr = b.thr[i], pay = b.pay[i];
             const float4 dir = b.dir[i];
             const bool terminal = nrc.mode == kNrcTerminate && rank != kNoHit &&
-                                  (depth >= 2 || (depth == 1 && nrc.prev_rough[i] >= 0.1f));
+                                  (depth > nrc.bounces || (depth == nrc.bounces && nrc.prev_rough[i] >= 0.1f));
             if (rank == kNoHit) {
                 const float3 sk = sky_radiance(sc, dir.x, dir.y, dir.z);
                 pay.x += thr.x * sk.x; pay.y += thr.y * sk.y; pay.z += thr.z * sk.z;
@@ -657,23 +657,39 @@ static unsigned grid_for(uint32_t n, int threads)
     return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
+// Persistent grid of a closest-hit launch: `ctas_per_sm` CTAs per SM (0 or more
+// than fit: as many as fit).
 template <int kOrder>
-static unsigned extend_grid()
+static unsigned extend_grid(uint32_t ctas_per_sm)
 {
     static int per_sm = 0;
     if (!per_sm) {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder>, 128, 0);
         if (per_sm < 1) per_sm = 1;
     }
-    return (unsigned)(sm_count() * per_sm);
+    const int k = (ctas_per_sm > 0 && (int)ctas_per_sm < per_sm) ? (int)ctas_per_sm : per_sm;
+    return (unsigned)(sm_count() * k);
 }
 
 template <int kOrder>
 static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
                           DeviceStatus* status, bool shadow, unsigned long long* tally, cudaStream_t st)
 {
-    extend_kernel<kOrder><<<extend_grid<kOrder>(), 128, 0, st>>>(sc, b, q, count, &status->work,
-                                                                  &status->trace_error, shadow, tally);
+    extend_kernel<kOrder><<<extend_grid<kOrder>(b.extend_ctas), 128, 0, st>>>(sc, b, q, count, &status->work,
+                                                                              &status->trace_error, shadow, tally);
+}
+
+__global__ void stamp_kernel(unsigned long long* dst)
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *dst = t;
+}
+
+cudaError_t launch_stamp(unsigned long long* dst, cudaStream_t st)
+{
+    stamp_kernel<<<1, 1, 0, st>>>(dst);
+    return cudaGetLastError();
 }
 
 // The extend / shade / shadow loop of one batch whose camera rays are queued.
@@ -748,7 +764,7 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     if (e != cudaSuccess) return e;
     if (na.mode == kNrcTerminate) {
         e = nrc::launch_infer(na.geo, na.table, na.weights, na.queries, na.capacity, nullptr, b.thr, b.pay, na.err, st,
-                              na.count);
+                              na.count, na.infer_groups);
         if (e != cudaSuccess) return e;
     }
     finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);

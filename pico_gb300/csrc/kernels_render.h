@@ -22,7 +22,8 @@ struct CameraView {
 // Structure-of-arrays path state of one batch (capacity >= n) and the
 // per-pixel accumulation buffers of the whole image.
 struct PathBatch {
-    uint32_t n, npix, width, pad;
+    uint32_t n, npix, width;
+    uint32_t extend_ctas;              // closest-hit launches: persistent CTAs per SM (0: as many as fit)
     const uint32_t* pix_list;          // npix pixel indices
     float4* org; float4* dir; float4* thr; float4* pay;
     float4* hit; uint32_t* hit_tri;
@@ -52,6 +53,7 @@ enum NrcMode { kNrcOff = 0, kNrcRecord = 1, kNrcTerminate = 2 };
 struct NrcShadeArgs {
     int mode;
     uint32_t capacity;        // entries of queries / rec_tp
+    uint32_t bounces;         // kNrcTerminate: bounces before the cache answers (one more behind a glossy vertex)
     float4* queries;          // 4 float4 per entry (pico_nrc_query)
     float4* rec_tp;           // kNrcRecord: 2 float4 per entry
     uint32_t* count;          // entries appended
@@ -61,6 +63,7 @@ struct NrcShadeArgs {
     const __half2* table;
     const uint8_t* weights;
     int* err;
+    int infer_groups;
 };
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
@@ -75,6 +78,8 @@ cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const Camer
                                   uint32_t frame, uint32_t n, uint32_t W, uint32_t H, uint32_t max_depth,
                                   const NrcShadeArgs& nrc, float4* targets, DeviceStatus* status, int order,
                                   cudaStream_t st);
+// Writes the device's global nanosecond timer to *dst when the stream reaches it.
+cudaError_t launch_stamp(unsigned long long* dst, cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
 // Floats of a-trous scratch per 64 x 64 tile: four partial statistics records

@@ -37,10 +37,11 @@ namespace nrc {
 namespace {
 
 constexpr int kThreads = 128;
-constexpr uint32_t kInferSmem = kWeightRegion + kTileBytes + 64 + 1024;
+// Inference CTAs hold G warpgroups (128-row tiles in flight), G = 1, 2 or 4.
+constexpr uint32_t infer_smem(int G) { return kWeightRegion + (uint32_t)G * kTileBytes + 64 + 1024; }
+constexpr uint32_t infer_tmem_cols(int G) { return 64u * (uint32_t)G; }   // a power of two for G = 1, 2, 4
 constexpr uint32_t kTrainSmem = kWeightRegion + 6 * kTileBytes + kTileBytes + kGuardBytes + 64 + 1024;
 constexpr uint32_t kTrainTmemCols = 512;   // accumulator 0-63, dW_l at 64 + 64 l
-constexpr uint32_t kInferTmemCols = 64;
 
 __device__ __forceinline__ uint8_t* align1024(uint8_t* p)
 {
@@ -92,41 +93,58 @@ struct InferArgs {
     const uint32_t* n_dev;
 };
 
-__global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
+// G warpgroups per CTA share one copy of the weights; each runs its own 128-row
+// tiles with its own shared-memory tile, TMEM columns (64 g .. 64 g + 63) and
+// mbarrier, and synchronises on its own named barrier (1 + g), so that one
+// group's encoding (hash-grid gathers) overlaps another's tensor-core layers.
+__device__ __forceinline__ bool group_sync_and(uint32_t id, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(id)
+        : "memory");
+    return r != 0;
+}
+
+template <int G>
+__global__ void __launch_bounds__(128 * G) infer_kernel(InferArgs a)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* sm = align1024(smem_raw);
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, g = tid >> 7, gtid = tid & 127u;
     uint8_t* W = sm;
-    uint8_t* X = sm + kWeightRegion;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(X + kTileBytes);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2);
-    const uint32_t tid = threadIdx.x, warp = tid >> 5;
-    const uint32_t bar_w = smem_addr(bars), bar_m = smem_addr(bars + 1);
+    uint8_t* X = sm + kWeightRegion + g * kTileBytes;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kWeightRegion + G * kTileBytes);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + G);
+    const uint32_t bar_w = smem_addr(bars), bar_m = smem_addr(bars + 1 + g);
     if (tid == 0) {
         mbar_init(bar_w, 1);
-        mbar_init(bar_m, 1);
+        for (int k = 0; k < G; ++k) mbar_init(smem_addr(bars + 1 + k), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        tmem_alloc(smem_addr(tslot), kInferTmemCols);
+        tmem_alloc(smem_addr(tslot), infer_tmem_cols(G));
         tmem_relinquish();
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *tslot;
+    const uint32_t tmem = *tslot + 64u * g;
     if (tid == 0) {
         mbar_expect_tx(bar_w, kWeightBytes);
         bulk_load(smem_addr(W), a.weights, kWeightBytes, bar_w);
     }
     bool ok = mbar_wait(bar_w, 0);
     uint32_t phase = 0;
-    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    const uint32_t lane_addr = tmem + (((warp & 3u) * 32u) << 16);
     const uint32_t x_addr = smem_addr(X), w_addr = smem_addr(W);
     const uint32_t n = a.n_dev ? min(*a.n_dev, a.n) : a.n;
     const uint32_t ntiles = (n + kRows - 1) / kRows;
-    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const uint32_t row = t * kRows + tid;
+    for (uint32_t t = blockIdx.x * G + g; t < ntiles; t += gridDim.x * G) {
+        const uint32_t row = t * kRows + gtid;
         const bool valid = row < n;
         uint32_t payload = 0;
         {
@@ -139,15 +157,15 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
 #pragma unroll
                 for (int k = 0; k < kWidth; ++k) in[k] = 0.0f;
             }
-            store_row<false>(X, tid, in);
+            store_row<false>(X, gtid, in);
         }
         bool abort = false;
 #pragma unroll 1
         for (int l = 0; l < kLayers; ++l) {
             fence_async_smem();
             tc_fence_before();
-            if (!__syncthreads_and(ok)) { abort = true; break; }
-            if (tid == 0) {
+            if (!group_sync_and(1u + g, ok)) { abort = true; break; }
+            if (gtid == 0) {
                 tc_fence_after();
                 issue_forward(tmem, x_addr, w_addr + (uint32_t)l * kLayerBytes, l);
                 mma_commit(bar_m);
@@ -159,7 +177,7 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
                 float v[kWidth];
 #pragma unroll
                 for (int c = 0; c < 4; ++c) tmem_ld16(lane_addr + 16 * c, v + 16 * c);
-                store_row<true>(X, tid, v);
+                store_row<true>(X, gtid, v);
             } else {
                 float v[16];
                 tmem_ld16(lane_addr, v);
@@ -180,10 +198,10 @@ __global__ void __launch_bounds__(kThreads) infer_kernel(InferArgs a)
         }
         if (abort) break;
     }
-    if (!ok && tid == 0) set_error(a.err, kErrTimeout);
+    if (!ok && gtid == 0) set_error(a.err, kErrTimeout);
     tc_fence_before();
     __syncthreads();
-    if (warp == 0) tmem_dealloc(tmem, kInferTmemCols);
+    if (warp == 0) tmem_dealloc(*tslot, infer_tmem_cols(G));
 }
 
 // ------------------------------------------------------------------ training
@@ -472,26 +490,37 @@ cudaError_t launch_encode(const GridGeometry& g, const __half2* table, const flo
     return cudaGetLastError();
 }
 
+template <int G>
+static cudaError_t launch_infer_groups(const InferArgs& a, cudaStream_t st)
+{
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaError_t e = cudaFuncSetAttribute(infer_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             infer_smem(G));
+        if (e != cudaSuccess) return e;
+        int occ = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, infer_kernel<G>, 128 * G, infer_smem(G));
+        const int tmem_cap = (int)(512u / infer_tmem_cols(G));   // resident CTAs' columns fit the SM's 512
+        per_sm = occ < 1 ? 1 : (occ > tmem_cap ? tmem_cap : occ);
+    }
+    const uint32_t tiles = (a.n + kRows - 1) / kRows;
+    const uint32_t want = (tiles + G - 1) / G;
+    const uint32_t cap = (uint32_t)(sm_count() * per_sm);
+    infer_kernel<G><<<want < cap ? want : cap, 128 * G, infer_smem(G), st>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint8_t* weights, const float4* queries,
                          uint32_t n, float* out_rgb, const float4* thr, float4* pay, int* err, cudaStream_t st,
-                         const uint32_t* n_dev)
+                         const uint32_t* n_dev, int groups)
 {
     if (n == 0) return cudaSuccess;
-    static bool configured = false;
-    static int per_sm = 1;
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kInferSmem);
-        if (e != cudaSuccess) return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, infer_kernel, kThreads, kInferSmem);
-        if (per_sm < 1) per_sm = 1;
-        if (per_sm > 8) per_sm = 8;   // 8 x 64 TMEM columns fill the SM's 512
-        configured = true;
+    const InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev};
+    switch (groups) {
+    case 1: return launch_infer_groups<1>(a, st);
+    case 4: return launch_infer_groups<4>(a, st);
+    default: return launch_infer_groups<2>(a, st);
     }
-    const uint32_t tiles = (n + kRows - 1) / kRows;
-    const uint32_t cap = (uint32_t)(sm_count() * per_sm);
-    InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev};
-    infer_kernel<<<tiles < cap ? tiles : cap, kThreads, kInferSmem, st>>>(a);
-    return cudaGetLastError();
 }
 
 cudaError_t launch_train(const GridGeometry& g, const __half2* table, const uint8_t* weights, const TrainBatch& b,

@@ -38,6 +38,11 @@ bool valid_config(const pico_nrc_config& c, std::string& why)
         return false;
     }
     if (c.train_batch == 0 || c.train_batch > kMaxTrainBatch) { why = "train_batch must lie in [1, 2^20]"; return false; }
+    if (c.bounces < 1 || c.bounces > 8) { why = "bounces must lie in [1, 8]"; return false; }
+    if (c.infer_groups != 0 && c.infer_groups != 1 && c.infer_groups != 2 && c.infer_groups != 4) {
+        why = "infer_groups must be 0, 1, 2 or 4";
+        return false;
+    }
     return true;
 }
 
@@ -139,6 +144,7 @@ int pico_gpu_nrc_default_config(pico_nrc_config* out)
     out->max_train_steps = 4;
     out->warmup_frames = 0;
     out->seed = 1;
+    out->bounces = 1;
     return PICO_OK;
 }
 
@@ -300,7 +306,8 @@ int pico_gpu_nrc_infer_device(pico_gpu_nrc* c, const pico_nrc_query* d_q, uint64
     if (n > kMaxQueries) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "too many queries");
     cudaSetDevice(c->ctx->device);
     cudaError_t e = launch_infer(c->geo, c->table, c->image, reinterpret_cast<const float4*>(d_q), (uint32_t)n, d_rgb,
-                                 nullptr, nullptr, c->err, static_cast<cudaStream_t>(stream));
+                                 nullptr, nullptr, c->err, static_cast<cudaStream_t>(stream), nullptr,
+                                 (int)c->cfg.infer_groups);
     if (e != cudaSuccess) return cuda_error(c->ctx, e, "radiance cache inference");
     return PICO_OK;
 }

@@ -9,9 +9,8 @@
 // paths (pixels x samples), each pixel's samples in order across batches; the
 // cancel flag is polled between batches.  When requested, the a-trous pass
 // then runs on the result and replaces it (Scene.cpp:212-234).
-#include "capi_internal.h"
-#include "kernels_render.h"
 #include "nrc_internal.h"
+#include "render_internal.h"
 
 #include <cmath>
 #include <cstring>
@@ -19,8 +18,6 @@
 using namespace pico;
 
 namespace {
-
-constexpr uint32_t kMaxPaths = 1u << 22;
 
 // glm-order float helpers for the host-side camera quantities.
 float dot3(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
@@ -36,7 +33,10 @@ void normalize3(const float* a, float* o)
     o[0] = a[0] * s; o[1] = a[1] * s; o[2] = a[2] * s;
 }
 
-// Camera::getRight (Core/Camera.hpp:64-65) and Camera::getViewMatrix (glm::lookAtRH).
+}  // namespace
+
+namespace pico {
+
 CameraView make_camera_view(const pico_camera& c)
 {
     CameraView v{};
@@ -65,32 +65,6 @@ CameraView make_camera_view(const pico_camera& c)
     return v;
 }
 
-template <class T>
-T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }
-
-}  // namespace
-
-// Path state and image buffers owned by the context, grown on demand.
-struct RenderBuffers {
-    DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, ior_n, ior_lo, ior_hi, sorg, sdir, scontrib, senergy,
-        q0, q1, sq, counters, samples;
-    DeviceBuffer pixels, variance, count, taken, done, pix_list;
-    DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
-    // radiance cache: terminal queries / training records, record throughput and
-    // payload, targets, previous roughness per path, entry counters
-    DeviceBuffer nrc_q, nrc_tp, nrc_tgt, nrc_prev, nrc_count;
-    ~RenderBuffers()
-    {
-        for (DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
-                                &sorg, &sdir, &scontrib,
-                                &senergy, &q0, &q1, &sq, &counters, &samples, &pixels, &variance, &count, &taken,
-                                &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats, &out, &tonemap, &nrc_q, &nrc_tp,
-                                &nrc_tgt, &nrc_prev, &nrc_count})
-            b->release();
-    }
-};
-
-namespace pico {
 RenderBuffers* render_buffers(pico_gpu_ctx* ctx)
 {
     if (!ctx->render) ctx->render = new RenderBuffers();
@@ -101,9 +75,6 @@ void free_render_buffers(pico_gpu_ctx* ctx)
     delete ctx->render;
     ctx->render = nullptr;
 }
-}  // namespace pico
-
-namespace {
 
 cudaError_t reserve_paths(RenderBuffers& r, size_t n)
 {
@@ -118,23 +89,6 @@ cudaError_t reserve_paths(RenderBuffers& r, size_t n)
     return e;
 }
 
-int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const float* d_n, const float* d_p,
-               const float* d_d, uint32_t W, uint32_t H, float* d_out, cudaStream_t st)
-{
-    const size_t n = (size_t)W * H * 3;
-    const size_t tiles = (size_t)((W + 63) / 64) * ((H + 63) / 64);
-    cudaError_t e = r.ga.reserve(n * sizeof(float));
-    if (e == cudaSuccess) e = r.gb.reserve(n * sizeof(float));
-    if (e == cudaSuccess) e = r.stats.reserve(tiles * kAtrousStatsFloatsPerTile * sizeof(float));
-    if (e == cudaSuccess)
-        e = launch_atrous(d_pix, d_n, d_p, d_d, W, H, as<float>(r.ga), as<float>(r.gb), as<float>(r.stats), d_out, st);
-    if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous");
-    return PICO_OK;
-}
-
-bool valid_camera(const pico_camera* c) { return c && c->resolution[0] > 0 && c->resolution[1] > 0; }
-
-// The path state of a batch of n paths over npix listed pixels, in the context's buffers.
 PathBatch make_batch(RenderBuffers& r, uint32_t n, uint32_t npix, uint32_t W, const uint32_t* pix_list)
 {
     PathBatch b{};
@@ -152,6 +106,26 @@ PathBatch make_batch(RenderBuffers& r, uint32_t n, uint32_t npix, uint32_t W, co
     b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
     return b;
 }
+
+}  // namespace pico
+
+namespace {
+
+int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const float* d_n, const float* d_p,
+               const float* d_d, uint32_t W, uint32_t H, float* d_out, cudaStream_t st)
+{
+    const size_t n = (size_t)W * H * 3;
+    const size_t tiles = (size_t)((W + 63) / 64) * ((H + 63) / 64);
+    cudaError_t e = r.ga.reserve(n * sizeof(float));
+    if (e == cudaSuccess) e = r.gb.reserve(n * sizeof(float));
+    if (e == cudaSuccess) e = r.stats.reserve(tiles * kAtrousStatsFloatsPerTile * sizeof(float));
+    if (e == cudaSuccess)
+        e = launch_atrous(d_pix, d_n, d_p, d_d, W, H, as<float>(r.ga), as<float>(r.gb), as<float>(r.stats), d_out, st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous");
+    return PICO_OK;
+}
+
+bool valid_camera(const pico_camera* c) { return c && c->resolution[0] > 0 && c->resolution[1] > 0; }
 
 // PICO_ESTIMATOR_RADIANCE_CACHE: warmup_frames training-only passes, then per
 // sample pass the cache trains on train_paths full-depth physical paths (at most
@@ -189,6 +163,8 @@ int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_n
     na.table = c->table;
     na.weights = c->image;
     na.err = c->err;
+    na.bounces = c->cfg.bounces;
+    na.infer_groups = (int)c->cfg.infer_groups;
     const unsigned long long train_seed = c->cfg.seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
     const int order = scene_order(ctx, scene);
     const bool training = ntrain > 0 && c->cfg.max_train_steps > 0;

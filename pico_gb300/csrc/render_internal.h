@@ -1,0 +1,39 @@
+// Render state shared by the single-render and batched-render entry points.
+#pragma once
+
+#include "capi_internal.h"
+#include "kernels_render.h"
+
+// Path state and image buffers of one render, grown on demand.
+struct RenderBuffers {
+    pico::DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, ior_n, ior_lo, ior_hi, sorg, sdir, scontrib,
+        senergy, q0, q1, sq, counters, samples;
+    pico::DeviceBuffer pixels, variance, count, taken, done, pix_list;
+    pico::DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
+    // radiance cache: terminal queries / training records, record throughput and
+    // payload, targets, previous roughness per path, entry counters
+    pico::DeviceBuffer nrc_q, nrc_tp, nrc_tgt, nrc_prev, nrc_count;
+    ~RenderBuffers()
+    {
+        for (pico::DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
+                                      &sorg, &sdir, &scontrib, &senergy, &q0, &q1, &sq, &counters, &samples, &pixels,
+                                      &variance, &count, &taken, &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats,
+                                      &out, &tonemap, &nrc_q, &nrc_tp, &nrc_tgt, &nrc_prev, &nrc_count})
+            b->release();
+    }
+};
+
+namespace pico {
+
+constexpr uint32_t kMaxPaths = 1u << 22;   // paths of one batch (pixels x samples)
+
+template <class T>
+T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }
+
+// Camera::getRight (Core/Camera.hpp:64-65) and Camera::getViewMatrix (glm::lookAtRH).
+CameraView make_camera_view(const pico_camera& c);
+cudaError_t reserve_paths(RenderBuffers& r, size_t n);
+// The path state of a batch of n paths over npix listed pixels, in r's buffers.
+PathBatch make_batch(RenderBuffers& r, uint32_t n, uint32_t npix, uint32_t W, const uint32_t* pix_list);
+
+}  // namespace pico

@@ -238,6 +238,30 @@ def lit_field(n_instances: int = 4096, level: int = 4, seed: int = 12345, n_ligh
     return s
 
 
+BATCH_RESOLUTIONS = ((128, 128), (256, 256), (512, 512), (768, 432), (1024, 1024))
+BATCH_SPP = (4, 16, 64)
+
+
+def batch_workload(n_renders: int = 64, seed: int = 2024, level: int = 4, size_scale: float = 1.0):
+    """Heterogeneous renders for batched rendering, each from its own seed: resolution uniform
+    from 128^2, 256^2, 512^2, 768x432, 1024^2 (times size_scale), a lit field of 64-4096
+    instances (log-uniform), spp uniform from {4, 16, 64}, depth uniform in 4-8.  Returns a list
+    of dicts with scene, camera, max_samples, max_depth and seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_renders):
+        W, H = BATCH_RESOLUTIONS[rng.integers(len(BATCH_RESOLUTIONS))]
+        W, H = max(8, int(W * size_scale)), max(8, int(H * size_scale))
+        n_inst = int(round(np.exp(rng.uniform(np.log(64), np.log(4096)))))
+        spp = int(BATCH_SPP[rng.integers(len(BATCH_SPP))])
+        depth = int(rng.integers(4, 9))
+        scene_seed = int(rng.integers(1, 2**31 - 1))
+        out.append({"scene": lit_field(n_instances=n_inst, level=level, seed=scene_seed),
+                    "camera": lit_field_camera(W, H), "max_samples": spp, "max_depth": depth, "seed": k + 1,
+                    "instances": n_inst})
+    return out
+
+
 def cornell_shapes() -> SceneData:
     """The Cornell box with the implicit assets and the remaining lobes: a Transparent
     and a Fresnel glass sphere (IoR 1.5), a Delta mirror cube, and a small sphere and a

@@ -64,13 +64,23 @@ class CCamera(C.Structure):
                 ("far_plane", C.c_float), ("fov", C.c_float)]
 
 
+class CLaunchParams(C.Structure):
+    _fields_ = [("wavefront", C.c_uint32), ("extend_ctas_per_sm", C.c_uint32), ("branches", C.c_uint32),
+                ("reserved", C.c_uint32)]
+
+
+class CBatchReport(C.Structure):
+    _fields_ = [("build_ms", C.c_double), ("run_ms", C.c_double), ("graph_nodes", C.c_uint64),
+                ("samples", C.c_uint64), ("rays", C.c_uint64)]
+
+
 class CNrcConfig(C.Structure):
     """pico_nrc_config: the radiance cache's encoding, optimiser and per-frame training budget."""
     _fields_ = [("log2_table_size", C.c_uint32), ("base_resolution", C.c_float), ("max_resolution", C.c_float),
                 ("aabb_min", C.c_float * 3), ("aabb_max", C.c_float * 3), ("learning_rate", C.c_float),
                 ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float), ("train_paths", C.c_uint32),
                 ("train_batch", C.c_uint32), ("max_train_steps", C.c_uint32), ("warmup_frames", C.c_uint32),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("bounces", C.c_uint32), ("infer_groups", C.c_uint32)]
 
 
 # pico_nrc_query: 16 x 4 bytes.
@@ -82,6 +92,13 @@ class CRenderConfig(C.Structure):
     _fields_ = [("max_ray_depth", C.c_uint32), ("max_samples", C.c_uint32), ("max_variance", C.c_float),
                 ("height", C.c_uint32), ("width", C.c_uint32), ("tonemap", C.c_int32),
                 ("denoise", C.c_int32), ("estimator", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class CRenderItem(C.Structure):
+    """pico_render_item: one render of a batch (scene handle, camera, config, progressive buffers)."""
+    _fields_ = [("scene", C.c_void_p), ("camera", CCamera), ("config", CRenderConfig),
+                ("pixels_rgb", C.POINTER(C.c_float)), ("sample_count", C.POINTER(C.c_uint32)),
+                ("variance_rgb", C.POINTER(C.c_float))]
 
 
 @dataclass
