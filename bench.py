@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--render-depth", type=int, default=8)
     ap.add_argument("--render-cpu-pixels", type=int, default=8192)
     ap.add_argument("--nrc-passes", type=int, nargs="*", default=[16, 32, 64, 96, 128])
+    ap.add_argument("--batch-renders", type=int, default=64, help="renders of the batched-rendering line (0: skip)")
     return ap.parse_args()
 
 
@@ -365,6 +366,11 @@ def bench_cache_kernels(ctx, torch, local):
         return a.elapsed_time(b) / reps
 
     ms_inf = timed(lambda: c.infer_device(dq.data_ptr(), n, dout.data_ptr(), s.cuda_stream))
+    per_groups = {}
+    for groups in (1, 2, 4):
+        cg = RadianceCache(ctx, seed=3, aabb_min=lo, aabb_max=hi, infer_groups=groups)
+        per_groups[str(groups)] = timed(lambda: cg.infer_device(dq.data_ptr(), n, dout.data_ptr(), s.cuda_stream))
+        cg.free()
     nt = 1 << 16
     tt = torch.from_numpy(np.random.default_rng(1).gamma(1.0, 1.0, (nt, 4)).astype(np.float32)).to(dev)
     ms_train = timed(lambda: c.train_device(dq.data_ptr(), tt.data_ptr(), nt, True, s.cuda_stream))
@@ -372,6 +378,9 @@ def bench_cache_kernels(ctx, torch, local):
     peak = measured_bf16_peak()
     ach = NRC_FLOPS_PER_QUERY * n / (ms_inf / 1e3) / 1e12
     return {"inference": {"queries": n, "ms": ms_inf, "Mqueries_per_s": n / ms_inf / 1e3,
+                          "ms_by_warpgroups_per_cta": per_groups,
+                          "queries_note": "uniformly random positions over the lit field's box: incoherent "
+                                          "hash-grid gathers (render queries are coherent)",
                           "roofline": {"bound": "tensor", "achieved": ach, "peak": peak[0], "unit": "TFLOP/s",
                                        "frac": ach / peak[0], "peak_source": peak[1],
                                        "algorithmic_flops_per_query": NRC_FLOPS_PER_QUERY},
@@ -379,6 +388,49 @@ def bench_cache_kernels(ctx, torch, local):
             "training_step": {"records": nt, "ms": ms_train,
                               "note": "grid-gradient clear, fused forward+backward, weight-gradient reduction and "
                                       "Adam over the network and all 16 x 2^19 x 2 grid features"}}
+
+
+def bench_batch(ctx, args, local):
+    """Batched heterogeneous rendering: args.batch_renders renders (resolutions from 128^2 to 1024^2,
+    lit fields of 64-4096 instances, 4/16/64 spp, depth 4-8, physical estimator) in one CUDA-graph
+    launch with launch parameters chosen by the autotuner; aggregate Msamples/s over the graph's run
+    and per-render completion times; the same renders as back-to-back pico_gpu_render calls beside it."""
+    work = scenes.batch_workload(args.batch_renders)
+    gsc = [ctx.upload(w["scene"]) for w in work]
+
+    def items():
+        return [{"gpu_scene": g, "camera": w["camera"], "max_samples": w["max_samples"], "max_depth": w["max_depth"],
+                 "seed": w["seed"], "estimator": 1} for g, w in zip(gsc, work)]
+    t0 = time.perf_counter()
+    best, trials = ctx.autotune_batch(items(), trial_samples=1)
+    tune_s = time.perf_counter() - t0
+    its = items()
+    with ClockSampler(local) as clocks:
+        done, rep = ctx.render_many(its, **best)
+    t0 = time.perf_counter()
+    seq_samples = 0
+    for g, w in zip(gsc, work):
+        _, cnt, _ = g.render(w["camera"], w["max_depth"], w["max_samples"], seed=w["seed"], estimator=1)
+        seq_samples += int(cnt.sum())
+    seq_s = time.perf_counter() - t0
+    for g in gsc:
+        g.free()
+    res = sorted({f"{w['camera'].resolution[0]}x{w['camera'].resolution[1]}" for w in work})
+    return {"workload": f"{len(work)} renders in one CUDA graph: resolutions {', '.join(res)}, lit fields of "
+                        f"{min(w['instances'] for w in work)}-{max(w['instances'] for w in work)} instances, "
+                        f"spp 4/16/64, depth 4-8, physical estimator",
+            "Msamples_per_s": rep["samples"] / rep["run_ms"] / 1e3, "Mrays_per_s": rep["rays"] / rep["run_ms"] / 1e3,
+            "samples": rep["samples"], "run_ms": rep["run_ms"], "graph_build_ms": rep["build_ms"],
+            "graph_nodes": rep["graph_nodes"],
+            "completion_ms": {"p50": float(np.percentile(done, 50)), "p99": float(np.percentile(done, 99)),
+                              "max": float(done.max())},
+            "autotuner": {"chosen": best, "seconds": tune_s,
+                          "trials": [{"params": t, "Msamples_per_s": r} for t, r in trials]},
+            "sequential_calls": {"Msamples_per_s": seq_samples / seq_s / 1e6, "seconds": seq_s,
+                                 "note": "the same renders as back-to-back pico_gpu_render calls (host buffers)"},
+            "timing": "run_ms: host clock around the graph launch and its completion; completion times from "
+                      "device timestamps at the graph start and at the end of each render",
+            "clocks": clocks.summary()}
 
 
 def measured_bf16_peak():
@@ -622,7 +674,7 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
-    render = render_physical = atrous = tonemap = hdr = cache = None
+    render = render_physical = atrous = tonemap = hdr = cache = batched = None
     if not args.no_render:
         gs.free()
         render = bench_render(ctx, args, torch, local)
@@ -630,6 +682,8 @@ def main():
         if args.nrc_passes:
             plain = (render_physical.get("relmse") or {}).get("plain_no_early_exit")
             cache = bench_radiance_cache(ctx, args, torch, local, plain)
+        if args.batch_renders > 0:
+            batched = bench_batch(ctx, args, local)
         atrous = bench_atrous(ctx, args, torch, local)
         tonemap, hdr = bench_tonemap_and_hdr(ctx, args, torch, local)
 
@@ -638,7 +692,8 @@ def main():
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
             "clocks": clocks.summary(), "scene": info, "render_1080p": render,
-            "render_1080p_physical": render_physical, "render_1080p_radiance_cache": cache, "atrous_1080p": atrous,
+            "render_1080p_physical": render_physical, "render_1080p_radiance_cache": cache,
+            "batched_renders": batched, "atrous_1080p": atrous,
             "tonemap_1080p": tonemap, "hdr_1080p": hdr}
     print(json.dumps(line), flush=True)
     if dist:

@@ -1,0 +1,83 @@
+"""Small drivers that run one part of the library on synthetic inputs, for profiling.
+
+    python -m pico_gb300.drivers cache [--queries N] [--records N] [--reps K]
+        radiance-cache inference over N queries and K training steps over N records
+        (uniformly random positions over a 400 x 125 x 400 box, seeded)
+    python -m pico_gb300.drivers cache-render [--passes K]
+        a 1920x1080 render of the lit field through the radiance cache
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+import pico_gb300
+from pico_gb300 import RadianceCache, scenes
+from pico_gb300.types import NRC_QUERY_DTYPE
+
+LO, HI = (-200.0, -60.0, -200.0), (200.0, 65.0, 200.0)
+
+
+def random_queries(n: int, seed: int = 5) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    q = np.zeros(n, NRC_QUERY_DTYPE)
+    q["position"] = np.asarray(LO) + (np.asarray(HI) - np.asarray(LO)) * rng.random((n, 3))
+    for k in ("direction", "normal"):
+        d = rng.normal(size=(n, 3))
+        q[k] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    q["roughness"] = rng.random(n)
+    q["albedo"] = rng.random((n, 3))
+    return q
+
+
+def cache(queries: int, records: int, reps: int) -> None:
+    import torch
+    ctx = pico_gb300.Context(0)
+    c = RadianceCache(ctx, seed=3, aabb_min=LO, aabb_max=HI)
+    q = random_queries(max(queries, records))
+    dq = torch.from_numpy(q.view(np.uint8).copy()).cuda()
+    out = torch.empty((queries, 3), dtype=torch.float32, device="cuda")
+    tgt = torch.from_numpy(np.random.default_rng(1).gamma(1.0, 1.0, (records, 4)).astype(np.float32)).cuda()
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(reps):
+        c.infer_device(dq.data_ptr(), queries, out.data_ptr(), s)
+    for _ in range(reps):
+        c.train_device(dq.data_ptr(), tgt.data_ptr(), records, True, s)
+    torch.cuda.synchronize()
+    print(f"cache driver: {reps} inferences of {queries} queries, {reps} training steps of {records} records, "
+          f"{c.info()['steps']} optimiser steps")
+    c.free()
+    ctx.close()
+
+
+def cache_render(passes: int) -> None:
+    ctx = pico_gb300.Context(0)
+    scene = scenes.lit_field()
+    cam = scenes.lit_field_camera(1920, 1080)
+    gs = ctx.upload(scene)
+    c = RadianceCache(ctx, seed=3)
+    c.attach()
+    gs.render(cam, 8, passes, seed=99, estimator=2)
+    print("cache-render driver:", c.stats())
+    c.free()
+    gs.free()
+    ctx.close()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["cache", "cache-render"])
+    ap.add_argument("--queries", type=int, default=1 << 21)
+    ap.add_argument("--records", type=int, default=1 << 16)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--passes", type=int, default=3)
+    a = ap.parse_args()
+    if a.what == "cache":
+        cache(a.queries, a.records, a.reps)
+    else:
+        cache_render(a.passes)
+
+
+if __name__ == "__main__":
+    main()
