@@ -378,7 +378,7 @@ typedef struct {
     uint64_t seed;                  /* initial weights and training-path streams */
     uint32_t bounces;               /* camera paths query the cache after this many bounces, one more
                                      * behind a vertex of roughness < 0.1 (a mirror counts as 0): 1 */
-    uint32_t infer_groups;          /* 128-query tiles each inference CTA keeps in flight: 1, 2 or 4; 0: 2 */
+    uint32_t infer_groups;          /* 128-query tiles each inference CTA keeps in flight: 1, 2 or 4; 0: 4 */
 } pico_nrc_config;
 
 int pico_gpu_nrc_default_config(pico_nrc_config* out);

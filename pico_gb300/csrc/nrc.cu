@@ -97,16 +97,29 @@ struct InferArgs {
 // tiles with its own shared-memory tile, TMEM columns (64 g .. 64 g + 63) and
 // mbarrier, and synchronises on its own named barrier (1 + g), so that one
 // group's encoding (hash-grid gathers) overlaps another's tensor-core layers.
-__device__ __forceinline__ bool group_sync_and(uint32_t id, bool v)
+template <int kId>
+__device__ __forceinline__ bool bar_and(bool v)
 {
     uint32_t r;
     asm volatile(
         "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, 128, p;\n\t"
         "selp.u32 %0, 1, 0, q;\n\t}\n"
         : "=r"(r)
-        : "r"((uint32_t)v), "r"(id)
+        : "r"((uint32_t)v), "n"(kId)
         : "memory");
     return r != 0;
+}
+
+// AND of v over warpgroup g's 128 threads on named barrier 1 + g; the barrier
+// numbers are immediates, so a CTA reserves only the barriers it uses.
+__device__ __forceinline__ bool group_sync_and(uint32_t g, bool v)
+{
+    switch (g) {
+    case 0: return bar_and<1>(v);
+    case 1: return bar_and<2>(v);
+    case 2: return bar_and<3>(v);
+    default: return bar_and<4>(v);
+    }
 }
 
 template <int G>
@@ -164,7 +177,7 @@ __global__ void __launch_bounds__(128 * G) infer_kernel(InferArgs a)
         for (int l = 0; l < kLayers; ++l) {
             fence_async_smem();
             tc_fence_before();
-            if (!group_sync_and(1u + g, ok)) { abort = true; break; }
+            if (!group_sync_and(g, ok)) { abort = true; break; }
             if (gtid == 0) {
                 tc_fence_after();
                 issue_forward(tmem, x_addr, w_addr + (uint32_t)l * kLayerBytes, l);
@@ -495,6 +508,7 @@ static cudaError_t launch_infer_groups(const InferArgs& a, cudaStream_t st)
 {
     static int per_sm = 0;
     if (!per_sm) {
+        // no carveout preference: the hash-grid gathers live on the L1 left beside the shared memory
         cudaError_t e = cudaFuncSetAttribute(infer_kernel<G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              infer_smem(G));
         if (e != cudaSuccess) return e;
@@ -518,8 +532,8 @@ cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint
     const InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev};
     switch (groups) {
     case 1: return launch_infer_groups<1>(a, st);
-    case 4: return launch_infer_groups<4>(a, st);
-    default: return launch_infer_groups<2>(a, st);
+    case 2: return launch_infer_groups<2>(a, st);
+    default: return launch_infer_groups<4>(a, st);
     }
 }
 

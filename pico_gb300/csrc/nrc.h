@@ -34,7 +34,7 @@ cudaError_t launch_encode(const GridGeometry& g, const __half2* table, const flo
 // is the number of 128-row tiles each CTA keeps in flight.
 cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint8_t* weights, const float4* queries,
                          uint32_t n, float* out_rgb, const float4* thr, float4* pay, int* err, cudaStream_t st,
-                         const uint32_t* n_dev = nullptr, int groups = 2);
+                         const uint32_t* n_dev = nullptr, int groups = 4);
 // Gradients of the relative L2 loss over one batch: per-CTA weight-gradient
 // partials (kMlpParams floats each, returned count in *parts) and the hash-grid
 // gradient (accumulated into grid_grad, which the caller zeroes); adds the mean
