@@ -7,13 +7,15 @@
 // layer one).  Weights and activations are bf16, products accumulate in fp32.
 //
 // Both network kernels work on tiles of 128 queries, one per thread of a
-// 4-warp CTA, which is also one TMEM lane: the thread encodes its query into
-// row `tid` of a swizzled shared-memory tile, thread 0 issues the layer's
-// tcgen05.mma (M = 128, N = 64 or 16, K = 64 as four K = 16 steps) with the
-// accumulator in TMEM and commits it to an mbarrier, and every thread reads its
-// row back with tcgen05.ld, applies ReLU and writes the next layer's input tile.
-// The weights (43 KB, bf16, already in the swizzled layout) reach shared memory
-// once per CTA with one bulk copy.
+// warpgroup (4 warps), which is also one TMEM lane: the thread encodes its
+// query into row `tid` of a swizzled shared-memory tile, the group's first
+// thread issues the layer's tcgen05.mma (M = 128, N = 64 or 16, K = 64 as four
+// K = 16 steps) with the accumulator in TMEM and commits it to an mbarrier, and
+// every thread reads its row back with tcgen05.ld, applies ReLU and writes the
+// next layer's input tile.  Inference CTAs hold 1, 2 or 4 such groups on their
+// own tiles and TMEM columns; training CTAs hold one.  The weights (43 KB,
+// bf16, already in the swizzled layout) reach shared memory once per CTA with
+// one bulk copy.
 //
 // Training keeps the six layer inputs of a tile in shared memory.  The loss is
 // relative L2, sum_c (y_c - t_c)^2 / (y_c^2 + 0.01) with the denominator held
