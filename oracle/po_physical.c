@@ -186,6 +186,7 @@ typedef struct {
     uint32_t* base;            /* per light: first triangle record */
     double* geo;               /* per light triangle: world unit normal, area density */
     uint32_t* light_of_inst;   /* instance -> light index or PO_INVALID */
+    double* pick;              /* per slot (lights, then the sun): probability of the next-event pick */
 } phys_scene;
 
 static d3 xform_point(const po_m4* T, d3 p)
@@ -241,6 +242,52 @@ static void phys_prepare(phys_scene* ps, const po_scene* s)
         }
         free(p);
     }
+    /* Next-event pick: the sun keeps a uniform share 1 / nl; triangle lights share
+     * the rest in proportion to their power (sum of the emitted radiance channels
+     * times the world area), implicit lights are never picked. */
+    ps->pick = (double*)calloc(ps->nl ? ps->nl : 1, sizeof(double));
+    double power = 0.0;
+    uint32_t ntri = 0;
+    for (uint32_t l = 0; l < s->nlights; ++l) {
+        const po_instance* in = &s->instances[s->lights[l]];
+        const po_mesh* m = &s->meshes[in->mesh];
+        if (m->desc.shape != PO_SHAPE_TRIANGLES) continue;
+        ++ntri;
+        double area = 0.0;
+        for (uint32_t t = 0; t < m->desc.ntris; ++t) {
+            const uint32_t* ix = m->desc.indices + 3 * t;
+            const d3 a = xform_point(&in->T, d3_of(m->desc.positions + 3 * ix[0]));
+            const d3 b = xform_point(&in->T, d3_of(m->desc.positions + 3 * ix[1]));
+            const d3 c = xform_point(&in->T, d3_of(m->desc.positions + 3 * ix[2]));
+            const d3 cr = d3_cross(d3_sub(b, a), d3_sub(c, a));
+            area += 0.5 * sqrt(d3_dot(cr, cr));
+        }
+        const float* le = s->materials[in->material].emissive;
+        const double pw = ((double)le[0] + (double)le[1] + (double)le[2]) * area;
+        ps->pick[l] = (isfinite(pw) && pw > 0.0) ? pw : 0.0;
+        power += ps->pick[l];
+    }
+    const double sun_share = s->sky.use_sun ? 1.0 / ps->nl : 0.0;
+    for (uint32_t l = 0; l < s->nlights; ++l) {
+        const po_mesh* m = &s->meshes[s->instances[s->lights[l]].mesh];
+        if (m->desc.shape != PO_SHAPE_TRIANGLES) continue;
+        ps->pick[l] = (1.0 - sun_share) * (power > 0.0 ? ps->pick[l] / power : 1.0 / ntri);
+    }
+    if (s->sky.use_sun) ps->pick[s->nlights] = ntri ? sun_share : 1.0;
+}
+
+/* The slot a uniform u picks from the next-event table. */
+static uint32_t pick_light(const phys_scene* ps, double u)
+{
+    double acc = 0.0;
+    uint32_t last = 0;
+    for (uint32_t l = 0; l < ps->nl; ++l) {
+        if (!(ps->pick[l] > 0.0)) continue;
+        last = l;
+        acc += ps->pick[l];
+        if (u < acc) return l;
+    }
+    return last;
 }
 
 static void phys_release(phys_scene* ps)
@@ -248,6 +295,7 @@ static void phys_release(phys_scene* ps)
     free(ps->base);
     free(ps->geo);
     free(ps->light_of_inst);
+    free(ps->pick);
 }
 
 /* ------------------------------------------------------------------ paths */
@@ -277,12 +325,13 @@ static d3 sky_of(const po_scene* s, d3 d)
 }
 
 /* Density with which next-event estimation picks world point y on light triangle
- * record g, seen from distance t along unit direction d (solid angle measure). */
-static double light_pdf(const phys_scene* ps, const double* g, double t, d3 d)
+ * record g of light slot li, seen from distance t along unit direction d (solid
+ * angle measure). */
+static double light_pdf(const phys_scene* ps, uint32_t li, const double* g, double t, d3 d)
 {
     const double cl = fabs(g[0] * d.x + g[1] * d.y + g[2] * d.z);
     if (!(cl > 0.0)) return INFINITY;
-    return g[3] * t * t / (cl * ps->nl);
+    return g[3] * t * t * ps->pick[li] / cl;
 }
 
 /* One path of the physical estimator.  With `cache` (the radiance-cache form,
@@ -319,7 +368,7 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
             if (pdf_prev > 0.0) {
                 if (strategy == PHYS_NEE_ONLY && tri_light) w = 0.0;
                 else if (strategy == PHYS_MIS && tri_light)
-                    w = mis_weight(pdf_prev, light_pdf(ps, ps->geo + 4 * (size_t)(ps->base[li] + f.prim), f.t, d));
+                    w = mis_weight(pdf_prev, light_pdf(ps, li, ps->geo + 4 * (size_t)(ps->base[li] + f.prim), f.t, d));
             }
             rad = d3_add(rad, d3_scale(d3_mul(thr, d3_of(m->emissive)), w));
             break;
@@ -349,8 +398,7 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
             const d3 vl = to_local(&fr, v);
             const lobes lb = lobes_of((int)in->bsdf, m);
             if (ps->nl > 0 && strategy != PHYS_BSDF_ONLY) {
-                uint32_t li = (uint32_t)(rnd(rng) * ps->nl);
-                if (li >= ps->nl) li = ps->nl - 1;
+                const uint32_t li = pick_light(ps, rnd(rng));
                 if (s->sky.use_sun && li == ps->nl - 1) {
                     const d3 wi = d3_norm(d3v(-s->sky.sun_direction[0], -s->sky.sun_direction[1],
                                               -s->sky.sun_direction[2]));
@@ -359,7 +407,7 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
                     if (wl.z > 0.0 && !trace(s, org, ow, wi, &h)) {
                         d3 fv; double pb;
                         eval_local(&lb, vl, wl, &fv, &pb);
-                        rad = d3_add(rad, d3_scale(d3_mul(d3_mul(thr, fv), d3_of(s->sky.sun_colour)), wl.z * ps->nl));
+                        rad = d3_add(rad, d3_scale(d3_mul(d3_mul(thr, fv), d3_of(s->sky.sun_colour)), wl.z / ps->pick[li]));
                     }
                 } else {
                     const po_instance* lin = &s->instances[s->lights[li]];
@@ -381,7 +429,7 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
                         const double dist2 = d3_dot(dd, dd), dist = sqrt(dist2);
                         const d3 wi = d3_scale(dd, 1.0 / dist);
                         const double* g = ps->geo + 4 * (size_t)(ps->base[li] + t);
-                        const double pl = light_pdf(ps, g, dist, wi);
+                        const double pl = light_pdf(ps, li, g, dist, wi);
                         const d3 wl = to_local(&fr, wi);
                         if (wl.z > 0.0 && isfinite(pl) && g[3] > 0.0 && dist > 0.0) {
                             po_fragment h;

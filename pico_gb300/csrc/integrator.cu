@@ -355,7 +355,8 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                         sc.lights[li].shape == PICO_SHAPE_TRIANGLES) {
                         const float4 g = light_geo[sc.lights[li].tri_base + sc.tris[tri].prim];
                         const float cl = fabsf(g.x * dir.x + g.y * dir.y + g.z * dir.z);
-                        const float pl = g.w * hit.x * hit.x / (cl * (float)nl);   // +inf at cl = 0
+                        const float pick = sc.light_pick[nl + li];
+                        const float pl = g.w * hit.x * hit.x * pick / cl;   // +inf at cl = 0
                         w = mis_weight(thr.w, pl);
                     }
                     pay.x += thr.x * m.emissive[0] * w;
@@ -392,10 +393,13 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                         const Frame fr = frame_of(nrm);
                         const float3 vl = to_local(fr, v);
                         const Lobes lb = lobes_of(is.bsdf, m);
-                        // next-event estimation towards one uniformly chosen light (the sun last)
+                        // next-event estimation towards one light (the sun last), picked by the
+                        // scene's power-proportional table
                         if (nl > 0) {
-                            uint32_t li = (uint32_t)(rng.uniform() * (float)nl);
-                            if (li >= nl) li = nl - 1;
+                            const float up = rng.uniform();
+                            uint32_t li = 0;
+                            while (li + 1 < nl && up >= sc.light_pick[li]) ++li;
+                            const float pick = sc.light_pick[nl + li];
                             float3 wi = make_float3(0.0f, 0.0f, 0.0f), c = wi;
                             float reach = 0.0f;
                             if (sc.use_sun && li == nl - 1) {
@@ -405,7 +409,7 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                                     float3 fv;
                                     float pb;
                                     eval(lb, vl, wl, fv, pb);
-                                    const float kk = wl.z * (float)nl;
+                                    const float kk = wl.z / pick;
                                     c = make_float3(thr.x * fv.x * sc.sun_col[0] * kk, thr.y * fv.y * sc.sun_col[1] * kk,
                                                     thr.z * fv.z * sc.sun_col[2] * kk);
                                     reach = __int_as_float(0x7f800000);   // only an escaping ray sees the sun
@@ -436,7 +440,7 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                                 const float cl = fabsf(g.x * wi.x + g.y * wi.y + g.z * wi.z);
                                 const float3 wl = to_local(fr, wi);
                                 if (wl.z > 0.0f && cl > 0.0f && g.w > 0.0f && dist > 0.0f) {
-                                    const float pl = g.w * dist2 / (cl * (float)nl);
+                                    const float pl = g.w * dist2 * pick / cl;
                                     float3 fv;
                                     float pb;
                                     eval(lb, vl, wl, fv, pb);

@@ -110,6 +110,7 @@ struct SceneView {
     const float* light_positions;       // per light triangle: v0, v1, v2 (9 floats)
     const float* light_tri_geo;         // per light triangle: world unit normal, area pdf (4 floats)
     const uint32_t* light_of_inst;      // original instance index -> light index, or ~0u
+    const float* light_pick;            // physical estimator's light pick over nlights + use_sun slots: cdf, then pdf
     uint32_t nlights;
     uint32_t tlas_root_ref;             // the reference's TLAS boxes
     float tlas_lo[3], tlas_hi[3];

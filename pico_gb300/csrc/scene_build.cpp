@@ -471,6 +471,60 @@ static void light_triangle_geometry(const pico_mesh& m, const float* T, const st
     }
 }
 
+// FlatScene::light_pick: cdf then pdf over the lights and, with `sun`, the sun.
+static void light_pick_table(const pico_scene_desc& desc, const std::vector<GpuLight>& lights, bool sun,
+                             std::vector<float>& out)
+{
+    const size_t n = lights.size(), slots = n + (sun ? 1 : 0);
+    std::vector<double> pdf(slots, 0.0), power(n, 0.0);
+    double total = 0.0;
+    size_t ntri = 0;
+    for (size_t k = 0; k < n; ++k) {
+        if (lights[k].shape != PICO_SHAPE_TRIANGLES) continue;
+        ++ntri;
+        const pico_instance& in = desc.instances[lights[k].inst];
+        const pico_mesh& m = desc.meshes[in.mesh];
+        const float* T = in.transform;
+        double area = 0.0;
+        for (uint32_t t = 0; t < m.ntris; ++t) {
+            double e[2][3];
+            const float* a = m.positions + 3 * m.indices[3 * t];
+            for (int j = 0; j < 2; ++j) {
+                const float* q = m.positions + 3 * m.indices[3 * t + 1 + j];
+                for (int r = 0; r < 3; ++r)
+                    e[j][r] = (double)T[0 * 4 + r] * ((double)q[0] - a[0]) +
+                              (double)T[1 * 4 + r] * ((double)q[1] - a[1]) +
+                              (double)T[2 * 4 + r] * ((double)q[2] - a[2]);
+            }
+            const double c[3] = {e[0][1] * e[1][2] - e[0][2] * e[1][1], e[0][2] * e[1][0] - e[0][0] * e[1][2],
+                                 e[0][0] * e[1][1] - e[0][1] * e[1][0]};
+            area += 0.5 * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        }
+        const float* le = desc.materials[in.material].emissive;
+        const double p = ((double)le[0] + (double)le[1] + (double)le[2]) * area;
+        power[k] = (std::isfinite(p) && p > 0.0) ? p : 0.0;
+        total += power[k];
+    }
+    const double sun_share = sun ? 1.0 / (double)slots : 0.0;
+    for (size_t k = 0; k < n; ++k) {
+        if (lights[k].shape != PICO_SHAPE_TRIANGLES) continue;
+        pdf[k] = (1.0 - sun_share) * (total > 0.0 ? power[k] / total : 1.0 / (double)ntri);
+    }
+    if (sun) pdf[n] = ntri ? sun_share : 1.0;
+    out.assign(2 * slots, 0.0f);
+    double acc = 0.0;
+    for (size_t k = 0; k < slots; ++k) {
+        acc += pdf[k];
+        out[k] = (float)acc;
+        out[slots + k] = (float)pdf[k];
+    }
+    // the last slot with a non-zero pdf closes the distribution at exactly 1
+    for (size_t k = slots; k-- > 0;) {
+        out[k] = 1.0f;
+        if (pdf[k] > 0.0) break;
+    }
+}
+
 std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
 {
     if (desc.nmeshes && !desc.meshes) return "meshes is NULL";
@@ -709,6 +763,8 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         fs.lights.push_back(l);
     }
     for (int a = 0; a < 3; ++a) fs.sky[a] = desc.sky_rgb[a];
+    const bool sun = desc.sky && desc.sky->use_sun;
+    light_pick_table(desc, fs.lights, sun, fs.light_pick);
 
     // ---- sky image and sun (Scene::process_globals, Core/Scene.cpp:639-700) -----
     if (const pico_sky* k = desc.sky) {

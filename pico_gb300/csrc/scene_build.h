@@ -26,6 +26,12 @@ struct FlatScene {
     std::vector<float> light_positions;
     std::vector<float> light_tri_geo;     // per light triangle: world unit normal, area pdf (4 floats)
     std::vector<uint32_t> light_of_inst;  // original instance index -> NEE light index, or ~0u
+    // The physical estimator's next-event light pick over the slots lights[0 .. n-1]
+    // and, with use_sun, the sun (slot n): cdf[n + sun] then pdf[n + sun].  The sun
+    // keeps a uniform share 1 / (n + 1); triangle lights share the rest in proportion
+    // to their power (sum of emitted radiance channels x world area), implicit
+    // lights get 0 (the physical estimator reaches them by BSDF sampling only).
+    std::vector<float> light_pick;
     uint32_t tlas_root_ref = PICO_REF_EMPTY;
     float tlas_lo[3] = {0, 0, 0}, tlas_hi[3] = {0, 0, 0};
     uint32_t tlas_fast_root_ref = PICO_REF_EMPTY;   // refitted TLAS for the near-first walk

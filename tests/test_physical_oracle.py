@@ -119,6 +119,33 @@ def test_light_strategies_converge_to_the_same_pixels(oracle):
         assert abs(np.mean(ma - mb)) < 4 * np.sqrt(np.sum(va + vb) / spp) / ma.size
 
 
+def test_power_light_pick_converges_with_bsdf_sampling(oracle):
+    """Lights of very different power (the glossy field's three quads): next-event estimation
+    with the power-proportional pick and BSDF sampling alone agree, and MIS, whose emission
+    weights use the same pick densities, agrees with both.  With the sun (a directional light
+    BSDF sampling cannot reach) MIS still agrees with next-event estimation alone."""
+    rng = np.random.default_rng(8)
+    cam = scenes.glossy_field_camera(32, 24)
+    idx = np.sort(rng.choice(32 * 24, 40, replace=False)).astype(np.uint32)
+    spp = 8192
+    with_sun = scenes.glossy_field()
+    no_sun = scenes.glossy_field()
+    no_sun.sky_image = None
+    pairs = []
+    for scene, strategies in ((no_sun, (0, 1, 2)), (with_sun, (0, 1))):
+        os_ = oracle.scene(scene)
+        out = []
+        for strategy in strategies:
+            seeds = rng.integers(1, 2**63, len(idx), dtype=np.uint64)
+            out.append(os_.phys_render_mean(cam, 4, spp, idx, seeds, strategy=strategy))
+        pairs += [(out[a], out[b]) for a in range(len(out)) for b in range(a + 1, len(out))]
+    for (ma, va), (mb, vb) in pairs:
+        noisy = (va + vb) > 0
+        z = np.abs(ma - mb)[noisy] / np.sqrt((va + vb)[noisy] / spp)
+        assert np.mean(z < 4) >= 0.97, np.sort(z)[-5:]
+        assert abs(np.mean(ma - mb)) < 4 * np.sqrt(np.sum(va + vb) / spp) / ma.size
+
+
 def test_white_furnace(oracle):
     """A Lambert sphere of albedo 0.5 under a uniform sky of radiance 1: every path that
     meets the (convex) sphere scatters once and escapes, so its pixels converge to 0.5.
