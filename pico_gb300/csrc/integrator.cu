@@ -83,15 +83,7 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
                                               int s, bool shadow)
 {
     const uint32_t rank = (s == kTraceOk) ? h.rank : kNoHit;
-    if (shadow && b.senergy[i].w == 2.0f) {
-        // physical estimator: the contribution counts unless something lies nearer than scontrib.w
-        const float4 c = b.scontrib[i];
-        if (s == kTraceOk && (rank == kNoHit || h.t >= c.w)) {
-            float4 p = b.pay[i];
-            p.x += c.x; p.y += c.y; p.z += c.z;
-            b.pay[i] = p;
-        }
-    } else if (shadow) {
+    if (shadow) {
         // a light hit adds (throughput * pdf) * Le * albedo (Integrators.cpp:109-117, 173-176);
         // a sun ray (senergy.w = 1) adds the sun colour when it escapes (Integrators.cpp:60-76)
         const float4 e = b.senergy[i];
@@ -132,11 +124,24 @@ __global__ void __launch_bounds__(128, 7) extend_kernel(SceneView sc, PathBatch 
         const unsigned long long k = base + lane;
         if (k < n) {
             const uint32_t i = q[k];
-            TraceHit h;
-            const int s = trace_closest<false, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
-                                                       shadow ? b.sdir[i] : b.dir[i], h, nullptr);
-            if (s != kTraceOk) atomicOr(err, s);
-            extend_finish(sc, b, i, h, s, shadow);
+            if (shadow && b.senergy[i].w == 2.0f) {
+                // physical estimator: an occlusion query bounded by the light sample's distance
+                const float4 c = b.scontrib[i];
+                bool occluded = true;
+                const int s = trace_occluded<kOrder>(sc, b.sorg[i], b.sdir[i], c.w, occluded);
+                if (s != kTraceOk) atomicOr(err, s);
+                if (s == kTraceOk && !occluded) {
+                    float4 p = b.pay[i];
+                    p.x += c.x; p.y += c.y; p.z += c.z;
+                    b.pay[i] = p;
+                }
+            } else {
+                TraceHit h;
+                const int s = trace_closest<false, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
+                                                           shadow ? b.sdir[i] : b.dir[i], h, nullptr);
+                if (s != kTraceOk) atomicOr(err, s);
+                extend_finish(sc, b, i, h, s, shadow);
+            }
         }
     }
 }

@@ -233,16 +233,19 @@ __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t ra
     return world_distance_at(sc, rank, px, py, pz, o);
 }
 
-template <bool kCount, bool kImplicit>
+// kAnyHit: only hits at a world distance below tmax count, and the walk returns
+// at the first instance whose candidate is one (an occlusion query: a hit is
+// reported exactly when the closest hit lies below tmax).
+template <bool kCount, bool kImplicit, bool kAnyHit = false>
 __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
-                                                TraceCounters* cnt)
+                                                TraceCounters* cnt, float tmax = INFINITY)
 {
     using namespace ex;
     const float kInf = __int_as_float(0x7f800000);
     const float kMaxFinite = __int_as_float(0x7f7fffff);
     uint32_t stack[kTraceStack];
     int sp = 0;
-    best.t = kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
+    best.t = kAnyHit ? tmax : kInf; best.rank = kNoHit; best.tri = kNoHit; best.u = 0.0f; best.v = 0.0f;
     const float wix = __frcp_rn(d.x), wiy = __frcp_rn(d.y), wiz = __frcp_rn(d.z);
     // node tests take the NaN-free form when the ray (world or object space) and the boxes are finite
     const bool wfast = sc.finite_boxes && all_finite(o.x, o.y, o.z, wix, wiy, wiz);
@@ -253,7 +256,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
     // finite float so that one comparison also rejects boxes at +inf.
     float cx = o.x, cy = o.y, cz = o.z, cix = wix, ciy = wiy, ciz = wiz;
     bool cfast = wfast;
-    float limit = kMaxFinite;
+    float limit = kAnyHit ? fminf(tmax, kMaxFinite) : kMaxFinite;
     float qdx = 0.0f, qdy = 0.0f, qdz = 0.0f;   // object-space direction of the instance being searched
     float gl = kInf, lt = kInf, lu = 0.0f, lv = 0.0f;
     uint32_t ltri = kNoHit, cur = 0;
@@ -316,8 +319,9 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             // leave the instance: its candidate is the closest triangle by object-space t
             if (ltri != kNoHit) {
                 const float tw = world_distance(sc, cur, ltri, lu, lv, o);
-                if (tw < best.t || (tw == best.t && cur < best.rank)) {
+                if (kAnyHit ? tw < best.t : (tw < best.t || (tw == best.t && cur < best.rank))) {
                     best.t = tw; best.rank = cur; best.tri = ltri; best.u = lu; best.v = lv;
+                    if (kAnyHit) return kTraceOk;
                 }
             }
             in_blas = false;
@@ -359,8 +363,9 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             // an implicit shape: one candidate, no BLAS and no root box test
             float tw, t;
             if (implicit_candidate(sc.insts + rank, o, d, tw, t) &&
-                (tw < best.t || (tw == best.t && rank < best.rank))) {
+                (kAnyHit ? tw < best.t : (tw < best.t || (tw == best.t && rank < best.rank)))) {
                 best.t = tw; best.rank = rank; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
+                if (kAnyHit) return kTraceOk;
                 limit = fminf(best.t, kMaxFinite);
             }
             ref = sp ? stack[--sp] : PICO_REF_DONE;
@@ -520,6 +525,27 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
     constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
     if ((kVariant & kReferenceOrder) != 0) return trace_reference_order<kCount, kImplicit>(sc, o, d, best, cnt);
     return trace_near_first<kCount, kImplicit>(sc, o, d, best, cnt);
+}
+
+// Whether anything lies at a world distance below tmax along the ray (closest-hit
+// semantics: exactly when the closest hit is nearer than tmax).  The near-first
+// walk bounds its search by tmax and stops at the first such instance; the
+// reference order runs the closest hit.
+template <int kVariant>
+__device__ __forceinline__ int trace_occluded(const SceneView& sc, const float4 o, const float4 d, float tmax,
+                                              bool& occluded)
+{
+    constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
+    TraceHit h;
+    int s;
+    if ((kVariant & kReferenceOrder) != 0) {
+        s = trace_reference_order<false, kImplicit>(sc, o, d, h, nullptr);
+        occluded = h.rank != kNoHit && h.t < tmax;
+    } else {
+        s = trace_near_first<false, kImplicit, true>(sc, o, d, h, nullptr, tmax);
+        occluded = h.rank != kNoHit;
+    }
+    return s;
 }
 
 // Calls f(std::integral_constant<int, V>) for the kernel variant V of (order, scene).
