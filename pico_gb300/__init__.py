@@ -99,7 +99,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         return _lib
     p = Path(path) if path else LIB_PATH
     if not p.exists():
-        raise RuntimeError(f"{p} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`")
+        raise RuntimeError(f"{p} is missing: build it with `python -m pico_gb300.build`")
     lib = C.CDLL(str(p))
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(lib, name)
