@@ -305,8 +305,9 @@ typedef struct {
 typedef struct {
     uint32_t wavefront;             /* paths per batch of one render; 0: 2^20 */
     uint32_t extend_ctas_per_sm;    /* persistent CTAs per SM of each closest-hit launch; 0: as many as fit */
-    uint32_t branches;              /* graph branches the renders are spread over; 0: one per render */
-    uint32_t reserved;
+    uint32_t branches;              /* graph branches the pieces are spread over; 0: one per piece */
+    uint32_t piece_paths;           /* a render of more paths (pixels x samples) than this is split into
+                                     * pieces of disjoint pixel ranges, each its own branch work; 0: none */
 } pico_launch_params;
 
 typedef struct {
@@ -324,7 +325,8 @@ int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* 
 /* Chooses launch parameters for a set of renders by timing short renders of the
  * same items (trial_samples samples per pixel into scratch buffers; the items'
  * buffers are not touched): the wavefront size, then the closest-hit CTAs per SM,
- * then the number of branches, each by the highest samples per second.
+ * then the piece size (relative to the items' total paths), then the number of
+ * branches, each by the highest samples per second.
  * trials_out / trial_msamples_per_s (may be NULL) receive up to max_trials tried
  * settings and their millions of samples per second; *ntrials the count. */
 int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, uint32_t trial_samples,

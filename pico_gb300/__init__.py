@@ -9,6 +9,13 @@ thin Python handles mirroring the reference's entry points:
     GpuScene.render(camera, params)  Scene::render_scene_to_memory
     Context.atrous(...)              Util::atrous_denoise
 
+and the additions without a reference counterpart:
+
+    RadianceCache(ctx, ...)          neural radiance cache (encode / infer / train, attach
+                                     for GpuScene.render(..., estimator=2))
+    Context.render_many(renders)     many renders in one CUDA graph launch
+    Context.autotune_batch(renders)  launch parameters for render_many
+
 There is no CPU fallback: if the library is missing, loading fails loudly.
 """
 from __future__ import annotations
@@ -176,11 +183,12 @@ class Context:
             it.variance_rgb = _f32(r["variance"])
         return arr
 
-    def render_many(self, renders, wavefront: int = 0, extend_ctas_per_sm: int = 0, branches: int = 0):
+    def render_many(self, renders, wavefront: int = 0, extend_ctas_per_sm: int = 0, branches: int = 0,
+                    piece_paths: int = 0):
         """pico_gpu_render_many: all renders in one CUDA graph launch; their buffers are updated in place.
         Returns (per-render completion times in ms, report dict)."""
         arr = self._items(renders)
-        params = CLaunchParams(wavefront, extend_ctas_per_sm, branches, 0)
+        params = CLaunchParams(wavefront, extend_ctas_per_sm, branches, piece_paths)
         done = (C.c_double * max(len(renders), 1))()
         rep = CBatchReport()
         self.check(self.lib.pico_gpu_render_many(self.handle, len(renders), arr, C.byref(params), done,
@@ -199,7 +207,8 @@ class Context:
                                                     trials, rates, 16, C.byref(nt)), "autotune_batch")
 
         def as_dict(p):
-            return {"wavefront": p.wavefront, "extend_ctas_per_sm": p.extend_ctas_per_sm, "branches": p.branches}
+            return {"wavefront": p.wavefront, "extend_ctas_per_sm": p.extend_ctas_per_sm, "branches": p.branches,
+                    "piece_paths": p.piece_paths}
         return as_dict(best), [(as_dict(trials[i]), rates[i]) for i in range(nt.value)]
 
     def atrous(self, pixels, normals, positions, diffuse, width: int, height: int) -> np.ndarray:

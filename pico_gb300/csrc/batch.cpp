@@ -1,14 +1,19 @@
 // Batched rendering (pico_gpu_render_many) and its autotuner: no counterpart in
 // the reference, which renders one scene at a time.
 //
-// Every render gets a slot of its own (path state, image buffers, device status
-// block) and its batches are captured, without host synchronisation, on one of
-// `branches` streams forked from the context's stream; the captured graph
-// (one branch per stream, renders on a branch in sequence) is instantiated and
-// launched once.  Small renders cannot fill 152 SMs on their own; side by side
-// their persistent closest-hit grids and shade kernels share the GPU.  A 1-thread
-// kernel at the graph's start and at the end of each render stores the device's
-// nanosecond timer, from which the per-render completion times are read.
+// Every render gets an image slot (its progressive buffers and active-pixel
+// list).  Its active pixels are split into pieces of disjoint pixel ranges
+// (one piece unless the render has more than piece_paths paths), and every
+// piece gets a path slot of its own (path state of at most `wavefront` paths,
+// device status block).  Each piece's batches are captured, without host
+// synchronisation, on one of `branches` streams forked from the context's
+// stream; the captured graph is instantiated and launched once.  Small renders
+// cannot fill 152 SMs on their own, and one large render would otherwise run
+// alone at the end: side by side their persistent closest-hit grids and shade
+// kernels share the GPU.  Pieces of one render write disjoint pixels of the
+// same buffers.  A 1-thread kernel at the graph's start and at the end of each
+// piece stores the device's nanosecond timer, from which the per-render
+// completion times (the last of its pieces) are read.
 #include "render_internal.h"
 
 #include <algorithm>
@@ -28,13 +33,15 @@ struct BatchSlot {
 };
 
 struct BatchState {
-    std::vector<std::unique_ptr<BatchSlot>> slots;
+    std::vector<std::unique_ptr<BatchSlot>> images;   // per render: progressive buffers, pixel list
+    std::vector<std::unique_ptr<BatchSlot>> pieces;   // per piece: path state and status
     std::vector<cudaStream_t> streams;
-    unsigned long long* stamps = nullptr;   // [0] graph start, [1 + r] end of render r
+    unsigned long long* stamps = nullptr;              // [0] graph start, [1 + j] end of piece j
     size_t stamp_cap = 0;
     ~BatchState()
     {
-        slots.clear();
+        images.clear();
+        pieces.clear();
         for (cudaStream_t s : streams) cudaStreamDestroy(s);
         if (stamps) cudaFree(stamps);
     }
@@ -51,28 +58,33 @@ void free_batch_state(pico_gpu_ctx* ctx)
 namespace {
 
 struct Params {
-    uint32_t wavefront, extend_ctas, branches;
+    uint32_t wavefront, extend_ctas, branches, piece_paths;
 };
 
 // Host-side state of one render between its upload and its download.
 struct Prepared {
     uint32_t W = 0, H = 0;
-    size_t npx = 0;
-    size_t nactive = 0;
+    size_t npx = 0, nactive = 0;
     uint64_t samples_before = 0;
-    uint32_t chunk_pix = 0, spb_max = 0;
     CameraView cam{};
 };
 
-Params resolve(const pico_launch_params* lp, uint32_t n)
+// A pixel range [p0, p1) of a render's active pixels, rendered on its own.
+struct Piece {
+    uint32_t render;
+    size_t p0, p1;
+    uint32_t chunk_pix, spb_max;
+};
+
+Params resolve(const pico_launch_params* lp)
 {
-    Params p{1u << 20, 0u, n};
+    Params p{1u << 20, 0u, 0u, 0u};
     if (lp) {
         if (lp->wavefront) p.wavefront = std::min<uint32_t>(std::max<uint32_t>(lp->wavefront, 1u << 12), kMaxPaths);
         p.extend_ctas = lp->extend_ctas_per_sm;
-        if (lp->branches) p.branches = std::min(lp->branches, n);
+        p.branches = lp->branches;
+        p.piece_paths = lp->piece_paths;
     }
-    if (p.branches == 0) p.branches = 1;
     return p;
 }
 
@@ -82,57 +94,57 @@ int validate(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items)
     for (uint32_t r = 0; r < n; ++r) {
         const pico_render_item& it = items[r];
         const pico_render_config& c = it.config;
+        const std::string who = "render " + std::to_string(r) + ": ";
         if (!it.scene || !it.pixels_rgb || !it.sample_count || !it.variance_rgb)
-            return set_error(ctx, PICO_ERR_INVALID_ARG, "render " + std::to_string(r) + ": null argument");
+            return set_error(ctx, PICO_ERR_INVALID_ARG, who + "null argument");
         if (it.camera.resolution[0] == 0 || it.camera.resolution[1] == 0 || c.width != it.camera.resolution[0] ||
             c.height != it.camera.resolution[1])
-            return set_error(ctx, PICO_ERR_INVALID_ARG, "render " + std::to_string(r) + ": bad image size");
+            return set_error(ctx, PICO_ERR_INVALID_ARG, who + "bad image size");
         if (c.estimator != PICO_ESTIMATOR_REFERENCE && c.estimator != PICO_ESTIMATOR_PHYSICAL)
-            return set_error(ctx, PICO_ERR_INVALID_ARG,
-                             "render " + std::to_string(r) + ": batches take the reference or physical estimator");
+            return set_error(ctx, PICO_ERR_INVALID_ARG, who + "batches take the reference or physical estimator");
         if (c.estimator == PICO_ESTIMATOR_PHYSICAL && it.scene->has_btdf)
-            return set_error(ctx, PICO_ERR_UNSUPPORTED,
-                             "render " + std::to_string(r) + ": the physical estimator has no Transparent or Fresnel lobes");
-        if (c.denoise || c.tonemap)
-            return set_error(ctx, PICO_ERR_INVALID_ARG,
-                             "render " + std::to_string(r) + ": batches do not denoise or tone map");
-        if (it.scene->ctx != ctx)
-            return set_error(ctx, PICO_ERR_INVALID_ARG, "render " + std::to_string(r) + ": scene of another context");
+            return set_error(ctx, PICO_ERR_UNSUPPORTED, who + "the physical estimator has no Transparent or Fresnel lobes");
+        if (c.denoise || c.tonemap) return set_error(ctx, PICO_ERR_INVALID_ARG, who + "batches do not denoise or tone map");
+        if (it.scene->ctx != ctx) return set_error(ctx, PICO_ERR_INVALID_ARG, who + "scene of another context");
     }
     return PICO_OK;
 }
 
-cudaError_t ensure_state(pico_gpu_ctx* ctx, uint32_t n, uint32_t branches)
+cudaError_t grow(std::vector<std::unique_ptr<BatchSlot>>& slots, size_t n)
 {
-    if (!ctx->batch) ctx->batch = new BatchState();
-    BatchState& bs = *ctx->batch;
-    while (bs.slots.size() < n) {
+    while (slots.size() < n) {
         auto s = std::make_unique<BatchSlot>();
         cudaError_t e = cudaMalloc(&s->status, sizeof(DeviceStatus));
-        if (e == cudaSuccess) e = cudaMemset(s->status, 0, sizeof(DeviceStatus));
         if (e != cudaSuccess) return e;
-        bs.slots.push_back(std::move(s));
-    }
-    while (bs.streams.size() < branches) {
-        cudaStream_t s = nullptr;
-        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
-        if (e != cudaSuccess) return e;
-        bs.streams.push_back(s);
-    }
-    if (bs.stamp_cap < (size_t)n + 1) {
-        if (bs.stamps) cudaFree(bs.stamps);
-        bs.stamps = nullptr;
-        bs.stamp_cap = 0;
-        cudaError_t e = cudaMalloc(&bs.stamps, ((size_t)n + 1) * sizeof(unsigned long long));
-        if (e != cudaSuccess) return e;
-        bs.stamp_cap = (size_t)n + 1;
+        slots.push_back(std::move(s));
     }
     return cudaSuccess;
 }
 
-// Uploads one render's progressive buffers and active-pixel list and reserves its path state.
-cudaError_t prepare(const pico_render_item& it, BatchSlot& s, const Params& p, Prepared& pr, cudaStream_t st,
-                    std::vector<uint32_t>& active, std::vector<uint32_t>& done)
+cudaError_t ensure_state(pico_gpu_ctx* ctx, uint32_t nrenders, size_t npieces, uint32_t branches)
+{
+    if (!ctx->batch) ctx->batch = new BatchState();
+    BatchState& bs = *ctx->batch;
+    cudaError_t e = grow(bs.images, nrenders);
+    if (e == cudaSuccess) e = grow(bs.pieces, npieces);
+    while (e == cudaSuccess && bs.streams.size() < branches) {
+        cudaStream_t s = nullptr;
+        e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) bs.streams.push_back(s);
+    }
+    if (e == cudaSuccess && bs.stamp_cap < npieces + 1) {
+        if (bs.stamps) cudaFree(bs.stamps);
+        bs.stamps = nullptr;
+        bs.stamp_cap = 0;
+        e = cudaMalloc(&bs.stamps, (npieces + 1) * sizeof(unsigned long long));
+        if (e == cudaSuccess) bs.stamp_cap = npieces + 1;
+    }
+    return e;
+}
+
+// Uploads one render's progressive buffers and active-pixel list into its image slot.
+cudaError_t upload_render(const pico_render_item& it, BatchSlot& s, Prepared& pr, cudaStream_t st,
+                          std::vector<uint32_t>& active, std::vector<uint32_t>& done)
 {
     const pico_render_config& cfg = it.config;
     RenderBuffers& r = s.r;
@@ -153,9 +165,6 @@ cudaError_t prepare(const pico_render_item& it, BatchSlot& s, const Params& p, P
     if (e == cudaSuccess) e = r.variance.reserve(pr.npx * 3 * sizeof(float));
     for (DeviceBuffer* b : {&r.count, &r.taken, &r.done, &r.pix_list})
         if (e == cudaSuccess) e = b->reserve(pr.npx * sizeof(uint32_t));
-    pr.chunk_pix = (uint32_t)std::min<size_t>(std::max<size_t>(pr.nactive, 1), p.wavefront);
-    pr.spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(std::max(cfg.max_samples, 1u), p.wavefront / pr.chunk_pix));
-    if (e == cudaSuccess && pr.nactive && cfg.max_samples) e = reserve_paths(r, (size_t)pr.chunk_pix * pr.spb_max);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.pixels.ptr, it.pixels_rgb, pr.npx * 3 * sizeof(float),
                                               cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.variance.ptr, it.variance_rgb, pr.npx * 3 * sizeof(float),
@@ -167,45 +176,84 @@ cudaError_t prepare(const pico_render_item& it, BatchSlot& s, const Params& p, P
     if (e == cudaSuccess) e = cudaMemsetAsync(r.taken.ptr, 0, pr.npx * sizeof(uint32_t), st);
     if (e == cudaSuccess && pr.nactive)
         e = cudaMemcpyAsync(r.pix_list.ptr, active.data(), pr.nactive * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s.status, 0, sizeof(DeviceStatus), st);
     // the pageable sources above must stay alive until the copies finish
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     return e;
 }
 
-// The render's batches on stream st, without synchronisation (they are captured).
-cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& s, const Params& p,
-                    const Prepared& pr, cudaStream_t st)
+// Splits every render's active pixels into pieces of at most piece_paths paths.
+std::vector<Piece> make_pieces(uint32_t n, const pico_render_item* items, const std::vector<Prepared>& prep,
+                               const Params& p)
+{
+    std::vector<Piece> pieces;
+    for (uint32_t r = 0; r < n; ++r) {
+        const uint32_t spp = items[r].config.max_samples;
+        const size_t na = prep[r].nactive;
+        if (!na || !spp) continue;
+        size_t k = 1;
+        if (p.piece_paths) k = std::min<size_t>(na, (na * spp + p.piece_paths - 1) / p.piece_paths);
+        for (size_t j = 0; j < k; ++j) {
+            Piece pc{r, na * j / k, na * (j + 1) / k, 0, 0};
+            const size_t range = pc.p1 - pc.p0;
+            pc.chunk_pix = (uint32_t)std::min<size_t>(range, p.wavefront);
+            pc.spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(spp, p.wavefront / pc.chunk_pix));
+            pieces.push_back(pc);
+        }
+    }
+    return pieces;
+}
+
+// A piece's batches on stream st, without synchronisation (they are captured):
+// path state from the piece's slot, pixels and progressive buffers from the render's.
+cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& image, BatchSlot& path,
+                    const Params& p, const Prepared& pr, const Piece& pc, cudaStream_t st)
 {
     const pico_render_config& cfg = it.config;
     const int order = scene_order(ctx, it.scene);
     cudaError_t e = cudaSuccess;
-    if (!pr.nactive || !cfg.max_samples) return e;
-    for (size_t p0 = 0; p0 < pr.nactive && e == cudaSuccess; p0 += pr.chunk_pix) {
-        const uint32_t npix = (uint32_t)std::min<size_t>(pr.chunk_pix, pr.nactive - p0);
-        for (uint32_t s0 = 0; s0 < cfg.max_samples && e == cudaSuccess; s0 += pr.spb_max) {
-            const uint32_t spb = std::min(pr.spb_max, cfg.max_samples - s0);
-            PathBatch b = make_batch(s.r, npix * spb, npix, pr.W, as<uint32_t>(s.r.pix_list) + p0);
+    for (size_t q0 = pc.p0; q0 < pc.p1 && e == cudaSuccess; q0 += pc.chunk_pix) {
+        const uint32_t npix = (uint32_t)std::min<size_t>(pc.chunk_pix, pc.p1 - q0);
+        for (uint32_t s0 = 0; s0 < cfg.max_samples && e == cudaSuccess; s0 += pc.spb_max) {
+            const uint32_t spb = std::min(pc.spb_max, cfg.max_samples - s0);
+            PathBatch b = make_batch(path.r, npix * spb, npix, pr.W, as<uint32_t>(image.r.pix_list) + q0);
+            b.pixels = as<float>(image.r.pixels);
+            b.variance = as<float>(image.r.variance);
+            b.count = as<uint32_t>(image.r.count);
+            b.taken = as<uint32_t>(image.r.taken);
+            b.done = as<uint32_t>(image.r.done);
             b.extend_ctas = p.extend_ctas;
             e = launch_render_batch(it.scene->view, b, pr.cam, cfg.seed, spb, cfg.max_ray_depth, cfg.max_samples,
-                                    cfg.max_variance, (int)cfg.estimator, s.status, order, st);
+                                    cfg.max_variance, (int)cfg.estimator, path.status, order, st);
         }
     }
     return e;
 }
 
-int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, const Params& p, double* completion_ms,
-              pico_batch_report* rep)
+int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, const Params& params,
+              double* completion_ms, pico_batch_report* rep)
 {
     using clock = std::chrono::steady_clock;
     cudaStream_t st = ctx->stream;
-    cudaError_t e = ensure_state(ctx, n, p.branches);
+    cudaError_t e = ensure_state(ctx, n, 0, 1);
     if (e != cudaSuccess) return cuda_error(ctx, e, "batch state");
-    BatchState& bs = *ctx->batch;
     std::vector<Prepared> prep(n);
     std::vector<uint32_t> active, done;
-    for (uint32_t r = 0; r < n && e == cudaSuccess; ++r) e = prepare(items[r], *bs.slots[r], p, prep[r], st, active, done);
+    for (uint32_t r = 0; r < n && e == cudaSuccess; ++r)
+        e = upload_render(items[r], *ctx->batch->images[r], prep[r], st, active, done);
     if (e != cudaSuccess) return cuda_error(ctx, e, "batch upload");
+    const std::vector<Piece> pieces = make_pieces(n, items, prep, params);
+    const size_t np = pieces.size();
+    Params p = params;
+    p.branches = (uint32_t)std::max<size_t>(1, std::min<size_t>(p.branches ? p.branches : np, std::max<size_t>(np, 1)));
+    e = ensure_state(ctx, n, np, p.branches);
+    BatchState& bs = *ctx->batch;
+    for (size_t j = 0; j < np && e == cudaSuccess; ++j) {
+        BatchSlot& ps = *bs.pieces[j];
+        e = reserve_paths(ps.r, (size_t)pieces[j].chunk_pix * pieces[j].spb_max);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ps.status, 0, sizeof(DeviceStatus), st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "batch path state");
 
     const auto t_build = clock::now();
     std::vector<cudaEvent_t> events(1 + p.branches, nullptr);
@@ -228,10 +276,11 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     cudaError_t ce = launch_stamp(bs.stamps, st);
     if (ce == cudaSuccess) ce = cudaEventRecord(events[0], st);
     for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(bs.streams[k], events[0], 0);
-    for (uint32_t r = 0; r < n && ce == cudaSuccess; ++r) {
-        cudaStream_t bst = bs.streams[r % p.branches];
-        ce = enqueue(ctx, items[r], *bs.slots[r], p, prep[r], bst);
-        if (ce == cudaSuccess) ce = launch_stamp(bs.stamps + 1 + r, bst);
+    for (size_t j = 0; j < np && ce == cudaSuccess; ++j) {
+        const Piece& pc = pieces[j];
+        cudaStream_t bst = bs.streams[j % p.branches];
+        ce = enqueue(ctx, items[pc.render], *bs.images[pc.render], *bs.pieces[j], p, prep[pc.render], pc, bst);
+        if (ce == cudaSuccess) ce = launch_stamp(bs.stamps + 1 + j, bst);
     }
     for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k) {
         ce = cudaEventRecord(events[1 + k], bs.streams[k]);
@@ -253,31 +302,39 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     cleanup();
     if (e != cudaSuccess) return cuda_error(ctx, e, "batch launch");
 
-    std::vector<unsigned long long> stamps((size_t)n + 1);
+    std::vector<unsigned long long> stamps(np + 1);
     e = cudaMemcpy(stamps.data(), bs.stamps, stamps.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    std::vector<DeviceStatus> status(np);
+    for (size_t j = 0; j < np && e == cudaSuccess; ++j)
+        e = cudaMemcpy(&status[j], bs.pieces[j]->status, sizeof(DeviceStatus), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "batch status");
     uint64_t samples = 0, rays = 0;
-    int status = PICO_OK;
+    int result = PICO_OK;
+    if (completion_ms)
+        for (uint32_t r = 0; r < n; ++r) completion_ms[r] = 0.0;
+    for (size_t j = 0; j < np; ++j) {
+        const DeviceStatus& ds = status[j];
+        rays += ds.rays[0] + ds.rays[1] + ds.rays[2];
+        const uint32_t r = pieces[j].render;
+        if (ds.trace_error && result == PICO_OK)
+            result = set_error(ctx, (ds.trace_error & kTraceStackOverflow) ? PICO_ERR_STACK_OVERFLOW : PICO_ERR_TIMEOUT,
+                               "render " + std::to_string(r) + ": a traversal failed");
+        if (completion_ms) completion_ms[r] = std::max(completion_ms[r], (double)(stamps[1 + j] - stamps[0]) * 1e-6);
+    }
     for (uint32_t r = 0; r < n && e == cudaSuccess; ++r) {
         const pico_render_item& it = items[r];
-        BatchSlot& s = *bs.slots[r];
+        BatchSlot& s = *bs.images[r];
         const Prepared& pr = prep[r];
         e = cudaMemcpyAsync(it.pixels_rgb, s.r.pixels.ptr, pr.npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(it.variance_rgb, s.r.variance.ptr, pr.npx * 3 * sizeof(float),
                                                   cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(it.sample_count, s.r.count.ptr, pr.npx * sizeof(uint32_t),
                                                   cudaMemcpyDeviceToHost, st);
-        DeviceStatus ds{};
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&ds, s.status, sizeof ds, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) break;
         uint64_t after = 0;
         for (size_t px = 0; px < pr.npx; ++px) after += it.sample_count[px];
         samples += after - pr.samples_before;
-        rays += ds.rays[0] + ds.rays[1] + ds.rays[2];
-        if (ds.trace_error && status == PICO_OK)
-            status = set_error(ctx, (ds.trace_error & kTraceStackOverflow) ? PICO_ERR_STACK_OVERFLOW : PICO_ERR_TIMEOUT,
-                               "render " + std::to_string(r) + ": a traversal failed");
-        if (completion_ms) completion_ms[r] = (double)(stamps[1 + r] - stamps[0]) * 1e-6;
     }
     if (e != cudaSuccess) return cuda_error(ctx, e, "batch download");
     if (rep) {
@@ -287,7 +344,7 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
         rep->samples = samples;
         rep->rays = rays;
     }
-    return status;
+    return result;
 }
 
 }  // namespace
@@ -302,7 +359,7 @@ int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* 
     if (report) *report = pico_batch_report{};
     if (n == 0) return PICO_OK;
     cudaSetDevice(ctx->device);
-    return run_batch(ctx, n, items, resolve(params, n), completion_ms, report);
+    return run_batch(ctx, n, items, resolve(params), completion_ms, report);
 }
 
 int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, uint32_t trial_samples,
@@ -317,9 +374,16 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
     if (n == 0) return PICO_OK;
     cudaSetDevice(ctx->device);
     // short renders of the same items into scratch buffers
+    const uint32_t tspp = std::max(1u, trial_samples);
     std::vector<pico_render_item> trial(items, items + n);
     std::vector<std::vector<float>> px(n), var(n);
     std::vector<std::vector<uint32_t>> cnt(n);
+    uint64_t paths_trial = 0, paths_real = 0;
+    for (uint32_t r = 0; r < n; ++r) {
+        const uint64_t npx = (uint64_t)items[r].config.width * items[r].config.height;
+        paths_trial += npx * tspp;
+        paths_real += npx * items[r].config.max_samples;
+    }
     auto reset = [&]() {
         for (uint32_t r = 0; r < n; ++r) {
             const size_t npx = (size_t)items[r].config.width * items[r].config.height;
@@ -329,48 +393,66 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
             trial[r].pixels_rgb = px[r].data();
             trial[r].variance_rgb = var[r].data();
             trial[r].sample_count = cnt[r].data();
-            trial[r].config.max_samples = std::max(1u, trial_samples);
+            trial[r].config.max_samples = tspp;
         }
     };
+    // the piece size is tuned as a fraction of all paths (1 / pieces_per_total) and
+    // scaled from the trial renders' paths to the items' own
+    struct Setting {
+        Params p;
+        uint32_t pieces_per_total;   // 0: no split
+    };
+    auto piece_paths = [](uint64_t total, uint32_t per) -> uint32_t {
+        if (!per) return 0u;
+        return (uint32_t)std::min<uint64_t>(0xffffffffull, std::max<uint64_t>(1, total / per));
+    };
     uint32_t count = 0;
-    auto measure = [&](const Params& p, double& msps) -> int {
+    auto measure = [&](const Setting& s, double& msps) -> int {
         reset();
+        Params p = s.p;
+        p.piece_paths = piece_paths(paths_trial, s.pieces_per_total);
         pico_batch_report rep{};
-        const int s = run_batch(ctx, n, trial.data(), p, nullptr, &rep);
-        if (s != PICO_OK) return s;
+        const int st = run_batch(ctx, n, trial.data(), p, nullptr, &rep);
+        if (st != PICO_OK) return st;
         msps = rep.run_ms > 0.0 ? (double)rep.samples / rep.run_ms / 1e3 : 0.0;
         if (count < max_trials) {
-            if (trials_out) trials_out[count] = pico_launch_params{p.wavefront, p.extend_ctas, p.branches, 0};
+            if (trials_out)
+                trials_out[count] = pico_launch_params{p.wavefront, p.extend_ctas, p.branches,
+                                                       piece_paths(paths_real, s.pieces_per_total)};
             if (trial_msamples_per_s) trial_msamples_per_s[count] = msps;
         }
         ++count;
         return PICO_OK;
     };
-    Params cur{1u << 20, 0u, n};
+    Setting cur{Params{1u << 20, 0u, 0u, 0u}, 0u};
     double rate = 0.0;
     status = measure(cur, rate);   // warm-up: module loading, buffer growth
     if (status != PICO_OK) return status;
     count = 0;
     double best_rate = 0.0;
     auto try_axis = [&](auto&& set, std::initializer_list<uint32_t> values) -> int {
-        Params keep = cur;
+        Setting keep = cur;
         for (uint32_t v : values) {
-            Params p = cur;
-            set(p, v);
+            Setting s = cur;
+            set(s, v);
             double m = 0.0;
-            const int s = measure(p, m);
-            if (s != PICO_OK) return s;
-            if (m > best_rate) { best_rate = m; keep = p; }
+            const int st = measure(s, m);
+            if (st != PICO_OK) return st;
+            if (m > best_rate) {
+                best_rate = m;
+                keep = s;
+            }
         }
         cur = keep;
         return PICO_OK;
     };
-    status = try_axis([](Params& p, uint32_t v) { p.wavefront = v; }, {1u << 18, 1u << 20, 1u << 22});
-    if (status == PICO_OK) status = try_axis([](Params& p, uint32_t v) { p.extend_ctas = v; }, {2u, 4u, 0u});
-    if (status == PICO_OK)
-        status = try_axis([n](Params& p, uint32_t v) { p.branches = std::min(v ? v : n, n); }, {8u, 16u, 0u});
+    status = try_axis([](Setting& s, uint32_t v) { s.p.wavefront = v; }, {1u << 18, 1u << 20, 1u << 22});
+    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.extend_ctas = v; }, {2u, 4u, 0u});
+    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.pieces_per_total = v; }, {0u, 32u, 128u});
+    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.branches = v; }, {8u, 16u, 0u});
     if (status != PICO_OK) return status;
-    *best = pico_launch_params{cur.wavefront, cur.extend_ctas, cur.branches, 0};
+    *best = pico_launch_params{cur.p.wavefront, cur.p.extend_ctas, cur.p.branches,
+                               piece_paths(paths_real, cur.pieces_per_total)};
     if (ntrials) *ntrials = std::min(count, max_trials);
     return PICO_OK;
 }
