@@ -123,6 +123,34 @@ def test_adam_step_matches_oracle(cache):
     assert cache.info()["steps"] == 1
 
 
+def test_invalid_configurations_and_arguments(ctx):
+    from pico_gb300 import PicoError
+    from pico_gb300.types import ESTIMATOR_RADIANCE_CACHE
+    from pico_gb300 import scenes
+    bad = [dict(log2_table_size=9), dict(log2_table_size=23), dict(base_resolution=0.5),
+           dict(base_resolution=64.0, max_resolution=32.0), dict(learning_rate=0.0), dict(beta1=1.0),
+           dict(train_batch=0), dict(train_batch=(1 << 20) + 1), dict(bounces=0), dict(infer_groups=3)]
+    for cfg in bad:
+        with pytest.raises(PicoError) as e:
+            RadianceCache(ctx, **cfg)
+        assert e.value.status == -1, cfg
+    # a render through the cache without one attached is refused before any work
+    gs = ctx.upload(scenes.cornell_box())
+    ctx.lib.pico_gpu_set_radiance_cache(ctx.handle, None)
+    with pytest.raises(PicoError) as e:
+        gs.render(scenes.cornell_camera(8, 8), 5, 1, estimator=ESTIMATOR_RADIANCE_CACHE)
+    assert e.value.status == -1
+    gs.free()
+    # a training batch over 2^20 records is refused
+    c = RadianceCache(ctx, log2_table_size=12)
+    big = np.zeros((1 << 20) + 1, po_nrc.QUERY_DTYPE)
+    with pytest.raises(PicoError) as e:
+        c.train(big, np.zeros((len(big), 3), np.float32))
+    assert e.value.status == -1 and c.info()["steps"] == 0
+    assert c.infer(big[:0]).shape == (0, 3)     # an empty query batch is fine
+    c.free()
+
+
 def test_training_fits_a_smooth_target(ctx):
     c = RadianceCache(ctx, log2_table_size=16, aabb_min=LO, aabb_max=HI, seed=9)
     try:
