@@ -308,6 +308,8 @@ typedef struct {
     uint32_t branches;              /* graph branches the pieces are spread over; 0: one per piece */
     uint32_t piece_paths;           /* a render of more paths (pixels x samples) than this is split into
                                      * pieces of disjoint pixel ranges, each its own branch work; 0: none */
+    uint32_t extend_threads;        /* threads per CTA of each closest-hit launch: 64, 128 or 256; 0: 128 */
+    uint32_t reserved;
 } pico_launch_params;
 
 typedef struct {
@@ -324,9 +326,10 @@ int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* 
                          const pico_launch_params* params, double* completion_ms, pico_batch_report* report);
 /* Chooses launch parameters for a set of renders by timing short renders of the
  * same items (trial_samples samples per pixel into scratch buffers; the items'
- * buffers are not touched): the wavefront size, then the closest-hit CTAs per SM,
- * then the piece size (relative to the items' total paths), then the number of
- * branches, each by the highest samples per second.
+ * buffers are not touched): the wavefront size, then the closest-hit block shape
+ * (threads per CTA), then the closest-hit CTAs per SM, then the piece size
+ * (relative to the items' total paths), then the number of branches, each by the
+ * highest samples per second.
  * trials_out / trial_msamples_per_s (may be NULL) receive up to max_trials tried
  * settings and their millions of samples per second; *ntrials the count. */
 int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, uint32_t trial_samples,

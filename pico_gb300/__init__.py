@@ -184,11 +184,11 @@ class Context:
         return arr
 
     def render_many(self, renders, wavefront: int = 0, extend_ctas_per_sm: int = 0, branches: int = 0,
-                    piece_paths: int = 0):
+                    piece_paths: int = 0, extend_threads: int = 0):
         """pico_gpu_render_many: all renders in one CUDA graph launch; their buffers are updated in place.
         Returns (per-render completion times in ms, report dict)."""
         arr = self._items(renders)
-        params = CLaunchParams(wavefront, extend_ctas_per_sm, branches, piece_paths)
+        params = CLaunchParams(wavefront, extend_ctas_per_sm, branches, piece_paths, extend_threads, 0)
         done = (C.c_double * max(len(renders), 1))()
         rep = CBatchReport()
         self.check(self.lib.pico_gpu_render_many(self.handle, len(renders), arr, C.byref(params), done,
@@ -208,7 +208,7 @@ class Context:
 
         def as_dict(p):
             return {"wavefront": p.wavefront, "extend_ctas_per_sm": p.extend_ctas_per_sm, "branches": p.branches,
-                    "piece_paths": p.piece_paths}
+                    "piece_paths": p.piece_paths, "extend_threads": p.extend_threads}
         return as_dict(best), [(as_dict(trials[i]), rates[i]) for i in range(nt.value)]
 
     def atrous(self, pixels, normals, positions, diffuse, width: int, height: int) -> np.ndarray:

@@ -58,7 +58,7 @@ void free_batch_state(pico_gpu_ctx* ctx)
 namespace {
 
 struct Params {
-    uint32_t wavefront, extend_ctas, branches, piece_paths;
+    uint32_t wavefront, extend_ctas, branches, piece_paths, extend_threads;
 };
 
 // Host-side state of one render between its upload and its download.
@@ -78,12 +78,13 @@ struct Piece {
 
 Params resolve(const pico_launch_params* lp)
 {
-    Params p{1u << 20, 0u, 0u, 0u};
+    Params p{1u << 20, 0u, 0u, 0u, 128u};
     if (lp) {
         if (lp->wavefront) p.wavefront = std::min<uint32_t>(std::max<uint32_t>(lp->wavefront, 1u << 12), kMaxPaths);
         p.extend_ctas = lp->extend_ctas_per_sm;
         p.branches = lp->branches;
         p.piece_paths = lp->piece_paths;
+        if (lp->extend_threads == 64 || lp->extend_threads == 256) p.extend_threads = lp->extend_threads;
     }
     return p;
 }
@@ -222,6 +223,7 @@ cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& im
             b.taken = as<uint32_t>(image.r.taken);
             b.done = as<uint32_t>(image.r.done);
             b.extend_ctas = p.extend_ctas;
+            b.extend_threads = p.extend_threads;
             e = launch_render_batch(it.scene->view, b, pr.cam, cfg.seed, spb, cfg.max_ray_depth, cfg.max_samples,
                                     cfg.max_variance, (int)cfg.estimator, path.status, order, st);
         }
@@ -418,13 +420,14 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
         if (count < max_trials) {
             if (trials_out)
                 trials_out[count] = pico_launch_params{p.wavefront, p.extend_ctas, p.branches,
-                                                       piece_paths(paths_real, s.pieces_per_total)};
+                                                       piece_paths(paths_real, s.pieces_per_total),
+                                                       p.extend_threads, 0};
             if (trial_msamples_per_s) trial_msamples_per_s[count] = msps;
         }
         ++count;
         return PICO_OK;
     };
-    Setting cur{Params{1u << 20, 0u, 0u, 0u}, 0u};
+    Setting cur{Params{1u << 20, 0u, 0u, 0u, 128u}, 0u};
     double rate = 0.0;
     status = measure(cur, rate);   // warm-up: module loading, buffer growth
     if (status != PICO_OK) return status;
@@ -447,12 +450,13 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
         return PICO_OK;
     };
     status = try_axis([](Setting& s, uint32_t v) { s.p.wavefront = v; }, {1u << 18, 1u << 20, 1u << 22});
+    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.extend_threads = v; }, {64u, 128u, 256u});
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.extend_ctas = v; }, {2u, 4u, 0u});
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.pieces_per_total = v; }, {0u, 32u, 128u});
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.branches = v; }, {8u, 16u, 0u});
     if (status != PICO_OK) return status;
     *best = pico_launch_params{cur.p.wavefront, cur.p.extend_ctas, cur.p.branches,
-                               piece_paths(paths_real, cur.pieces_per_total)};
+                               piece_paths(paths_real, cur.pieces_per_total), cur.p.extend_threads, 0};
     if (ntrials) *ntrials = std::min(count, max_trials);
     return PICO_OK;
 }

@@ -108,8 +108,10 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
     }
 }
 
-template <int kOrder>
-__global__ void __launch_bounds__(128, 7) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
+// kThreads per CTA (64, 128 or 256): the block shape batched renders tune; the
+// register budget is the same 896 threads per SM for every shape.
+template <int kOrder, int kThreads>
+__global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                        const uint32_t* count, unsigned long long* work, int* err,
                                                        bool shadow, unsigned long long* tally)
 {
@@ -668,12 +670,12 @@ static unsigned grid_for(uint32_t n, int threads)
 
 // Persistent grid of a closest-hit launch: `ctas_per_sm` CTAs per SM (0 or more
 // than fit: as many as fit).
-template <int kOrder>
+template <int kOrder, int kThreads>
 static unsigned extend_grid(uint32_t ctas_per_sm)
 {
     static int per_sm = 0;
     if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder, kThreads>, kThreads, 0);
         if (per_sm < 1) per_sm = 1;
     }
     const int k = (ctas_per_sm > 0 && (int)ctas_per_sm < per_sm) ? (int)ctas_per_sm : per_sm;
@@ -684,8 +686,19 @@ template <int kOrder>
 static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
                           DeviceStatus* status, bool shadow, unsigned long long* tally, cudaStream_t st)
 {
-    extend_kernel<kOrder><<<extend_grid<kOrder>(b.extend_ctas), 128, 0, st>>>(sc, b, q, count, &status->work,
-                                                                              &status->trace_error, shadow, tally);
+    switch (b.extend_threads) {
+    case 64:
+        extend_kernel<kOrder, 64><<<extend_grid<kOrder, 64>(b.extend_ctas), 64, 0, st>>>(
+            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+        break;
+    case 256:
+        extend_kernel<kOrder, 256><<<extend_grid<kOrder, 256>(b.extend_ctas), 256, 0, st>>>(
+            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+        break;
+    default:
+        extend_kernel<kOrder, 128><<<extend_grid<kOrder, 128>(b.extend_ctas), 128, 0, st>>>(
+            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+    }
 }
 
 __global__ void stamp_kernel(unsigned long long* dst)

@@ -24,6 +24,8 @@ struct CameraView {
 struct PathBatch {
     uint32_t n, npix, width;
     uint32_t extend_ctas;              // closest-hit launches: persistent CTAs per SM (0: as many as fit)
+    uint32_t extend_threads;           // closest-hit launches: threads per CTA, 64, 128 or 256 (other: 128)
+    uint32_t pad;
     const uint32_t* pix_list;          // npix pixel indices
     float4* org; float4* dir; float4* thr; float4* pay;
     float4* hit; uint32_t* hit_tri;

@@ -66,7 +66,7 @@ class CCamera(C.Structure):
 
 class CLaunchParams(C.Structure):
     _fields_ = [("wavefront", C.c_uint32), ("extend_ctas_per_sm", C.c_uint32), ("branches", C.c_uint32),
-                ("piece_paths", C.c_uint32)]
+                ("piece_paths", C.c_uint32), ("extend_threads", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class CBatchReport(C.Structure):

@@ -43,15 +43,16 @@ def singles(specs, gscenes):
     return out
 
 
-@pytest.mark.parametrize("wavefront,ctas,branches,piece_paths",
-                         [(0, 0, 0, 0), (1 << 12, 2, 2, 0), (1 << 14, 1, 1, 0), (0, 0, 0, 3000), (1 << 12, 4, 3, 777)])
-def test_batch_equals_single_renders(ctx, batch, wavefront, ctas, branches, piece_paths):
+@pytest.mark.parametrize("wavefront,ctas,branches,piece_paths,threads",
+                         [(0, 0, 0, 0, 0), (1 << 12, 2, 2, 0, 64), (1 << 14, 1, 1, 0, 256), (0, 0, 0, 3000, 128),
+                          (1 << 12, 4, 3, 777, 64)])
+def test_batch_equals_single_renders(ctx, batch, wavefront, ctas, branches, piece_paths, threads):
     """Also with renders split into pieces of disjoint pixel ranges on different branches."""
     specs, gscenes = batch
     want = singles(specs, gscenes)
     renders = renders_of(specs, gscenes)
     done_ms, rep = ctx.render_many(renders, wavefront=wavefront, extend_ctas_per_sm=ctas, branches=branches,
-                                   piece_paths=piece_paths)
+                                   piece_paths=piece_paths, extend_threads=threads)
     for r, (px, cnt, var) in zip(renders, want):
         np.testing.assert_array_equal(r["pixels"], px)
         np.testing.assert_array_equal(r["sample_count"], cnt)
@@ -82,7 +83,7 @@ def test_autotune_picks_a_timed_setting(ctx, batch):
     specs, gscenes = batch
     renders = renders_of(specs, gscenes)
     best, trials = ctx.autotune_batch(renders, trial_samples=1)
-    assert len(trials) == 12 and all(rate > 0 for _, rate in trials)
+    assert len(trials) == 15 and all(rate > 0 for _, rate in trials)
     assert best == max(trials, key=lambda t: t[1])[0]
     # the items' own buffers are untouched
     for r in renders:
