@@ -387,6 +387,9 @@ typedef struct {
 } pico_nrc_config;
 
 int pico_gpu_nrc_default_config(pico_nrc_config* out);
+/* A cache lives on its context's device and must be freed before the context is
+ * shut down.  An empty box (aabb_max not above aabb_min on any axis) is set from
+ * the bounds of the first scene rendered with the cache; set_bounds changes it. */
 int pico_gpu_nrc_create(pico_gpu_ctx* ctx, const pico_nrc_config* config, pico_gpu_nrc** out);
 void pico_gpu_nrc_free(pico_gpu_nrc* cache);
 int pico_gpu_nrc_get_params(pico_gpu_nrc* cache, float* mlp, float* grid);

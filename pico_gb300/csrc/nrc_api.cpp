@@ -212,7 +212,6 @@ void pico_gpu_nrc_free(pico_gpu_nrc* c)
     cudaSetDevice(c->ctx->device);
     if (c->ctx->cache == c) c->ctx->cache = nullptr;
     for (void* p : c->allocations) cudaFree(p);
-    for (void* p : c->render_allocations) cudaFree(p);
     delete c;
 }
 

@@ -26,8 +26,6 @@ struct pico_gpu_nrc {
     float* loss = nullptr;
     int* err = nullptr;
     std::vector<void*> allocations;
-    // render-time buffers: training path state and records
-    std::vector<void*> render_allocations;
     // cumulative render work: training paths, training records, optimiser steps, cache queries
     uint64_t render_stats[4] = {0, 0, 0, 0};
 };
