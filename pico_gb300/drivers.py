@@ -5,6 +5,9 @@
         (uniformly random positions over a 400 x 125 x 400 box, seeded)
     python -m pico_gb300.drivers cache-render [--passes K]
         a 1920x1080 render of the lit field through the radiance cache
+    python -m pico_gb300.drivers render [--estimator E] [--passes K]
+        a 1920x1080 render of the lit field, K samples per pixel, estimator E
+        (0 the reference's, 1 the physical one)
 """
 from __future__ import annotations
 
@@ -65,18 +68,30 @@ def cache_render(passes: int) -> None:
     ctx.close()
 
 
+def render(estimator: int, passes: int) -> None:
+    ctx = pico_gb300.Context(0)
+    gs = ctx.upload(scenes.lit_field())
+    gs.render(scenes.lit_field_camera(1920, 1080), 8, passes, seed=99, estimator=estimator)
+    print("render driver:", ctx.render_stats())
+    gs.free()
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["cache", "cache-render"])
+    ap.add_argument("what", choices=["cache", "cache-render", "render"])
     ap.add_argument("--queries", type=int, default=1 << 21)
     ap.add_argument("--records", type=int, default=1 << 16)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--passes", type=int, default=3)
+    ap.add_argument("--estimator", type=int, default=1)
     a = ap.parse_args()
     if a.what == "cache":
         cache(a.queries, a.records, a.reps)
-    else:
+    elif a.what == "cache-render":
         cache_render(a.passes)
+    else:
+        render(a.estimator, a.passes)
 
 
 if __name__ == "__main__":
