@@ -440,6 +440,51 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
+def bench_cornell(ctx, args, local):
+    """The reference's CPU-runnable case: the Cornell box at 256x256, 16 spp, depth 5, reference
+    estimator, a-trous denoise, through pico_gpu_render (host buffers), next to the reference's
+    render loop over the whole image on the host cores (its own code where its harness is built,
+    else the port; no denoise on the CPU side)."""
+    scene = scenes.cornell_box()
+    cam = scenes.cornell_camera(256, 256)
+    gs = ctx.upload(scene)
+    gs.render(cam, 5, 16, seed=7, denoise=True)   # warm-up
+    times, samples = [], 0
+    with ClockSampler(local) as clocks:
+        for k in range(5):
+            t0 = time.perf_counter()
+            gs.render(cam, 5, 16, seed=11 + k, denoise=True)
+            times.append(time.perf_counter() - t0)
+            samples = ctx.render_stats()["samples"]
+    gs.free()
+    secs = float(np.median(times))
+    out = {"workload": "Cornell box 256x256, 16 spp, depth 5, reference estimator (early exit at zero variance), "
+                       "a-trous 5 levels", "ms_per_render": secs * 1e3, "Msamples_per_s": samples / secs / 1e6,
+           "samples": samples, "timing": "median wall clock of 5 pico_gpu_render calls, host buffers in and out",
+           "clocks": clocks.summary()}
+    if not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pico_oracle
+        W, H = cam.resolution
+        idx = np.arange(W * H, dtype=np.uint32)
+        seeds = np.random.default_rng(3).integers(1, 2**32 - 1, size=W * H, dtype=np.uint64)
+        cores = os.cpu_count() or 1
+        try:
+            rs = pico_oracle.Reference().scene(scene)
+            _, cnt, _, csecs = rs.render_pixels(cam, 5, 16, idx, seeds)
+            kind = "reference"
+        except (FileNotFoundError, OSError):
+            os_ = pico_oracle.Oracle().scene(scene)
+            t0 = time.perf_counter()
+            _, cnt, _ = os_.render_pixels(cam, 5, 16, idx, seeds)
+            csecs = time.perf_counter() - t0
+            kind = "port"
+        out["cpu_baseline"] = {"value": int(cnt.sum()) / csecs / 1e6, "unit": "Msamples/s", "cores": cores,
+                               "kind": kind, "sample": "the whole 256x256 image, 16 spp, depth 5, no denoise",
+                               "ms_per_render": csecs * 1e3}
+    return out
+
+
 def cpu_render(scene, cam, args):
     """The reference render loop on host cores over a seeded pixel subset (reference code, else the port)."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -674,9 +719,10 @@ def main():
         cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
                "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
 
-    render = render_physical = atrous = tonemap = hdr = cache = batched = None
+    render = render_physical = atrous = tonemap = hdr = cache = batched = cornell = None
     if not args.no_render:
         gs.free()
+        cornell = bench_cornell(ctx, args, local)
         render = bench_render(ctx, args, torch, local)
         render_physical = bench_render(ctx, args, torch, local, estimator=1)
         if args.nrc_passes:
@@ -691,7 +737,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
             "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clocks.summary(), "scene": info, "render_1080p": render,
+            "clocks": clocks.summary(), "scene": info, "cornell_256": cornell, "render_1080p": render,
             "render_1080p_physical": render_physical, "render_1080p_radiance_cache": cache,
             "batched_renders": batched, "atrous_1080p": atrous,
             "tonemap_1080p": tonemap, "hdr_1080p": hdr}
