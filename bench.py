@@ -402,7 +402,7 @@ def bench_batch(ctx, args, local):
         return [{"gpu_scene": g, "camera": w["camera"], "max_samples": w["max_samples"], "max_depth": w["max_depth"],
                  "seed": w["seed"], "estimator": 1} for g, w in zip(gsc, work)]
     t0 = time.perf_counter()
-    best, trials = ctx.autotune_batch(items(), trial_samples=1)
+    best, trials = ctx.autotune_batch(items(), trial_samples=8)
     tune_s = time.perf_counter() - t0
     its = items()
     with ClockSampler(local) as clocks:

@@ -288,11 +288,14 @@ int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t* kinds
  * No counterpart in the reference, which renders one scene at a time.  Many
  * independent renders, each what pico_gpu_render does for one (scene, camera,
  * config, progressive buffers) with the REFERENCE or PHYSICAL estimator and
- * no denoise / tone map, run as one CUDA graph: every render's batches are
- * captured on its own branch (streams), the graph is instantiated and launched
- * once, and the branches share the GPU.  The cancel flag is not polled.  Each
- * render keeps its own path state (at most `wavefront` paths), so device
- * memory grows with the number of renders. */
+ * no denoise / tone map, run as one CUDA graph: the renders (or their pieces)
+ * are spread over graph branches (streams) by estimated cost (pixels x samples
+ * x (1 + min(depth, 4))) so that the branches end together, each branch runs
+ * its work cheapest first, and the cheaper a piece the higher the scheduling
+ * priority of its kernels; the graph is instantiated and launched once, and the
+ * branches share the GPU.  The cancel flag is not polled.  Each render keeps
+ * its own path state (at most `wavefront` paths), so device memory grows with
+ * the number of renders. */
 typedef struct {
     const pico_gpu_scene* scene;
     pico_camera camera;
@@ -305,7 +308,9 @@ typedef struct {
 typedef struct {
     uint32_t wavefront;             /* paths per batch of one render; 0: 2^20 */
     uint32_t extend_ctas_per_sm;    /* persistent CTAs per SM of each closest-hit launch; 0: as many as fit */
-    uint32_t branches;              /* graph branches the pieces are spread over; 0: one per piece */
+    uint32_t branches;              /* graph branches the pieces are spread over; 0: one per piece; at
+                                     * most the device's work queues (CUDA_DEVICE_MAX_CONNECTIONS, 8 by
+                                     * default), past which branches would share queues */
     uint32_t piece_paths;           /* a render of more paths (pixels x samples) than this is split into
                                      * pieces of disjoint pixel ranges, each its own branch work; 0: none */
     uint32_t extend_threads;        /* threads per CTA of each closest-hit launch: 64, 128 or 256; 0: 128 */
@@ -325,11 +330,13 @@ typedef struct {
 int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items,
                          const pico_launch_params* params, double* completion_ms, pico_batch_report* report);
 /* Chooses launch parameters for a set of renders by timing short renders of the
- * same items (trial_samples samples per pixel into scratch buffers; the items'
- * buffers are not touched): the wavefront size, then the closest-hit block shape
+ * same items into scratch buffers (the items' buffers are not touched): the item
+ * with the most samples per pixel takes trial_samples of them, every other item
+ * the same fraction of its own, rounded, at least 1.  Tuned, each by the highest
+ * samples per second: the wavefront size, then the closest-hit block shape
  * (threads per CTA), then the closest-hit CTAs per SM, then the piece size
- * (relative to the items' total paths), then the number of branches, each by the
- * highest samples per second.
+ * (relative to the items' total paths), then the number of branches (2, 4, or
+ * as many as the device has work queues).
  * trials_out / trial_msamples_per_s (may be NULL) receive up to max_trials tried
  * settings and their millions of samples per second; *ntrials the count. */
 int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, uint32_t trial_samples,

@@ -7,17 +7,19 @@
 // piece gets a path slot of its own (path state of at most `wavefront` paths,
 // device status block).  Each piece's batches are captured, without host
 // synchronisation, on one of `branches` streams forked from the context's
-// stream; the captured graph is instantiated and launched once.  Small renders
-// cannot fill 152 SMs on their own, and one large render would otherwise run
-// alone at the end: side by side their persistent closest-hit grids and shade
-// kernels share the GPU.  Pieces of one render write disjoint pixels of the
-// same buffers.  A 1-thread kernel at the graph's start and at the end of each
-// piece stores the device's nanosecond timer, from which the per-render
-// completion times (the last of its pieces) are read.
+// stream (placed by estimated cost: schedule()); the captured graph is
+// instantiated and launched once.  Small renders cannot fill 152 SMs on their
+// own, and one large render would otherwise run alone at the end: side by side
+// their persistent closest-hit grids and shade kernels share the GPU.  Pieces of
+// one render write disjoint pixels of the same buffers.  A 1-thread kernel at
+// the graph's start and at the end of each piece stores the device's nanosecond
+// timer, from which the per-render completion times (the last of its pieces)
+// are read.
 #include "render_internal.h"
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <memory>
 #include <vector>
 
@@ -75,6 +77,17 @@ struct Piece {
     size_t p0, p1;
     uint32_t chunk_pix, spb_max;
 };
+
+// The device's hardware work queues for this process (CUDA_DEVICE_MAX_CONNECTIONS,
+// 8 by default).  More branches than queues share queues, and a cheap piece's
+// kernels then wait behind a costly piece's in the same queue whatever their
+// priorities, so a batch uses at most this many branches.
+uint32_t work_queues()
+{
+    const char* v = std::getenv("CUDA_DEVICE_MAX_CONNECTIONS");
+    const long n = v ? std::strtol(v, nullptr, 10) : 0;
+    return n >= 1 && n <= 128 ? (uint32_t)n : 8u;
+}
 
 Params resolve(const pico_launch_params* lp)
 {
@@ -204,6 +217,57 @@ std::vector<Piece> make_pieces(uint32_t n, const pico_render_item* items, const 
     return pieces;
 }
 
+// A piece's cost: its paths times (1 + min(depth, 4)), an estimate of the
+// segments a path traces.
+std::vector<double> piece_costs(const std::vector<Piece>& pieces, const pico_render_item* items)
+{
+    std::vector<double> cost(pieces.size());
+    for (size_t j = 0; j < pieces.size(); ++j) {
+        const pico_render_config& c = items[pieces[j].render].config;
+        cost[j] = (double)(pieces[j].p1 - pieces[j].p0) * c.max_samples * (1.0 + std::min(c.max_ray_depth, 4u));
+    }
+    return cost;
+}
+
+// Which pieces run on which branch, in order.  Pieces are placed costliest
+// first on the branch with the least cost so far (longest processing time
+// first), so that the branches end close together and no lone branch holds the
+// GPU at the end; each branch then runs its pieces cheapest first.
+std::vector<std::vector<size_t>> schedule(const std::vector<double>& cost, uint32_t branches)
+{
+    const size_t np = cost.size();
+    std::vector<size_t> order(np);
+    for (size_t j = 0; j < np; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] > cost[b]; });
+    std::vector<double> load(branches, 0.0);
+    std::vector<std::vector<size_t>> lanes(branches);
+    for (size_t j : order) {
+        const size_t k = (size_t)(std::min_element(load.begin(), load.end()) - load.begin());
+        lanes[k].push_back(j);
+        load[k] += cost[j];
+    }
+    for (std::vector<size_t>& lane : lanes)
+        std::stable_sort(lane.begin(), lane.end(), [&](size_t a, size_t b) { return cost[a] < cost[b]; });
+    return lanes;
+}
+
+// Scheduling priority of every piece's kernels (lower numbers are higher, as
+// for streams): the device's priority levels split the pieces by cost rank, the
+// cheapest at the greatest.  Branches interleave roughly kernel by kernel, not by
+// work, so without priorities a small render waits behind the big batches of
+// every other branch; with them its kernels take the next free SMs.
+std::vector<int> piece_priorities(const std::vector<double>& cost, int least, int greatest)
+{
+    const size_t np = cost.size();
+    const size_t levels = (size_t)(least - greatest) + 1;
+    std::vector<size_t> order(np);
+    for (size_t j = 0; j < np; ++j) order[j] = j;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return cost[a] < cost[b]; });
+    std::vector<int> prio(np, least);
+    for (size_t i = 0; i < np; ++i) prio[order[i]] = greatest + (int)(i * levels / np);
+    return prio;
+}
+
 // A piece's batches on stream st, without synchronisation (they are captured):
 // path state from the piece's slot, pixels and progressive buffers from the render's.
 cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& image, BatchSlot& path,
@@ -246,7 +310,8 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     const std::vector<Piece> pieces = make_pieces(n, items, prep, params);
     const size_t np = pieces.size();
     Params p = params;
-    p.branches = (uint32_t)std::max<size_t>(1, std::min<size_t>(p.branches ? p.branches : np, std::max<size_t>(np, 1)));
+    p.branches = (uint32_t)std::max<size_t>(
+        1, std::min<size_t>({p.branches ? (size_t)p.branches : np, np, (size_t)work_queues()}));
     e = ensure_state(ctx, n, np, p.branches);
     BatchState& bs = *ctx->batch;
     for (size_t j = 0; j < np && e == cudaSuccess; ++j) {
@@ -278,19 +343,31 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     cudaError_t ce = launch_stamp(bs.stamps, st);
     if (ce == cudaSuccess) ce = cudaEventRecord(events[0], st);
     for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(bs.streams[k], events[0], 0);
-    for (size_t j = 0; j < np && ce == cudaSuccess; ++j) {
-        const Piece& pc = pieces[j];
-        cudaStream_t bst = bs.streams[j % p.branches];
-        ce = enqueue(ctx, items[pc.render], *bs.images[pc.render], *bs.pieces[j], p, prep[pc.render], pc, bst);
-        if (ce == cudaSuccess) ce = launch_stamp(bs.stamps + 1 + j, bst);
-    }
+    const std::vector<double> cost = piece_costs(pieces, items);
+    const std::vector<std::vector<size_t>> lanes = schedule(cost, p.branches);
+    int least = 0, greatest = 0;
+    if (ce == cudaSuccess) ce = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    const std::vector<int> prio = piece_priorities(cost, least, greatest);
+    for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k)
+        for (size_t j : lanes[k]) {
+            const Piece& pc = pieces[j];
+            cudaLaunchAttributeValue pv{};
+            pv.priority = prio[j];
+            ce = cudaStreamSetAttribute(bs.streams[k], cudaStreamAttributePriority, &pv);
+            if (ce == cudaSuccess)
+                ce = enqueue(ctx, items[pc.render], *bs.images[pc.render], *bs.pieces[j], p, prep[pc.render], pc,
+                             bs.streams[k]);
+            if (ce == cudaSuccess) ce = launch_stamp(bs.stamps + 1 + j, bs.streams[k]);
+            if (ce != cudaSuccess) break;
+        }
     for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k) {
         ce = cudaEventRecord(events[1 + k], bs.streams[k]);
         if (ce == cudaSuccess) ce = cudaStreamWaitEvent(st, events[1 + k], 0);
     }
     e = cudaStreamEndCapture(st, &graph);
     if (ce != cudaSuccess) e = ce;
-    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    // the kernels keep the priorities they were captured with
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     size_t nodes = 0;
     if (e == cudaSuccess) e = cudaGraphGetNodes(graph, nullptr, &nodes);
     if (e != cudaSuccess) {
@@ -375,15 +452,21 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
     *best = pico_launch_params{};
     if (n == 0) return PICO_OK;
     cudaSetDevice(ctx->device);
-    // short renders of the same items into scratch buffers
-    const uint32_t tspp = std::max(1u, trial_samples);
+    // short renders of the same items into scratch buffers: the item with the most
+    // samples per pixel takes trial_samples, the others the same fraction of theirs
+    // (at least 1), so that the trials keep the batch's balance of work
+    uint32_t max_spp = 1;
+    for (uint32_t r = 0; r < n; ++r) max_spp = std::max(max_spp, items[r].config.max_samples);
+    const uint64_t tspp = std::min<uint64_t>(std::max(1u, trial_samples), max_spp);
+    std::vector<uint32_t> trial_spp(n);
     std::vector<pico_render_item> trial(items, items + n);
     std::vector<std::vector<float>> px(n), var(n);
     std::vector<std::vector<uint32_t>> cnt(n);
     uint64_t paths_trial = 0, paths_real = 0;
     for (uint32_t r = 0; r < n; ++r) {
         const uint64_t npx = (uint64_t)items[r].config.width * items[r].config.height;
-        paths_trial += npx * tspp;
+        trial_spp[r] = (uint32_t)std::max<uint64_t>(1, (items[r].config.max_samples * tspp + max_spp / 2) / max_spp);
+        paths_trial += npx * trial_spp[r];
         paths_real += npx * items[r].config.max_samples;
     }
     auto reset = [&]() {
@@ -395,7 +478,7 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
             trial[r].pixels_rgb = px[r].data();
             trial[r].variance_rgb = var[r].data();
             trial[r].sample_count = cnt[r].data();
-            trial[r].config.max_samples = tspp;
+            trial[r].config.max_samples = trial_spp[r];
         }
     };
     // the piece size is tuned as a fraction of all paths (1 / pieces_per_total) and
@@ -453,7 +536,7 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.extend_threads = v; }, {64u, 128u, 256u});
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.extend_ctas = v; }, {2u, 4u, 0u});
     if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.pieces_per_total = v; }, {0u, 32u, 128u});
-    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.branches = v; }, {8u, 16u, 0u});
+    if (status == PICO_OK) status = try_axis([](Setting& s, uint32_t v) { s.p.branches = v; }, {2u, 4u, 0u});
     if (status != PICO_OK) return status;
     *best = pico_launch_params{cur.p.wavefront, cur.p.extend_ctas, cur.p.branches,
                                piece_paths(paths_real, cur.pieces_per_total), cur.p.extend_threads, 0};
