@@ -145,6 +145,17 @@ def test_single_instance_and_misses(ctx, oracle):
     assert np.isinf(got["t"][miss]).all()
 
 
+def test_full_size_instance_field(ctx, oracle):
+    """The traversal workload at its full size: 4096 instances of a level-4 icosphere
+    (5120 triangles each), 16,777,216 rays (half primary rays of a 4096x4096 pinhole,
+    half cosine-distributed bounce rays from surface points), both orders bit-exact."""
+    scene = scenes.instance_field(n_instances=4096, level=4, seed=12345)
+    rays = scenes.field_rays(scene, n_total=1 << 24, resolution=4096, seed=7)
+    got, want = check(ctx, oracle, scene, rays, "full-size field")
+    hit = want["inst"] != pico_gb300.MISS
+    assert 0.2 < hit.mean() < 1.0
+
+
 def test_empty_batch(ctx):
     gs = ctx.upload(scenes.cornell_box())
     out = gs.trace_closest(np.zeros(0, RAY_DTYPE))
