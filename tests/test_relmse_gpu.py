@@ -48,3 +48,51 @@ def test_device_early_exit_bias_matches_the_reference(cornell):
     assert abs(exited - j.ref64_exited) < 150, (exited, j.ref64_exited)
     ratio = j.relmse(pix) / j.ref64_relmse
     assert 0.6 < ratio < 1.6, ratio
+
+
+@pytest.fixture(scope="module")
+def lit(ctx):
+    scene = scenes.lit_field()
+    gs = ctx.upload(scene)
+    yield scene, gs
+    gs.free()
+
+
+@pytest.mark.parametrize("name,estimator", [("lit", 0), ("lit_phys", 1)])
+def test_full_render_agrees_with_the_judge_per_pixel(lit, name, estimator):
+    """The full render workload (lit field, 1920x1080, depth 8) at 256 spp without the early
+    exit, against the converged judge of the same estimator (the reference's own samples for
+    estimator 0, the FP64 oracle's for the physical one): the judged pixels and channels within
+    4 standard errors (of the render's n samples and the judge's 4096), the median standardised
+    error near 0, and a relMSE no larger than an unbiased estimator's.
+
+    Lamps of radiance up to 50 make the per-sample radiance heavy-tailed.  A render that meets
+    one of the rare paths that dominate a pixel's variance lands far above the judge (z of 5 to
+    70), and one that meets none sits a little below it (median z about -0.1).  Measured over
+    three seeds, 0.2-0.4 % (reference estimator) and 1.2-1.7 % (physical) of the channels fell
+    beyond 4 standard errors, no channel on all three seeds, the physical ones all above the
+    judge; hence up to 2 % are allowed, and the relMSE, far below the variance-based
+    expectation for the same reason, is bounded from above only.  The reference loop keeps
+    samples 2..n (Scene.cpp:185-191), the physical estimator every sample."""
+    scene, gs = lit
+    j = Judge(name)
+    j.check_scene(scene)
+    cam = scenes.lit_field_camera(j.width, j.height)
+    spp = 256
+    pix, cnt, _ = gs.render(cam, j.depth, spp, seed=4242, max_variance=-1.0, estimator=estimator)
+    assert (cnt == spp).all()
+    n = spp - 1 if estimator == 0 else spp
+    x = j.take(pix).astype(np.float64)
+    assert np.isfinite(x).all()
+    se = np.sqrt(j.var * (1.0 / n + 1.0 / j.spp))
+    zs = (x - j.mean) / np.maximum(se, 1e-30)
+    flat = se == 0
+    assert (x[flat] == j.mean[flat]).all()   # pixels whose samples never vary (e.g. the black sky)
+    beyond = float((np.abs(zs[~flat]) > 4.0).mean())
+    median = float(np.median(zs[~flat]))
+    ratio = j.relmse(pix) / j.expected(n)
+    print(f"{name}: {beyond:.4f} of {int((~flat).sum())} channels beyond 4 SE, median z {median:.3f}, "
+          f"relMSE / expected {ratio:.3f}")
+    assert beyond <= 0.02, beyond
+    assert abs(median) < 0.3, median
+    assert ratio < 1.5, ratio
