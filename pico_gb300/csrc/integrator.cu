@@ -403,9 +403,15 @@ __global__ void __launch_bounds__(kRenderThreads) shade_physical_kernel(SceneVie
                         // next-event estimation towards one light (the sun last), picked by the
                         // scene's power-proportional table
                         if (nl > 0) {
+                            // the first slot whose cumulative share exceeds up (the last
+                            // slot otherwise), by bisection over the non-decreasing table
                             const float up = rng.uniform();
-                            uint32_t li = 0;
-                            while (li + 1 < nl && up >= sc.light_pick[li]) ++li;
+                            uint32_t li = 0, hi = nl - 1;
+                            while (li < hi) {
+                                const uint32_t mid = (li + hi) >> 1;
+                                if (up >= sc.light_pick[mid]) li = mid + 1;
+                                else hi = mid;
+                            }
                             const float pick = sc.light_pick[nl + li];
                             float3 wi = make_float3(0.0f, 0.0f, 0.0f), c = wi;
                             float reach = 0.0f;

@@ -90,6 +90,15 @@ def test_glossy_field_physical_render_matches_oracle(ctx, oracle):
                          512, 12)
 
 
+def test_many_light_field_physical_render_matches_oracle(ctx, oracle):
+    """300 quad lights over a small field: the power-proportional light pick bisects a
+    301-slot table (the oracle scans it)."""
+    from pico_gb300.types import Camera
+    scene = scenes.lit_field(n_instances=48, level=2, seed=77, n_lights=300, extent=20.0)
+    cam = Camera(position=(0.0, 8.0, -60.0), direction=(0.0, -0.15, 1.0), resolution=(48, 32), aspect=1.5)
+    check_against_oracle(ctx, oracle, scene, cam, 5, 1024, 2048, 256, 13)
+
+
 def test_physical_counts_every_sample(ctx):
     """No early exit and no dropped first sample: black pixels take every sample too."""
     gs = ctx.upload(scenes.cornell_box())
