@@ -8,6 +8,10 @@
     python -m pico_gb300.drivers render [--estimator E] [--passes K]
         a 1920x1080 render of the lit field, K samples per pixel, estimator E
         (0 the reference's, 1 the physical one)
+    python -m pico_gb300.drivers batch [--renders N] [--scale S]
+        N renders of the batched-rendering workload (resolutions times S) in one
+        CUDA-graph launch, physical estimator, 2^22-path wavefront, 64-thread
+        closest-hit CTAs, 8 branches
 """
 from __future__ import annotations
 
@@ -77,9 +81,24 @@ def render(estimator: int, passes: int) -> None:
     ctx.close()
 
 
+def batch(renders: int, scale: float) -> None:
+    ctx = pico_gb300.Context(0)
+    work = scenes.batch_workload(renders, size_scale=scale)
+    gsc = [ctx.upload(w["scene"]) for w in work]
+    items = [{"gpu_scene": g, "camera": w["camera"], "max_samples": w["max_samples"], "max_depth": w["max_depth"],
+              "seed": w["seed"], "estimator": 1} for g, w in zip(gsc, work)]
+    done, rep = ctx.render_many(items, wavefront=1 << 22, extend_threads=64, branches=8)
+    print("batch driver:", rep, "completion p50 %.2f ms" % float(np.percentile(done, 50)))
+    for g in gsc:
+        g.free()
+    ctx.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["cache", "cache-render", "render"])
+    ap.add_argument("what", choices=["cache", "cache-render", "render", "batch"])
+    ap.add_argument("--renders", type=int, default=16)
+    ap.add_argument("--scale", type=float, default=0.5)
     ap.add_argument("--queries", type=int, default=1 << 21)
     ap.add_argument("--records", type=int, default=1 << 16)
     ap.add_argument("--reps", type=int, default=3)
@@ -90,8 +109,10 @@ def main() -> None:
         cache(a.queries, a.records, a.reps)
     elif a.what == "cache-render":
         cache_render(a.passes)
-    else:
+    elif a.what == "render":
         render(a.estimator, a.passes)
+    else:
+        batch(a.renders, a.scale)
 
 
 if __name__ == "__main__":
