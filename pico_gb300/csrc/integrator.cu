@@ -3,11 +3,12 @@
 //
 // A batch holds `npix` pixels x `spb` samples, one path per thread slot, with
 // the path state in structure-of-arrays form in HBM.  Per bounce depth:
-//   extend   closest hit for every queued path (traverse.cuh)
+//   extend   closest hit for every queued path (traverse.cuh) and, in the
+//            same launch, the NEE shadow rays the previous shade queued (a
+//            light hit adds its radiance)
 //   shade    BSRDF sample, emission, NEE setup, Russian roulette, next ray;
 //            survivors and shadow rays are appended to queues with one
 //            atomic per warp (ballot + popc + shuffle)
-//   shadow   closest hit for the NEE rays; a light hit adds its radiance
 // then `finish` turns payloads into sample values (NaN/Inf -> pink, as
 // Integrators.cpp:145-146) and `accumulate` applies the reference's running
 // mean / variance and early-exit rule per pixel, samples in order.
@@ -77,8 +78,7 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
     }
 }
 
-// Closest hit for the paths in `q` (count in *count): persistent, 32 queue
-// entries per warp fetch, each lane runs its ray to completion.
+// Stores a path segment's hit, or adds what a shadow ray delivers.
 __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b, uint32_t i, const TraceHit& h,
                                               int s, bool shadow)
 {
@@ -108,16 +108,26 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
     }
 }
 
-// kThreads per CTA (64, 128 or 256): the block shape batched renders tune; the
-// register budget is the same 896 threads per SM for every shape.
+// Persistent: 32 queue entries per warp fetch, each lane runs its ray to
+// completion.  One launch traces two queues back to back: the paths' next segments q[0, *count)
+// and, when sq is given, the shadow rays sq[0, *scount) the previous shade left
+// (they write disjoint path fields and both finish before the next shade), so a
+// depth pays one launch and one tail.  kThreads per CTA (64, 128 or 256): the
+// block shape batched renders tune; the register budget is the same 896 threads
+// per SM for every shape.
 template <int kOrder, int kThreads>
 __global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
-                                                       const uint32_t* count, unsigned long long* work, int* err,
-                                                       bool shadow, unsigned long long* tally)
+                                                       const uint32_t* count, const uint32_t* sq,
+                                                       const uint32_t* scount, unsigned long long* work, int* err,
+                                                       unsigned long long* tally, unsigned long long* stally)
 {
     const unsigned lane = threadIdx.x & 31u;
-    const uint32_t n = *count;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(tally, (unsigned long long)n);
+    const uint32_t n0 = *count, n1 = sq ? *scount : 0u;
+    const uint64_t n = (uint64_t)n0 + n1;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(tally, (unsigned long long)n0);
+        if (sq) atomicAdd(stally, (unsigned long long)n1);
+    }
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(work, 32ull);
@@ -125,7 +135,8 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneV
         if (base >= n) break;
         const unsigned long long k = base + lane;
         if (k < n) {
-            const uint32_t i = q[k];
+            const bool shadow = k >= n0;
+            const uint32_t i = shadow ? sq[k - n0] : q[k];
             if (shadow && b.senergy[i].w == 2.0f) {
                 // physical estimator: an occlusion query bounded by the light sample's distance
                 const float4 c = b.scontrib[i];
@@ -690,20 +701,22 @@ static unsigned extend_grid(uint32_t ctas_per_sm)
 
 template <int kOrder>
 static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
-                          DeviceStatus* status, bool shadow, unsigned long long* tally, cudaStream_t st)
+                          const uint32_t* sq, const uint32_t* scount, DeviceStatus* status,
+                          unsigned long long* tally, cudaStream_t st)
 {
+    unsigned long long* stally = &status->rays[2];
     switch (b.extend_threads) {
     case 64:
         extend_kernel<kOrder, 64><<<extend_grid<kOrder, 64>(b.extend_ctas), 64, 0, st>>>(
-            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
         break;
     case 256:
         extend_kernel<kOrder, 256><<<extend_grid<kOrder, 256>(b.extend_ctas), 256, 0, st>>>(
-            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
         break;
     default:
         extend_kernel<kOrder, 128><<<extend_grid<kOrder, 128>(b.extend_ctas), 128, 0, st>>>(
-            sc, b, q, count, &status->work, &status->trace_error, shadow, tally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
     }
 }
 
@@ -732,8 +745,11 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
         e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
         if (e != cudaSuccess) return e;
         unsigned long long* tally = &status->rays[depth == 0 ? 0 : 1];
+        // this depth's segments, and from depth 1 on the previous shade's shadow rays
+        const uint32_t* sq = depth > 0 ? b.shadow_queue : nullptr;
         with_variant(order, sc, [&](auto v) {
-            launch_extend<decltype(v)::value>(sc, b, b.queue[cur], &b.counters[cur], status, false, tally, st);
+            launch_extend<decltype(v)::value>(sc, b, b.queue[cur], &b.counters[cur], sq, &b.counters[2], status,
+                                              tally, st);
         });
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
@@ -744,14 +760,6 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
         else
             shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
                                                                                     trace_last);
-        if (depth < max_depth) {
-            e = cudaMemsetAsync(&status->work, 0, sizeof(unsigned long long), st);
-            if (e != cudaSuccess) return e;
-            with_variant(order, sc, [&](auto v) {
-                launch_extend<decltype(v)::value>(sc, b, b.shadow_queue, &b.counters[2], status, true,
-                                                  &status->rays[2], st);
-            });
-        }
         cur ^= 1;
     }
     return cudaGetLastError();
