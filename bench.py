@@ -10,7 +10,9 @@ rays leaving random surface points.  One step = one closest-hit pass
   value   rays/s with rays and hits resident in HBM (device-pointer entry point),
           timed with CUDA events on the launching stream.
   e2e     rays/s through the host-buffer entry point from pinned host memory:
-          every step copies the rays in and the hits out.
+          every step moves the rays in and the hits out (page-locked buffers are
+          read and written in place by the kernel over the host link, others are
+          staged through device buffers in overlapped chunks).
   cpu_baseline / --impl reference
           the reference algorithm on this machine's host cores: the reference's own
           code when its harness is built here (oracle/_ref), else the oracle port.
@@ -691,7 +693,8 @@ def main():
             gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
         e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, f"cuda:{local}")
         e2e = {"value": replica_throughput(n, world, e2e_s), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
-               "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3}
+               "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3,
+               "transfer": "pinned buffers read and written in place by the kernel over NVLink-C2C"}
 
     if rank != 0:
         if dist:

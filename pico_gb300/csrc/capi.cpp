@@ -283,14 +283,55 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
     return take_device_status(ctx, st);
 }
 
-// Host-buffer closest hit: the batch is cut into chunks that alternate between
-// two streams, so the copy of one chunk overlaps the traversal of the other.
+}  // extern "C"
+
+namespace {
+
+// The device address of [p, p + bytes) when both of its ends lie in page-locked
+// host memory mapped into the device's address space (cudaHostAlloc, or
+// cudaHostRegister under unified addressing) at one linear offset; null for
+// pageable memory, which the kernels never touch.
+void* mapped_range(const void* p, size_t bytes)
+{
+    cudaPointerAttributes a{}, b{};
+    const char* last = static_cast<const char*>(p) + (bytes - 1);
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+        return nullptr;
+    if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a.devicePointer;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Host-buffer closest hit.  Page-locked, mapped buffers are traversed in place:
+// one launch reads the rays and writes the hits through their device addresses
+// (over NVLink-C2C on a Grace host), with no staging copies.  Other buffers are
+// cut into chunks that alternate between two streams, so the copy of one chunk
+// overlaps the traversal of the other.
 int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_ray* rays, uint64_t n,
                            pico_hit* hits)
 {
     if (!ctx || !scene || (n && (!rays || !hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     cudaSetDevice(ctx->device);
     if (n == 0) return PICO_OK;
+    {
+        const void* mr = mapped_range(rays, n * sizeof(pico_ray));
+        void* mh = mr ? mapped_range(hits, n * sizeof(pico_hit)) : nullptr;
+        if (mr && mh) {
+            cudaError_t e = launch_trace(scene->view, static_cast<const pico_ray*>(mr), n, static_cast<pico_hit*>(mh),
+                                         ctx->status, false, scene_order(ctx, scene), ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
+            return take_device_status(ctx, ctx->stream);
+        }
+    }
     // 1M-ray chunks alternate between two streams: each chunk's copies overlap the
     // other stream's traversal, and only the first upload and the last download
     // (32 MB / 20 MB) stay exposed

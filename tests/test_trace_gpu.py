@@ -179,6 +179,24 @@ def test_device_pointer_path_matches_host_path(ctx, oracle):
     assert stats["nodes"] > 0 and stats["tris"] > 0 and stats["instances"] > 0
 
 
+def test_pinned_host_buffers_match_oracle(ctx, oracle):
+    """Page-locked, mapped host buffers are traversed in place (no staging copies); pinned
+    rays with pageable hits take the chunked copies: both give the oracle's hits."""
+    torch = pytest.importorskip("torch")
+    scene = scenes.instance_field(n_instances=256, level=3, seed=33, extent=20.0)
+    rays = np.concatenate([scenes.primary_rays(scenes.field_camera(256), seed=3),
+                           scenes.surface_rays(scene, 40000, seed=4)])
+    want = oracle.scene(scene).trace(rays)
+    gs = ctx.upload(scene)
+    h_rays = torch.from_numpy(rays.view(np.uint8).copy()).pin_memory()
+    h_hits = torch.zeros(len(rays) * HIT_DTYPE.itemsize, dtype=torch.uint8).pin_memory()
+    gs.trace_closest_ptr(h_rays.data_ptr(), len(rays), h_hits.data_ptr())
+    assert_same_hits(h_hits.numpy().view(HIT_DTYPE), want, "pinned")
+    pageable = np.zeros(len(rays), HIT_DTYPE)
+    gs.trace_closest_ptr(h_rays.data_ptr(), len(rays), pageable.ctypes.data)
+    assert_same_hits(pageable, want, "pinned rays, pageable hits")
+
+
 def test_scene_info(ctx):
     gs = ctx.upload(scenes.instance_field(n_instances=64, level=2, seed=1))
     info = gs.info()
