@@ -199,6 +199,10 @@ void pico_gpu_scene_free(pico_gpu_scene* scene);
 int pico_gpu_scene_info(const pico_gpu_scene* scene, uint64_t* out6);
 
 /* ---- closest hit (UpperLevelBVH::get_closest_intersection) --------------- */
+/* rays / hits are host buffers.  When both are page-locked and mapped
+ * (cudaHostAlloc, or cudaHostRegister under unified addressing) the kernel
+ * reads and writes them in place (over NVLink-C2C on a Grace host), with no
+ * staging copies; other buffers are staged through device memory in chunks. */
 int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                            const pico_ray* rays, uint64_t n, pico_hit* hits);
 /* Device-pointer variant on a caller stream (cudaStream_t, NULL = legacy default). */
