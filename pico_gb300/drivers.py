@@ -8,6 +8,9 @@
     python -m pico_gb300.drivers render [--estimator E] [--passes K]
         a 1920x1080 render of the lit field, K samples per pixel, estimator E
         (0 the reference's, 1 the physical one)
+    python -m pico_gb300.drivers cornell [--passes K]
+        K renders of the Cornell box at 256x256, 16 spp, depth 5, denoised
+        (after one warm-up render)
     python -m pico_gb300.drivers batch [--renders N] [--scale S]
         N renders of the batched-rendering workload (resolutions times S) in one
         CUDA-graph launch, physical estimator, 2^22-path wavefront, 64-thread
@@ -81,6 +84,17 @@ def render(estimator: int, passes: int) -> None:
     ctx.close()
 
 
+def cornell(passes: int) -> None:
+    ctx = pico_gb300.Context(0)
+    gs = ctx.upload(scenes.cornell_box())
+    cam = scenes.cornell_camera(256, 256)
+    for k in range(passes + 1):
+        gs.render(cam, 5, 16, seed=11 + k, denoise=True)
+    print("cornell driver:", ctx.render_stats())
+    gs.free()
+    ctx.close()
+
+
 def batch(renders: int, scale: float) -> None:
     ctx = pico_gb300.Context(0)
     work = scenes.batch_workload(renders, size_scale=scale)
@@ -96,7 +110,7 @@ def batch(renders: int, scale: float) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["cache", "cache-render", "render", "batch"])
+    ap.add_argument("what", choices=["cache", "cache-render", "render", "batch", "cornell"])
     ap.add_argument("--renders", type=int, default=16)
     ap.add_argument("--scale", type=float, default=0.5)
     ap.add_argument("--queries", type=int, default=1 << 21)
@@ -111,6 +125,8 @@ def main() -> None:
         cache_render(a.passes)
     elif a.what == "render":
         render(a.estimator, a.passes)
+    elif a.what == "cornell":
+        cornell(a.passes)
     else:
         batch(a.renders, a.scale)
 
