@@ -218,6 +218,10 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                          const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
+/* The render runs in batches of up to 2^24 paths (pixels x samples; about 3.5 GB
+ * of path state at the limit) and polls *should_quit between batches: a 1080p
+ * render at 64 spp is eight batches of 8 samples per pixel, about 60 ms each
+ * on a GB300, which bounds how soon a cancel is seen. */
 int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
                     const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
                     float* variance_rgb, const volatile int32_t* should_quit);
