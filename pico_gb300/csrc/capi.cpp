@@ -288,10 +288,11 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
 namespace {
 
 // The device address of [p, p + bytes) when both of its ends lie in page-locked
-// host memory mapped into the device's address space (cudaHostAlloc, or
-// cudaHostRegister under unified addressing) at one linear offset; null for
-// pageable memory, which the kernels never touch.
-void* mapped_range(const void* p, size_t bytes)
+// host memory mapped into `device`'s address space (cudaHostAlloc, or
+// cudaHostRegister under unified addressing, pinned against that device) at one
+// linear offset; null for pageable memory and for memory pinned against another
+// device, which the kernels never touch.
+void* mapped_range(const void* p, size_t bytes, int device)
 {
     cudaPointerAttributes a{}, b{};
     const char* last = static_cast<const char*>(p) + (bytes - 1);
@@ -299,7 +300,8 @@ void* mapped_range(const void* p, size_t bytes)
         cudaGetLastError();
         return nullptr;
     }
-    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer)
+    if (a.type != cudaMemoryTypeHost || b.type != cudaMemoryTypeHost || !a.devicePointer || !b.devicePointer ||
+        a.device != device || b.device != device)
         return nullptr;
     if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
         return nullptr;
@@ -322,8 +324,8 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
     cudaSetDevice(ctx->device);
     if (n == 0) return PICO_OK;
     {
-        const void* mr = mapped_range(rays, n * sizeof(pico_ray));
-        void* mh = mr ? mapped_range(hits, n * sizeof(pico_hit)) : nullptr;
+        const void* mr = mapped_range(rays, n * sizeof(pico_ray), ctx->device);
+        void* mh = mr ? mapped_range(hits, n * sizeof(pico_hit), ctx->device) : nullptr;
         if (mr && mh) {
             cudaError_t e = launch_trace(scene->view, static_cast<const pico_ray*>(mr), n, static_cast<pico_hit*>(mh),
                                          ctx->status, false, scene_order(ctx, scene), ctx->stream);
