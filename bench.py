@@ -1,23 +1,35 @@
-"""Benchmark: closest-hit traversal throughput (Mrays/s) on the instance-field workload.
+"""Benchmark: path-traced 1080p renders (Msamples/s, with Mrays/s beside it).
 
-Workload: 4096 instances of a level-4 icosphere (5120 triangles each, 21M
-triangles instanced) under random translation in [-50, 50]^3, log-uniform
-scale in [0.5, 4] and random rotation, as a two-level SAH BVH; 16,777,216 rays,
-half coherent primary rays of a 4096 x 4096 pinhole and half cosine-distributed
-rays leaving random surface points.  One step = one closest-hit pass
-(UpperLevelBVH::get_closest_intersection semantics) over the whole batch.
+Headline workload (the metric's own configuration): the lit field -- 4096
+instances of a level-4 icosphere (5120 triangles each) under random translation,
+log-uniform scale and random rotation, metalness-roughness materials, a ground
+quad and 8 quad area lights -- rendered at 1920 x 1080, 64 samples per pixel,
+path depth 8, a-trous denoised, with the reference's estimator
+(Monte_Carlo_Integrator, Render/Integrators.cpp:46-209, and the render loop of
+Scene::render_scene_to_memory, Core/Scene.cpp:143-235, early exit included).
+One step = one whole render of the image from cleared buffers.
 
-  value   rays/s with rays and hits resident in HBM (device-pointer entry point),
-          timed with CUDA events on the launching stream.
-  e2e     rays/s through the host-buffer entry point from pinned host memory:
-          every step moves the rays in and the hits out (page-locked buffers are
-          read and written in place by the kernel over the host link, others are
-          staged through device buffers in overlapped chunks).
+  value   samples/s with the scene and the image buffers in HBM
+          (pico_gpu_render_device), CUDA events on the launching stream.
+  e2e     samples/s through pico_gpu_render with pinned host buffers: every step
+          copies the progressive buffers in and the image, counts and variance out.
+  roofline  the closest-hit (extend) kernel, 90 % of a render's GPU time: its
+          algorithmic bytes (64 B per node visited, 48 B per triangle tested,
+          144 B per instance entry, 52 B of ray and hit per ray; counted by the
+          counting variant of the same launches on the same render) over its
+          launches' durations (CUDA events around every launch of the timed
+          renders), against the L2 read bandwidth measured in the same run (the
+          scene data stays in L2), with the fraction of HBM beside it.
   cpu_baseline / --impl reference
-          the reference algorithm on this machine's host cores: the reference's own
-          code when its harness is built here (oracle/_ref), else the oracle port.
+          the reference's render loop on this machine's host cores, on a seeded
+          subset of the same image's pixels: the reference's own code where its
+          harness is built here (oracle/_ref), else the oracle port.
 
-With --gpus N under torchrun each rank traces the full batch on its own GPU
+Secondary objects on the same line: the closest-hit microbench (16,777,216 rays on
+the instance field), the physical estimator at 1080p, the radiance-cache series,
+batched renders, the Cornell box, a-trous, tone map and .hdr output.
+
+With --gpus N under torchrun each rank renders the whole image on its own GPU
 (replicas: the path does not shard) and value is the sum over ranks.
 """
 from __future__ import annotations
@@ -60,7 +72,10 @@ def parse():
     ap.add_argument("--no-render", action="store_true", help="skip the 1080p render and a-trous measurements")
     ap.add_argument("--render-spp", type=int, default=64)
     ap.add_argument("--render-depth", type=int, default=8)
-    ap.add_argument("--render-cpu-pixels", type=int, default=8192)
+    ap.add_argument("--render-cpu-pixels", type=int, default=32768,
+                    help="seeded pixels of the 1080p image the CPU baseline renders")
+    ap.add_argument("--headline", choices=["render", "trace"], default="render",
+                    help="the line's headline: the 1080p render (default) or the closest-hit microbench")
     ap.add_argument("--nrc-passes", type=int, nargs="*", default=[16, 32, 64, 96, 128])
     ap.add_argument("--batch-renders", type=int, default=64, help="renders of the batched-rendering line (0: skip)")
     return ap.parse_args()
@@ -203,7 +218,7 @@ ATROUS_BYTES_PER_PIXEL_LEVEL = 60   # 4 x 12 B in (colour, normal, position, alb
 L2_FLUSH_BYTES = 512 << 20
 
 
-def bench_render(ctx, args, torch, local, estimator=0):
+def bench_render(ctx, args, torch, local, estimator=0, with_cpu=True):
     """1080p render of the lit field through pico_gpu_render (host buffers in and out, denoised):
     wall time per render, samples added and rays traced (camera, bounce, shadow, G-buffer).
     estimator 0 is the reference's estimator, 1 the physical one (NEE + BSDF sampling with MIS)."""
@@ -233,7 +248,7 @@ def bench_render(ctx, args, torch, local, estimator=0):
     conv = convergence(ctx, gs, scene, cam, args, pix, estimator)
     if conv:
         out["relmse"] = conv
-    if not args.no_cpu and args.render_cpu_pixels > 0 and estimator == 0:
+    if with_cpu and not args.no_cpu and args.render_cpu_pixels > 0 and estimator == 0:
         out["cpu_baseline"] = cpu_render(scene, cam, args)
     gs.free()
     return out
@@ -509,7 +524,8 @@ def cpu_render(scene, cam, args):
     samples = int(cnt.reshape(-1)[idx].sum())
     return {"value": samples / secs / 1e6, "unit": "Msamples/s", "cores": cores, "kind": kind,
             "sample": f"{len(idx)} seeded pixels of the 1920x1080 image, {args.render_spp} spp, "
-                      f"depth {args.render_depth}, no denoise"}
+                      f"depth {args.render_depth}, reference estimator with its early exit, no denoise",
+            "samples": samples, "seconds": secs}
 
 
 def bench_atrous(ctx, args, torch, local):
@@ -600,27 +616,277 @@ def atrous_traffic_per_call():
     return None
 
 
+RENDER_WORKLOAD = ("lit field: 4096 x level-4 icosphere (5120 tris each) with metalness-roughness materials, "
+                   "ground quad, 8 quad lights; 1920x1080, {spp} spp, depth {depth}, a-trous 5 levels; reference "
+                   "estimator (Integrators.cpp:46-209, Scene.cpp:143-235: zero-variance pixels stop after 5 samples)")
+
+
+def render_config(args, n_gpus):
+    return {"workload": RENDER_WORKLOAD.format(spp=args.render_spp, depth=args.render_depth),
+            "resolution": [1920, 1080], "spp": args.render_spp, "max_depth": args.render_depth,
+            "instances": 4096, "triangles_per_mesh": 5120, "lights": 8, "denoise": "a-trous 5 levels",
+            "seed": "fixed: every step renders the same seed from cleared buffers (identical work per step)",
+            "l2": "path state (2^24 paths x 224 B = 3.8 GB per batch) and image buffers (57 MB) exceed L2; "
+                  "the scene (1.5 MB) stays in L2 by design",
+            "parallelism": f"replicas x{n_gpus}"}
+
+
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU implementation on this machine's host cores (rank 0 only)."""
     if rank != 0:
         return
-    scene, rays = workload(args)
-    sample = cpu_sample(rays, args.cpu_sample)
-    times = []
-    kind = cores = None
+    if args.headline == "trace":
+        scene, rays = workload(args)
+        sample = cpu_sample(rays, args.cpu_sample)
+        times = []
+        kind = cores = None
+        for i in range(args.warmup + args.steps):
+            kind, secs, cores = cpu_trace(scene, sample)
+            if i >= args.warmup:
+                times.append(secs)
+        t = float(np.mean(times))
+        v = len(sample) / t / 1e6
+        line = {"metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
+                "config": config_of(args, args.gpus),
+                "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": kind,
+                                 "sample": f"{len(sample)} rays, every {len(rays) // len(sample)}th ray of the batch"},
+                "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+    scene = scenes.lit_field()
+    cam = scenes.lit_field_camera(1920, 1080)
+    runs = []
     for i in range(args.warmup + args.steps):
-        kind, secs, cores = cpu_trace(scene, sample)
+        r = cpu_render(scene, cam, args)
         if i >= args.warmup:
-            times.append(secs)
-    t = float(np.mean(times))
-    v = len(sample) / t / 1e6
-    line = {"metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+            runs.append(r)
+    secs = float(np.mean([r["seconds"] for r in runs]))
+    v = runs[-1]["samples"] / secs / 1e6
+    base = dict(runs[-1])
+    base.pop("seconds")
+    base["value"] = v
+    line = {"metric": "Msamples/s", "value": v, "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": secs * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "impl": "reference",
-            "config": config_of(args, args.gpus),
-            "cpu_baseline": {"value": v, "unit": "Mrays/s", "cores": cores, "kind": kind,
-                             "sample": f"{len(sample)} rays, every {len(rays) // len(sample)}th ray of the batch"},
-            "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": render_config(args, args.gpus), "cpu_baseline": base,
+            "e2e": {"value": v, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def l2_peak(ctx):
+    """L2 read bandwidth measured now (GB/s), the roof of the closest-hit kernels."""
+    return ctx.l2_read_bandwidth(32 << 20, 200)
+
+
+def extend_traffic_per_launch():
+    """DRAM bytes per closest-hit launch of the 1080p render, from an ncu capture of the same
+    render (profiles/extend_kernel_render_1080p.md), if recorded."""
+    p = ROOT / "profiles" / "extend_kernel_render_1080p.md"
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == "dram_bytes_per_launch":
+                return float(parts[1])
+    return None
+
+
+def bench_render_headline(ctx, args, torch, local, dist, world, l2_gbs):
+    """The headline: whole 1080p renders of the lit field (reference estimator, denoised) with the image
+    buffers in HBM (pico_gpu_render_device, CUDA events), then through pico_gpu_render with pinned host
+    buffers (e2e); the extend kernel's roofline from its counted work and its timed launches."""
+    scene = scenes.lit_field()
+    cam = scenes.lit_field_camera(1920, 1080)
+    W, H = cam.resolution
+    gs = ctx.upload(scene)
+    dev = f"cuda:{local}"
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_pix = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+    d_var = torch.zeros((H, W, 3), dtype=torch.float32, device=dev)
+    d_cnt = torch.zeros((H, W), dtype=torch.int32, device=dev)
+    seed, depth, spp = 1, args.render_depth, args.render_spp
+
+    # a fresh render needs cleared sample counts only: a pixel's mean and variance restart at
+    # its first sample (Scene.cpp:185-191)
+    def step():
+        d_cnt.zero_()
+        gs.render_device(cam, depth, spp, d_pix.data_ptr(), d_cnt.data_ptr(), d_var.data_ptr(), sh, seed=seed,
+                         denoise=True)
+
+    for _ in range(args.warmup):
+        step()
+    gs.check(sh)
+    # work of one render, counted by the counting variant of the same closest-hit launches
+    ctx.set_render_probe(count_work=True)
+    step()
+    gs.check(sh)
+    work = ctx.render_probe_read()
+    ctx.set_render_probe(time_extend=True)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        evs[0].record(stream)
+        for k in range(args.steps):
+            step()
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    gs.check(sh)
+    timing = ctx.render_probe_read()
+    ctx.set_render_probe()
+    st = ctx.render_stats()
+    total_ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), dist, dev)
+    ms = total_ms / args.steps
+    rays = st["camera_paths"] + st["bounce_rays"] + st["shadow_rays"] + st["gbuffer_rays"]
+    value = replica_throughput(st["samples"], world, ms / 1e3)
+
+    # end to end: pico_gpu_render with pinned host buffers in and out every step
+    h_pix = torch.zeros((H, W, 3), dtype=torch.float32).pin_memory()
+    h_var = torch.zeros((H, W, 3), dtype=torch.float32).pin_memory()
+    h_cnt = torch.zeros((H, W), dtype=torch.int32).pin_memory()
+    np_pix, np_var, np_cnt = h_pix.numpy(), h_var.numpy(), h_cnt.numpy().view(np.uint32)
+
+    def e2e_step():
+        np_cnt.fill(0)
+        gs.render(cam, depth, spp, seed=seed, pixels=np_pix, sample_count=np_cnt, variance=np_var, denoise=True,
+                  cancellable=False)
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
+    e2e_samples = ctx.render_stats()["samples"]
+    io_bytes = W * H * (12 + 12 + 4)
+    e2e = {"value": replica_throughput(e2e_samples, world, e2e_s), "unit": "Msamples/s",
+           "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes, "ms_per_step": e2e_s * 1e3,
+           "Mrays_per_s": replica_throughput(rays, world, e2e_s),
+           "transfer": "pico_gpu_render from pinned host buffers (mean, count, variance in; denoised image, "
+                       "count, variance out), wall clock per call"}
+
+    # roofline of the closest-hit kernel: counted bytes over the timed launches
+    launches = timing["launches"] // args.steps
+    traced = st["camera_paths"] + st["bounce_rays"] + st["shadow_rays"]
+    algo_render = (work["nodes"] * NODE_BYTES + work["tris"] * TRI_BYTES + work["instances"] * INST_BYTES
+                   + traced * (RAY_BYTES + HIT_BYTES))
+    algo_launch = algo_render / max(launches, 1)
+    launch_ms = timing["extend_ms"] / max(timing["launches"], 1)
+    achieved = algo_launch / (launch_ms / 1e3) / 1e9
+    hbm, hbm_src = measured_peaks()
+    roofline = {"bound": "l2", "achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
+                "peak_source": "measured in this run: L2 read bandwidth (pico_gpu_l2_read_bandwidth, 32 MiB "
+                               "buffer, loads cached in L2 only)",
+                "hbm_peak": hbm, "hbm_frac": achieved / hbm, "hbm_peak_source": hbm_src,
+                "traffic": extend_traffic_per_launch(),
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per extend launch of the same "
+                                  "render (profiles/extend_kernel_render_1080p.md)",
+                "kernel": "extend_kernel<near-first, 128 threads> (closest hit of path segments and shadow rays)",
+                "launches_per_render": launches, "ms_per_launch": launch_ms,
+                "extend_ms_per_render": timing["extend_ms"] / args.steps,
+                "extend_share_of_step": timing["extend_ms"] / args.steps / ms,
+                "algorithmic_bytes_per_launch": algo_launch,
+                "work_per_render": {"nodes": work["nodes"], "triangle_tests": work["tris"],
+                                    "instance_entries": work["instances"], "rays": traced},
+                "bytes_model": "64 B per node visited, 48 B per triangle tested, 144 B per instance entry, "
+                               "52 B of ray in / hit out per ray"}
+    batches = launches // (depth + 1) if launches else 0
+    kernels_per_render = 2 * launches + 3 * batches + 1 + (1 + 10)   # + prepare, G-buffer, a-trous
+    out = {"value": value, "ms_per_step": ms, "Mrays_per_s": replica_throughput(rays, world, ms / 1e3),
+           "samples_per_render": st["samples"], "rays_per_render": {k: st[k] for k in (
+               "camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
+           "e2e": e2e, "roofline": roofline, "clocks": clocks.summary(),
+           "gpu_launches": kernels_per_render * args.steps}
+    gs.free()
+    return out
+
+
+def bench_trace(ctx, args, torch, local, dist, world, l2_gbs):
+    """The closest-hit microbench on the instance field: 16,777,216 rays per step, device-resident and
+    end to end through the host-buffer entry point; roofline against the measured L2 bandwidth."""
+    scene, rays = workload(args)
+    n = len(rays)
+    ctx.set_traversal_order(args.order)
+    gs = ctx.upload(scene)
+    info = gs.info()
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    d_rays = torch.from_numpy(rays.view(np.uint8)).to(f"cuda:{local}")
+    d_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def step():
+        gs.trace_closest_device(d_rays.data_ptr(), n, d_hits.data_ptr(), sh)
+
+    for _ in range(args.warmup):
+        step()
+    gs.check(sh)
+    counts = gs.trace_stats(d_rays.data_ptr(), n, sh)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        evs[0].record(stream)
+        for k in range(args.steps):
+            step()
+            evs[k + 1].record(stream)
+        torch.cuda.synchronize()
+    gs.check(sh)
+    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
+    total_ms = max_over_ranks(evs[0].elapsed_time(evs[-1]), dist, f"cuda:{local}")
+    ms = total_ms / args.steps
+    value = replica_throughput(n, world, ms / 1e3)
+    e2e = None
+    if not args.no_e2e:
+        h_rays = torch.from_numpy(rays.view(np.uint8)).pin_memory()
+        h_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8).pin_memory()
+        in_place = ctx.host_buffer_in_place(h_rays.data_ptr(), n * RAY_BYTES) and \
+            ctx.host_buffer_in_place(h_hits.data_ptr(), n * HIT_BYTES)
+        for _ in range(max(1, min(args.warmup, 2))):
+            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, f"cuda:{local}")
+        e2e = {"value": replica_throughput(n, world, e2e_s), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
+               "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3,
+               "transfer": ("pinned buffers read and written in place by the kernel over NVLink-C2C" if in_place
+                            else "pinned buffers staged through device memory in overlapped 1M-ray chunks")}
+    algo_bytes = (counts["nodes"] * NODE_BYTES + counts["tris"] * TRI_BYTES + counts["instances"] * INST_BYTES
+                  + n * (RAY_BYTES + HIT_BYTES))
+    launch_s = float(np.mean(per_step)) / 1e3
+    achieved = algo_bytes / launch_s / 1e9
+    hbm, hbm_src = measured_peaks()
+    dpr = dram_traffic_per_ray()
+    roofline = {"bound": "l2", "achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
+                "peak_source": "measured in this run: L2 read bandwidth (pico_gpu_l2_read_bandwidth)",
+                "hbm_peak": hbm, "hbm_frac": achieved / hbm, "hbm_peak_source": hbm_src,
+                "traffic": dpr * n if dpr else None,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of trace_kernel on this "
+                                  "16,777,216-ray batch (profiles/trace_kernel_dram.txt)",
+                "kernel": f"trace_kernel<false, {'near-first' if args.order == 0 else 'reference order'}>",
+                "algorithmic_bytes_per_launch": algo_bytes,
+                "visits_per_ray": {k: v / n for k, v in counts.items()},
+                "bytes_model": "64 B per node visited, 48 B per triangle tested, 144 B per instance entry, "
+                               "32 B ray in + 20 B hit out per ray"}
+    cpu = None
+    if not args.no_cpu:
+        sample = cpu_sample(rays, args.cpu_sample)
+        kind, secs, cores = cpu_trace(scene, sample)
+        cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
+               "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
+    gs.free()
+    ctx.set_traversal_order(0)
+    return {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "ms_per_step": ms,
+            "config": config_of(args, world), "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clocks.summary(), "scene": info, "gpu_launches": args.steps}
 
 
 def main():
@@ -640,110 +906,49 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    scene, rays = workload(args)
-    n = len(rays)
     ctx = pico_gb300.Context(local)
-    ctx.set_traversal_order(args.order)
-    gs = ctx.upload(scene)
-    info = gs.info()
-
-    stream = torch.cuda.current_stream()
-    sh = stream.cuda_stream
-    d_rays = torch.from_numpy(rays.view(np.uint8)).to(f"cuda:{local}")
-    d_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
-
-    def step():
-        gs.trace_closest_device(d_rays.data_ptr(), n, d_hits.data_ptr(), sh)
-
-    for _ in range(args.warmup):
-        step()
-    gs.check(sh)
-    counts = gs.trace_stats(d_rays.data_ptr(), n, sh)
-
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    with ClockSampler(local) as clocks:
-        evs[0].record(stream)
-        for k in range(args.steps):
-            step()
-            evs[k + 1].record(stream)
-        torch.cuda.synchronize()
-    gs.check(sh)
-    per_step = [evs[k].elapsed_time(evs[k + 1]) for k in range(args.steps)]
-    total_ms = evs[0].elapsed_time(evs[-1])
-    total_ms = max_over_ranks(total_ms, dist, f"cuda:{local}")
-    if dist:
-        dist.barrier()
-    ms = total_ms / args.steps
-    value = replica_throughput(n, world, ms / 1e3)
-
-    # end to end from pinned host memory through the host-buffer entry point
-    e2e = None
-    if not args.no_e2e:
-        h_rays = torch.from_numpy(rays.view(np.uint8)).pin_memory()
-        h_hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8).pin_memory()
-        for _ in range(max(1, min(args.warmup, 2))):
-            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            gs.trace_closest_ptr(h_rays.data_ptr(), n, h_hits.data_ptr())
-        e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, dist, f"cuda:{local}")
-        e2e = {"value": replica_throughput(n, world, e2e_s), "unit": "Mrays/s", "h2d_bytes_per_step": n * RAY_BYTES,
-               "d2h_bytes_per_step": n * HIT_BYTES, "ms_per_step": e2e_s * 1e3,
-               "transfer": "pinned buffers read and written in place by the kernel over NVLink-C2C"}
-
+    l2_gbs = l2_peak(ctx)
+    trace = bench_trace(ctx, args, torch, local, dist, world, l2_gbs)
+    render = None
+    if args.headline == "render":
+        render = bench_render_headline(ctx, args, torch, local, dist, world, l2_gbs)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
 
-    algo_bytes = (counts["nodes"] * NODE_BYTES + counts["tris"] * TRI_BYTES + counts["instances"] * INST_BYTES
-                  + n * (RAY_BYTES + HIT_BYTES))
-    launch_s = float(np.mean(per_step)) / 1e3
-    achieved = algo_bytes / launch_s / 1e9
-    peak, peak_src = measured_peaks()
-    dpr = dram_traffic_per_ray()
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": dpr * n if dpr else None, "peak_source": peak_src,
-                "kernel": f"trace_kernel<false, {'near-first' if args.order == 0 else 'reference order'}>",
-                "algorithmic_bytes_per_launch": algo_bytes,
-                "visits_per_ray": {k: v / n for k, v in counts.items()},
-                "note": "scene (~1.3 MB) is L2-resident; algorithmic bytes count every node/triangle/instance "
-                        "fetch (64/48/144 B) plus ray in/hit out, so frac vs HBM can exceed 1"}
-
-    cpu = None
-    if not args.no_cpu:
-        sample = cpu_sample(rays, args.cpu_sample)
-        kind, secs, cores = cpu_trace(scene, sample)
-        cpu = {"value": len(sample) / secs / 1e6, "unit": "Mrays/s", "cores": cores, "kind": kind,
-               "sample": f"{len(sample)} rays, every {n // len(sample)}th ray of the batch"}
-
-    render = render_physical = atrous = tonemap = hdr = cache = batched = cornell = None
+    cpu_render_line = None
+    extras = {}
     if not args.no_render:
-        gs.free()
-        cornell = bench_cornell(ctx, args, local)
-        render = bench_render(ctx, args, torch, local)
-        render_physical = bench_render(ctx, args, torch, local, estimator=1)
+        scene = scenes.lit_field()
+        cam = scenes.lit_field_camera(1920, 1080)
+        if not args.no_cpu and args.render_cpu_pixels > 0:
+            r = cpu_render(scene, cam, args)
+            r.pop("seconds")
+            cpu_render_line = r
+        extras["cornell_256"] = bench_cornell(ctx, args, local)
+        extras["render_1080p_physical"] = bench_render(ctx, args, torch, local, estimator=1)
+        extras["render_1080p_relmse"] = bench_render(ctx, args, torch, local, estimator=0, with_cpu=False)
         if args.nrc_passes:
-            plain = (render_physical.get("relmse") or {}).get("plain_no_early_exit")
-            cache = bench_radiance_cache(ctx, args, torch, local, plain)
+            plain = (extras["render_1080p_physical"].get("relmse") or {}).get("plain_no_early_exit")
+            extras["render_1080p_radiance_cache"] = bench_radiance_cache(ctx, args, torch, local, plain)
         if args.batch_renders > 0:
-            batched = bench_batch(ctx, args, local)
-        atrous = bench_atrous(ctx, args, torch, local)
-        tonemap, hdr = bench_tonemap_and_hdr(ctx, args, torch, local)
+            extras["batched_renders"] = bench_batch(ctx, args, local)
+        extras["atrous_1080p"] = bench_atrous(ctx, args, torch, local)
+        extras["tonemap_1080p"], extras["hdr_1080p"] = bench_tonemap_and_hdr(ctx, args, torch, local)
 
-    line = {"metric": "Mrays/s", "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_of(args, world),
-            "e2e": e2e, "gpu_launches": args.steps, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clocks.summary(), "scene": info, "cornell_256": cornell, "render_1080p": render,
-            "render_1080p_physical": render_physical, "render_1080p_radiance_cache": cache,
-            "batched_renders": batched, "atrous_1080p": atrous,
-            "tonemap_1080p": tonemap, "hdr_1080p": hdr}
+    common = {"n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)"}
+    if render is not None:
+        line = {"metric": "Msamples/s", "value": render["value"], "unit": "Msamples/s", **common,
+                "ms_per_step": render["ms_per_step"], "Mrays_per_s": render["Mrays_per_s"],
+                "config": render_config(args, world), "e2e": render["e2e"],
+                "gpu_launches": render["gpu_launches"], "roofline": render["roofline"],
+                "cpu_baseline": cpu_render_line, "clocks": render["clocks"],
+                "samples_per_render": render["samples_per_render"], "rays_per_render": render["rays_per_render"],
+                "l2_read_gbs": l2_gbs, "traversal_microbench": trace, **extras}
+    else:
+        line = {**common, **trace, "l2_read_gbs": l2_gbs, **extras}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -199,12 +199,21 @@ void pico_gpu_scene_free(pico_gpu_scene* scene);
 int pico_gpu_scene_info(const pico_gpu_scene* scene, uint64_t* out6);
 
 /* ---- closest hit (UpperLevelBVH::get_closest_intersection) --------------- */
-/* rays / hits are host buffers.  When both are page-locked and mapped
- * (cudaHostAlloc, or cudaHostRegister under unified addressing) the kernel
- * reads and writes them in place (over NVLink-C2C on a Grace host), with no
- * staging copies; other buffers are staged through device memory in chunks. */
+/* rays / hits are host buffers.  When each lies inside one page-locked, mapped
+ * allocation (cudaHostAlloc, or one cudaHostRegister under unified addressing)
+ * the kernel reads and writes them in place (over NVLink-C2C on a Grace host),
+ * with no staging copies; other buffers are staged through device memory in
+ * chunks, and a buffer only partly inside page-locked memory through
+ * page-locked bounce buffers of the context (slower, chunk by chunk). */
 int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                            const pico_ray* rays, uint64_t n, pico_hit* hits);
+/* No counterpart in the reference: whether pico_gpu_trace_closest reads or
+ * writes the host range [p, p + bytes) in place (*in_place = 1) or stages it
+ * through device memory (0).  In place needs the whole range inside ONE
+ * page-locked allocation or registration that is mapped for the context's
+ * device; a range spanning several pinned regions is staged, since pageable
+ * memory may lie between them. */
+int pico_gpu_host_buffer_in_place(pico_gpu_ctx* ctx, const void* p, uint64_t bytes, int32_t* in_place);
 /* Device-pointer variant on a caller stream (cudaStream_t, NULL = legacy default). */
 int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                                   const pico_ray* d_rays, uint64_t n, pico_hit* d_hits,
@@ -218,18 +227,51 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                          const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
-/* The render runs in batches of up to 2^24 paths (pixels x samples; about 3.5 GB
- * of path state at the limit) and polls *should_quit between batches: a 1080p
- * render at 64 spp is eight batches of 8 samples per pixel, about 60 ms each
- * on a GB300, which bounds how soon a cancel is seen. */
+/* The render runs in batches of up to 2^24 paths (pixels x samples; 224 bytes of
+ * path state each, 3.8 GB at the limit).  With a cancel flag (should_quit not
+ * NULL) it polls *should_quit before every batch and a batch takes at most 16
+ * samples per pixel: a 1080p render at 64 spp is eight batches of 8 samples per
+ * pixel, about 30 ms each on a GB300, which bounds how soon a cancel is seen. */
 int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
                     const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
                     float* variance_rgb, const volatile int32_t* should_quit);
 /* Work of the context's last pico_gpu_render call: [0] samples added to the
  * image (the growth of sample_count), [1] camera paths traced (pixels past their
  * early exit trace none), [2] bounce rays, [3] next-event shadow rays,
- * [4] G-buffer primary rays (W*H when denoising, else 0). */
+ * [4] G-buffer primary rays (W*H when denoising, else 0).  After
+ * pico_gpu_render_device it first waits for that render's stream. */
 int pico_gpu_render_stats(const pico_gpu_ctx* ctx, uint64_t* out5);
+/* No counterpart in the reference, whose RenderParams buffers are host memory:
+ * pico_gpu_render on device buffers (d_pixels and d_variance W*H*3 floats,
+ * d_count W*H), enqueued on `stream` (cudaStream_t, NULL = legacy default)
+ * without waiting for it and without host copies: the same samples, denoise
+ * and tone map, so the same images as pico_gpu_render gives for the same
+ * inputs.  There is no cancel flag; the reference and physical estimators only.
+ * Traversal errors are latched like the other device-pointer calls and
+ * returned by pico_gpu_check(ctx, stream); pico_gpu_render_stats reports this
+ * render's work.  The buffers must not be touched until the stream reaches the
+ * end of the render. */
+int pico_gpu_render_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                           const pico_render_config* config, float* d_pixels, uint32_t* d_count,
+                           float* d_variance, void* stream);
+
+/* ---- measurement ---------------------------------------------------------------
+ * No counterpart in the reference, whose only profiler is a stub (Core/Profiler.hpp).
+ * pico_gpu_set_render_probe switches the hooks on the closest-hit launches of this
+ * context's renders (both off by default) and clears their totals: time_extend
+ * brackets every such launch with CUDA events on its stream; count_work runs a
+ * counting variant of the launches (the same traversal, 128-thread CTAs) that
+ * tallies the nodes visited, triangles tested and instance entries transformed.
+ * pico_gpu_render_probe_read waits for the device and returns the totals since:
+ * out4 = {launches timed, nodes, triangles, instance entries}, *extend_ms = the
+ * timed launches' summed duration. */
+int pico_gpu_set_render_probe(pico_gpu_ctx* ctx, int32_t time_extend, int32_t count_work);
+int pico_gpu_render_probe_read(pico_gpu_ctx* ctx, uint64_t* out4, double* extend_ms);
+/* The read bandwidth of the L2 cache (GB/s), the roof of the closest-hit kernels
+ * whose scene data stays in L2: one launch reads a device buffer of `bytes` bytes
+ * (0: 32 MiB, which the GB300's L2 holds) `passes` times (0: 100) with 16-byte
+ * loads cached in L2 only, after a warm-up pass; the best of five launches. */
+int pico_gpu_l2_read_bandwidth(pico_gpu_ctx* ctx, uint64_t bytes, uint32_t passes, double* gbs);
 
 /* ---- denoiser ------------------------------------------------------------ */
 int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
@@ -244,10 +286,11 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
  * must not allocate device memory during their denoise step: a frame loop that
  * overlaps streams (cudaFree, and often cudaMalloc, synchronises the whole
  * device) or a process whose device memory belongs to another allocator.  On
- * success it allocates nothing: its scratch is a fixed 48 MiB + 2.25 MiB device
+ * success it allocates nothing: its scratch is a fixed 48 MiB + 2 MiB device
  * array per device, so images are limited to 2,097,152 pixels (1920 x 1080
  * fits) and 65,535 rows; larger ones return PICO_ERR_INVALID_ARG with a
- * message.  All calls on a device share that array: calls that overlap on the
+ * message, and so does an output that overlaps an input.  The caller's current
+ * device is left as it was.  All calls on a device share that array: calls that overlap on the
  * GPU race, so order them on one stream.  Nothing in it has to start at zero.
  * The first call on a device looks up the array's address (set-up); make that
  * first call before any stream capture. */

@@ -23,7 +23,8 @@ from pico_gb300.types import HIT_DTYPE, RAY_DTYPE, CCamera, CMaterial, Marshalle
 HERE = Path(__file__).resolve().parent
 ORACLE_LIB = HERE / "_build" / "libpico_oracle.so"
 REF_LIB = HERE / "_ref" / "libpico_ref.so"
-REFERENCE_TREE = Path(os.environ.get("PICO_REFERENCE", "/root/reference"))
+# The Pico source tree the harness was built from, recorded by build_reference.
+REF_TREE_RECORD = HERE / "_ref" / "reference_tree.txt"
 
 FRAG_DTYPE = np.dtype([("inst", "<u4"), ("prim", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4"),
                        ("position", "<f4", (4,)), ("normal", "<f4", (3,)), ("uv", "<f4", (2,))])
@@ -38,13 +39,27 @@ def build_oracle() -> Path:
     return ORACLE_LIB
 
 
-def build_reference() -> Path | None:
-    """Compiles the reference harness when the Pico source tree is present."""
-    if not (REFERENCE_TREE / "Source" / "Core" / "BVH.cpp").exists():
+def build_reference(tree: str | os.PathLike | None = None) -> Path | None:
+    """Compiles the reference harness from the Pico source tree `tree` (default: the
+    PICO_REFERENCE environment variable); returns None when no tree is given or present.
+    The tree's path is recorded beside the library for the tests that compile against
+    the reference's headers."""
+    tree = tree or os.environ.get("PICO_REFERENCE")
+    if not tree or not (Path(tree) / "Source" / "Core" / "BVH.cpp").exists():
         return None
     jobs = str(os.cpu_count() or 4)
-    subprocess.run(["make", "-s", "-j", jobs, "-C", str(HERE), "ref", f"REF={REFERENCE_TREE}"], check=True)
+    subprocess.run(["make", "-s", "-j", jobs, "-C", str(HERE), "ref", f"REF={tree}"], check=True)
+    REF_TREE_RECORD.write_text(str(Path(tree).resolve()) + "\n")
     return REF_LIB
+
+
+def reference_tree() -> Path | None:
+    """The Pico source tree the reference harness was built from, if it is still there."""
+    if REF_TREE_RECORD.exists():
+        p = Path(REF_TREE_RECORD.read_text().strip())
+        if (p / "Source" / "Core" / "Scene.hpp").exists():
+            return p
+    return None
 
 
 def _mat(m: Material) -> CMaterial:

@@ -51,11 +51,17 @@ SIGNATURES = {
     "pico_gpu_scene_info": (C.c_int, [_vp, C.POINTER(_u64)]),
     "pico_gpu_trace_closest": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
     "pico_gpu_trace_closest_device": (C.c_int, [_vp, _vp, _vp, _u64, _vp, _vp]),
+    "pico_gpu_host_buffer_in_place": (C.c_int, [_vp, _vp, _u64, C.POINTER(_i32)]),
     "pico_gpu_check": (C.c_int, [_vp, _vp]),
     "pico_gpu_trace_stats": (C.c_int, [_vp, _vp, _vp, _u64, C.POINTER(_u64), _vp]),
     "pico_gpu_render": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _fp,
                                   C.POINTER(_u32), _fp, C.POINTER(_i32)]),
     "pico_gpu_render_stats": (C.c_int, [_vp, C.POINTER(_u64)]),
+    "pico_gpu_render_device": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _vp, _vp, _vp,
+                                         _vp]),
+    "pico_gpu_set_render_probe": (C.c_int, [_vp, _i32, _i32]),
+    "pico_gpu_render_probe_read": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(C.c_double)]),
+    "pico_gpu_l2_read_bandwidth": (C.c_int, [_vp, _u64, _u32, C.POINTER(C.c_double)]),
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
     "pico_gpu_atrous_device": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _u32, _u32, _vp, _vp]),
@@ -151,6 +157,32 @@ class Context:
     def set_traversal_order(self, order: int):
         """0: near-first (default), 1: the reference's child order (exact in near-tie cases)."""
         self.check(self.lib.pico_gpu_set_traversal_order(self.handle, order), "set_traversal_order")
+
+    def host_buffer_in_place(self, ptr: int, nbytes: int) -> bool:
+        """Whether trace_closest reads / writes the host range [ptr, ptr + nbytes) in place (it lies in one
+        page-locked, mapped allocation) rather than staging it through device memory."""
+        out = C.c_int32(0)
+        self.check(self.lib.pico_gpu_host_buffer_in_place(self.handle, ptr, nbytes, C.byref(out)),
+                   "host_buffer_in_place")
+        return bool(out.value)
+
+    def set_render_probe(self, time_extend: bool = False, count_work: bool = False):
+        """Measurement hooks on the closest-hit launches of renders (events / work counters); clears totals."""
+        self.check(self.lib.pico_gpu_set_render_probe(self.handle, int(time_extend), int(count_work)),
+                   "set_render_probe")
+
+    def render_probe_read(self) -> dict:
+        out = (C.c_uint64 * 4)()
+        ms = C.c_double(0.0)
+        self.check(self.lib.pico_gpu_render_probe_read(self.handle, out, C.byref(ms)), "render_probe_read")
+        return {"launches": int(out[0]), "nodes": int(out[1]), "tris": int(out[2]), "instances": int(out[3]),
+                "extend_ms": ms.value}
+
+    def l2_read_bandwidth(self, nbytes: int = 0, passes: int = 0) -> float:
+        """Measured L2 read bandwidth in GB/s (pico_gpu_l2_read_bandwidth)."""
+        g = C.c_double(0.0)
+        self.check(self.lib.pico_gpu_l2_read_bandwidth(self.handle, nbytes, passes, C.byref(g)), "l2_read_bandwidth")
+        return g.value
 
     def render_stats(self) -> dict:
         """Work of the last render: samples added, camera paths, bounce, shadow and G-buffer rays."""
@@ -342,9 +374,11 @@ class GpuScene:
 
     def render(self, camera: Camera, max_depth: int, max_samples: int, seed: int = 1, pixels=None,
                sample_count=None, variance=None, max_variance: float = 0.0, denoise: bool = False,
-               tonemap: bool = False, should_quit=None, estimator: int = 0):
+               tonemap: bool = False, should_quit=None, estimator: int = 0, cancellable: bool = True):
         """Scene::render_scene_to_memory into (H, W, 3) buffers that are updated in place;
-        estimator 1 (ESTIMATOR_PHYSICAL) selects the physical estimator of pico_gpu.h."""
+        estimator 1 (ESTIMATOR_PHYSICAL) selects the physical estimator of pico_gpu.h.
+        should_quit: a ctypes c_int32 the render polls (a zero flag of its own by default);
+        cancellable=False passes no flag (batches are then not limited to 16 samples per pixel)."""
         W, H = int(camera.resolution[0]), int(camera.resolution[1])
         if pixels is None:
             pixels = np.zeros((H, W, 3), np.float32)
@@ -358,8 +392,22 @@ class GpuScene:
         quit_flag = should_quit if should_quit is not None else C.c_int32(0)
         self.ctx.check(self.lib.pico_gpu_render(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),
                                                 _f32(pixels), sample_count.ctypes.data_as(C.POINTER(C.c_uint32)),
-                                                _f32(variance), C.byref(quit_flag)), "render")
+                                                _f32(variance), C.byref(quit_flag) if cancellable else None),
+                       "render")
         return pixels, sample_count, variance
+
+    def render_device(self, camera: Camera, max_depth: int, max_samples: int, d_pixels: int, d_count: int,
+                      d_variance: int, stream: int = 0, seed: int = 1, max_variance: float = 0.0,
+                      denoise: bool = False, tonemap: bool = False, estimator: int = 0):
+        """pico_gpu_render_device: the render on caller device buffers (pointers as ints: W*H*3 floats,
+        W*H uint32, W*H*3 floats), enqueued on `stream` without waiting for it."""
+        W, H = int(camera.resolution[0]), int(camera.resolution[1])
+        cfg = CRenderConfig(max_depth, max_samples, max_variance, H, W, int(tonemap), int(denoise), int(estimator),
+                            seed)
+        cam = camera.to_c()
+        self.ctx.check(self.lib.pico_gpu_render_device(self.ctx.handle, self.handle, C.byref(cam), C.byref(cfg),
+                                                       d_pixels, d_count, d_variance, stream or None),
+                       "render_device")
 
     def render_to_file(self, camera: Camera, max_depth: int, max_samples: int, path, seed: int = 1,
                        pixels=None, sample_count=None, variance=None, denoise: bool = False, tonemap: bool = False):

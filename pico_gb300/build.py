@@ -25,7 +25,7 @@ LIB = BUILD / "libpico_gpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["scene_build.cpp", "capi.cpp", "render.cpp", "trace.cu", "integrator.cu", "atrous.cu",
-           "bsdf_eval.cu", "output.cu", "atrous_noalloc.cu", "nrc.cu", "nrc_api.cpp", "batch.cpp"]
+           "bsdf_eval.cu", "output.cu", "atrous_noalloc.cu", "nrc.cu", "nrc_api.cpp", "batch.cpp", "probe.cu"]
 
 
 def nvcc_path() -> str:

@@ -17,7 +17,9 @@
 //   * at most kNoAllocMaxPixels = 2,097,152 pixels (1920 x 1080 fits) and
 //     65,535 rows per call; larger images are rejected with
 //     PICO_ERR_INVALID_ARG and a message in the context, before any launch;
-//   * the array takes 48 MiB + 2.25 MiB of device memory on each device;
+//   * the array takes 48 MiB + 2 MiB of device memory on each device;
+//   * the output must not overlap any input (the last level writes it while it
+//     still reads the colour and the G-buffer): rejected with PICO_ERR_INVALID_ARG;
 //   * every call on a device shares that one array, so calls whose kernels
 //     overlap on the GPU (different streams, or different host threads) race
 //     and corrupt each other's output: order them on one stream or with events;
@@ -36,7 +38,12 @@ namespace {
 
 constexpr size_t kNoAllocMaxPixels = size_t(1) << 21;
 constexpr uint32_t kNoAllocMaxRows = 65535;            // the blend kernel's grid.y
-constexpr size_t kNoAllocMaxTiles = 36864;             // 64 x 64 tiles; 2^21 pixels need at most 32,768
+// 64 x 64 statistics tiles: ceil(W / 64) * ceil(H / 64).  An image of at most 2^21
+// pixels in at most 64 rows has one tile row of at most 2^21 / 64 tiles (a single
+// row of 2^21 pixels is the worst case); from 65 rows on it has at most 2^21 / 65
+// columns, so at most 505 tiles per tile row and far fewer than 2^15 in all.
+constexpr size_t kNoAllocMaxTiles = kNoAllocMaxPixels / 64;
+static_assert(kNoAllocMaxTiles == 32768, "statistics region of 2 MiB");
 constexpr size_t kNoAllocImageFloats = 3 * kNoAllocMaxPixels;
 constexpr size_t kNoAllocFloats = 2 * kNoAllocImageFloats + pico::kAtrousStatsFloatsPerTile * kNoAllocMaxTiles;
 constexpr int kNoAllocMaxDevices = 64;
@@ -80,13 +87,14 @@ extern "C" int pico_gpu_atrous_device_noalloc(pico_gpu_ctx* ctx, const float* d_
 {
     if (!ctx || !d_pixels || !d_normals || !d_positions || !d_diffuse || !d_out)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    if (d_out == d_pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "output must not alias the input");
     const size_t npx = (size_t)width * height;
     const size_t tiles = (size_t)((width + 63) / 64) * ((height + 63) / 64);
     if (npx > kNoAllocMaxPixels || height > kNoAllocMaxRows || tiles > kNoAllocMaxTiles)
         return set_error(ctx, PICO_ERR_INVALID_ARG,
                          "a-trous without allocation: the image exceeds the fixed scratch "
                          "(at most 2,097,152 pixels and 65,535 rows)");
+    if (atrous_output_aliases(d_out, d_pixels, d_normals, d_positions, d_diffuse, 3 * npx))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "the output must not overlap an input");
     if (npx == 0) return PICO_OK;
     if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "a-trous without allocation: device index above 63");

@@ -4,10 +4,12 @@
 // Every render gets an image slot (its progressive buffers and active-pixel
 // list).  Its active pixels are split into pieces of disjoint pixel ranges
 // (one piece unless the render has more than piece_paths paths), and every
-// piece gets a path slot of its own (path state of at most `wavefront` paths,
-// device status block).  Each piece's batches are captured, without host
-// synchronisation, on one of `branches` streams forked from the context's
-// stream (placed by estimated cost: schedule()); the captured graph is
+// piece gets a device status block of its own.  Each piece's batches are
+// captured, without host synchronisation, on one of `branches` streams forked
+// from the context's stream (placed by estimated cost: schedule()); the pieces
+// of one branch run one after another, so each branch has one path slot (path
+// state of at most `wavefront` paths) that its pieces reuse in turn, and the path
+// state grows with the branches, not with the renders.  The captured graph is
 // instantiated and launched once.  Small renders cannot fill 152 SMs on their
 // own, and one large render would otherwise run alone at the end: side by side
 // their persistent closest-hit grids and shade kernels share the GPU.  Pieces of
@@ -36,7 +38,8 @@ struct BatchSlot {
 
 struct BatchState {
     std::vector<std::unique_ptr<BatchSlot>> images;   // per render: progressive buffers, pixel list
-    std::vector<std::unique_ptr<BatchSlot>> pieces;   // per piece: path state and status
+    std::vector<std::unique_ptr<BatchSlot>> pieces;   // per piece: status block
+    std::vector<std::unique_ptr<RenderBuffers>> paths;   // per branch: path state its pieces reuse in turn
     std::vector<cudaStream_t> streams;
     unsigned long long* stamps = nullptr;              // [0] graph start, [1 + j] end of piece j
     size_t stamp_cap = 0;
@@ -44,6 +47,7 @@ struct BatchState {
     {
         images.clear();
         pieces.clear();
+        paths.clear();
         for (cudaStream_t s : streams) cudaStreamDestroy(s);
         if (stamps) cudaFree(stamps);
     }
@@ -141,6 +145,7 @@ cudaError_t ensure_state(pico_gpu_ctx* ctx, uint32_t nrenders, size_t npieces, u
     BatchState& bs = *ctx->batch;
     cudaError_t e = grow(bs.images, nrenders);
     if (e == cudaSuccess) e = grow(bs.pieces, npieces);
+    while (bs.paths.size() < branches) bs.paths.push_back(std::make_unique<RenderBuffers>());
     while (e == cudaSuccess && bs.streams.size() < branches) {
         cudaStream_t s = nullptr;
         e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
@@ -269,9 +274,10 @@ std::vector<int> piece_priorities(const std::vector<double>& cost, int least, in
 }
 
 // A piece's batches on stream st, without synchronisation (they are captured):
-// path state from the piece's slot, pixels and progressive buffers from the render's.
-cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& image, BatchSlot& path,
-                    const Params& p, const Prepared& pr, const Piece& pc, cudaStream_t st)
+// path state from its branch's slot, status from the piece's, pixels and
+// progressive buffers from the render's.
+cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& image, RenderBuffers& paths,
+                    DeviceStatus* status, const Params& p, const Prepared& pr, const Piece& pc, cudaStream_t st)
 {
     const pico_render_config& cfg = it.config;
     const int order = scene_order(ctx, it.scene);
@@ -280,7 +286,7 @@ cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& im
         const uint32_t npix = (uint32_t)std::min<size_t>(pc.chunk_pix, pc.p1 - q0);
         for (uint32_t s0 = 0; s0 < cfg.max_samples && e == cudaSuccess; s0 += pc.spb_max) {
             const uint32_t spb = std::min(pc.spb_max, cfg.max_samples - s0);
-            PathBatch b = make_batch(path.r, npix * spb, npix, pr.W, as<uint32_t>(image.r.pix_list) + q0);
+            PathBatch b = make_batch(paths, npix * spb, npix, pr.W, as<uint32_t>(image.r.pix_list) + q0);
             b.pixels = as<float>(image.r.pixels);
             b.variance = as<float>(image.r.variance);
             b.count = as<uint32_t>(image.r.count);
@@ -289,7 +295,7 @@ cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& im
             b.extend_ctas = p.extend_ctas;
             b.extend_threads = p.extend_threads;
             e = launch_render_batch(it.scene->view, b, pr.cam, cfg.seed, spb, cfg.max_ray_depth, cfg.max_samples,
-                                    cfg.max_variance, (int)cfg.estimator, path.status, order, st);
+                                    cfg.max_variance, (int)cfg.estimator, status, order, st);
         }
     }
     return e;
@@ -313,12 +319,34 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     p.branches = (uint32_t)std::max<size_t>(
         1, std::min<size_t>({p.branches ? (size_t)p.branches : np, np, (size_t)work_queues()}));
     e = ensure_state(ctx, n, np, p.branches);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "batch state");
     BatchState& bs = *ctx->batch;
-    for (size_t j = 0; j < np && e == cudaSuccess; ++j) {
-        BatchSlot& ps = *bs.pieces[j];
-        e = reserve_paths(ps.r, (size_t)pieces[j].chunk_pix * pieces[j].spb_max);
-        if (e == cudaSuccess) e = cudaMemsetAsync(ps.status, 0, sizeof(DeviceStatus), st);
+    const std::vector<double> cost = piece_costs(pieces, items);
+    const std::vector<std::vector<size_t>> lanes = schedule(cost, p.branches);
+    // one path slot per branch, sized for the largest batch of its pieces
+    std::vector<size_t> lane_paths(p.branches, 0);
+    size_t total_paths = 0;
+    for (uint32_t k = 0; k < p.branches; ++k) {
+        for (size_t j : lanes[k])
+            lane_paths[k] = std::max(lane_paths[k], (size_t)pieces[j].chunk_pix * pieces[j].spb_max);
+        total_paths += lane_paths[k];
     }
+    {
+        size_t free_b = 0, total_b = 0, held = 0;
+        for (uint32_t k = 0; k < p.branches; ++k) held += bs.paths[k]->org.cap / sizeof(float4) * kPathStateBytes;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && total_paths * kPathStateBytes > free_b + held)
+            return set_error(ctx, PICO_ERR_OUT_OF_MEMORY,
+                             "batch path state: " + std::to_string(p.branches) + " branches of up to " +
+                                 std::to_string(p.wavefront) + " paths need " +
+                                 std::to_string(total_paths * kPathStateBytes >> 20) + " MiB, " +
+                                 std::to_string((free_b + held) >> 20) + " MiB available; lower the wavefront "
+                                 "or the branches");
+        cudaGetLastError();
+    }
+    for (uint32_t k = 0; k < p.branches && e == cudaSuccess; ++k)
+        if (lane_paths[k]) e = reserve_paths(*bs.paths[k], lane_paths[k]);
+    for (size_t j = 0; j < np && e == cudaSuccess; ++j)
+        e = cudaMemsetAsync(bs.pieces[j]->status, 0, sizeof(DeviceStatus), st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "batch path state");
 
@@ -343,8 +371,6 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
     cudaError_t ce = launch_stamp(bs.stamps, st);
     if (ce == cudaSuccess) ce = cudaEventRecord(events[0], st);
     for (uint32_t k = 0; k < p.branches && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(bs.streams[k], events[0], 0);
-    const std::vector<double> cost = piece_costs(pieces, items);
-    const std::vector<std::vector<size_t>> lanes = schedule(cost, p.branches);
     int least = 0, greatest = 0;
     if (ce == cudaSuccess) ce = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     const std::vector<int> prio = piece_priorities(cost, least, greatest);
@@ -355,8 +381,8 @@ int run_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items, cons
             pv.priority = prio[j];
             ce = cudaStreamSetAttribute(bs.streams[k], cudaStreamAttributePriority, &pv);
             if (ce == cudaSuccess)
-                ce = enqueue(ctx, items[pc.render], *bs.images[pc.render], *bs.pieces[j], p, prep[pc.render], pc,
-                             bs.streams[k]);
+                ce = enqueue(ctx, items[pc.render], *bs.images[pc.render], *bs.paths[k], bs.pieces[j]->status, p,
+                             prep[pc.render], pc, bs.streams[k]);
             if (ce == cudaSuccess) ce = launch_stamp(bs.stamps + 1 + j, bs.streams[k]);
             if (ce != cudaSuccess) break;
         }
@@ -437,7 +463,7 @@ int pico_gpu_render_many(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* 
     if (status != PICO_OK) return status;
     if (report) *report = pico_batch_report{};
     if (n == 0) return PICO_OK;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     return run_batch(ctx, n, items, resolve(params), completion_ms, report);
 }
 
@@ -451,7 +477,7 @@ int pico_gpu_autotune_batch(pico_gpu_ctx* ctx, uint32_t n, const pico_render_ite
     if (ntrials) *ntrials = 0;
     *best = pico_launch_params{};
     if (n == 0) return PICO_OK;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     // short renders of the same items into scratch buffers: the item with the most
     // samples per pixel takes trial_samples, the others the same fraction of theirs
     // (at least 1), so that the trials keep the batch's balance of work

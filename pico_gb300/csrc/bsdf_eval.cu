@@ -76,7 +76,7 @@ extern "C" int pico_gpu_phys_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint
     for (uint64_t i = 0; i < n; ++i)
         if (kinds[i] != PICO_BSDF_DIFFUSE && kinds[i] != PICO_BSDF_SPECULAR && kinds[i] != PICO_BSDF_DIELECTRIC)
             return set_error(ctx, PICO_ERR_INVALID_ARG, "the physical BSDF covers Diffuse, Specular and Dielectric");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     std::vector<GpuMaterial> gm(n);
     for (uint64_t i = 0; i < n; ++i) {
         GpuMaterial g{};
@@ -119,7 +119,7 @@ extern "C" int pico_gpu_bsdf_eval(pico_gpu_ctx* ctx, uint64_t n, const uint32_t*
     if (!ctx || (n && (!kinds || !mats || !V || !N || !H || !xi || !pdf || !L || !P || !energy || !direct_pdf)))
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (n == 0) return PICO_OK;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     std::vector<GpuMaterial> gm(n);
     for (uint64_t i = 0; i < n; ++i) {
         const pico_material& m = mats[i];

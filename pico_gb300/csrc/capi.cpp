@@ -2,6 +2,8 @@
 // the closest-hit entry points.  Rendering and denoising live in render.cpp.
 #include "capi_internal.h"
 
+#include <cuda.h>   // driver types for cuPointerGetAttribute (resolved at run time, not linked)
+
 #include <cstring>
 #include <new>
 
@@ -17,6 +19,7 @@ int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg)
 
 int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what)
 {
+    cudaGetLastError();   // a failed call's (non-sticky) error is reported here, not to the caller's next CUDA call
     if (e == cudaErrorMemoryAllocation)
         return set_error(ctx, PICO_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
     return set_error(ctx, PICO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
@@ -68,7 +71,8 @@ int pico_gpu_init(int device, pico_gpu_ctx** out)
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return PICO_ERR_NO_DEVICE;
     if (device < 0 || device >= count) return PICO_ERR_INVALID_ARG;
-    if (cudaSetDevice(device) != cudaSuccess) return PICO_ERR_CUDA;
+    const DeviceScope device_scope(device);
+    if (device_scope.status != cudaSuccess) return PICO_ERR_CUDA;
     auto* ctx = new (std::nothrow) pico_gpu_ctx();
     if (!ctx) return PICO_ERR_OUT_OF_MEMORY;
     ctx->device = device;
@@ -87,8 +91,10 @@ int pico_gpu_init(int device, pico_gpu_ctx** out)
 void pico_gpu_shutdown(pico_gpu_ctx* ctx)
 {
     if (!ctx) return;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     for (DeviceBuffer* b : {&ctx->buf_a, &ctx->buf_b, &ctx->buf_c, &ctx->buf_d, &ctx->buf_e}) b->release();
+    if (ctx->bounce_in) cudaFreeHost(ctx->bounce_in);
+    if (ctx->bounce_out) cudaFreeHost(ctx->bounce_out);
     free_render_buffers(ctx);
     free_batch_state(ctx);
     if (ctx->status) cudaFree(ctx->status);
@@ -127,7 +133,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
 {
     if (!ctx || !desc || !out) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     *out = nullptr;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     FlatScene fs;
     const std::string why = build_flat_scene(*desc, fs);
     if (!why.empty()) {
@@ -234,7 +240,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
 void pico_gpu_scene_free(pico_gpu_scene* s)
 {
     if (!s) return;
-    if (s->ctx) cudaSetDevice(s->ctx->device);
+    const DeviceScope device_scope(s->ctx ? s->ctx->device : -1);
     for (void* p : s->allocations) cudaFree(p);
     delete s;
 }
@@ -251,6 +257,7 @@ int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene
 {
     if (!ctx || !scene || (n && (!d_rays || !d_hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return set_error(ctx, PICO_ERR_INVALID_ARG, "rays not 16-byte aligned");
+    const DeviceScope device_scope(ctx->device);
     const cudaError_t e = launch_trace(scene->view, d_rays, n, d_hits, ctx->status, false,
                                        scene_order(ctx, scene), static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_error(ctx, e, "trace launch");
@@ -260,7 +267,7 @@ int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene
 int pico_gpu_check(pico_gpu_ctx* ctx, void* stream)
 {
     if (!ctx) return PICO_ERR_INVALID_ARG;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     const cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_error(ctx, e, "stream");
     return take_device_status(ctx, static_cast<cudaStream_t>(stream));
@@ -270,6 +277,7 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
                          uint64_t* out3, void* stream)
 {
     if (!ctx || !scene || !out3 || (n && !d_rays)) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = ctx->buf_e.reserve(sizeof(pico_hit) * (n ? n : 1));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->counters, 0, sizeof(ctx->status->counters), st);
@@ -287,11 +295,48 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
 
 namespace {
 
-// The device address of [p, p + bytes) when both of its ends lie in page-locked
-// host memory mapped into `device`'s address space (cudaHostAlloc, or
-// cudaHostRegister under unified addressing, pinned against that device) at one
-// linear offset; null for pageable memory and for memory pinned against another
-// device, which the kernels never touch.
+// cuPointerGetAttribute, resolved through the runtime (the library does not link
+// the driver library itself); null where the driver does not provide it.
+using PointerAttributeFn = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+PointerAttributeFn pointer_attribute_fn()
+{
+    static PointerAttributeFn fn = []() -> PointerAttributeFn {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return reinterpret_cast<PointerAttributeFn>(f);
+    }();
+    return fn;
+}
+
+// The address range [start, start + size) of the allocation (or registration) that
+// holds p, as the driver reports it; false when it reports none.
+bool allocation_range(const void* p, uintptr_t& start, size_t& size)
+{
+    const PointerAttributeFn fn = pointer_attribute_fn();
+    if (!fn) return false;
+    CUdeviceptr s = 0;
+    size_t n = 0;
+    const CUdeviceptr dp = static_cast<CUdeviceptr>(reinterpret_cast<uintptr_t>(p));
+    if (fn(&s, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, dp) != CUDA_SUCCESS ||
+        fn(&n, CU_POINTER_ATTRIBUTE_RANGE_SIZE, dp) != CUDA_SUCCESS || n == 0)
+        return false;
+    start = static_cast<uintptr_t>(s);
+    size = n;
+    return true;
+}
+
+// The device address of [p, p + bytes) when the whole range lies in ONE page-locked
+// host allocation mapped into `device`'s address space (cudaHostAlloc, or one
+// cudaHostRegister under unified addressing, pinned against that device); null
+// otherwise: pageable memory, memory pinned against another device, and ranges
+// that span several pinned regions (pageable memory may lie between them), which
+// the kernels never touch.
 void* mapped_range(const void* p, size_t bytes, int device)
 {
     cudaPointerAttributes a{}, b{};
@@ -305,10 +350,74 @@ void* mapped_range(const void* p, size_t bytes, int device)
         return nullptr;
     if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
         return nullptr;
+    uintptr_t start = 0;
+    size_t size = 0;
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(p);
+    if (!allocation_range(p, start, size) || lo < start || lo - start > size || bytes > size - (lo - start))
+        return nullptr;
     return a.devicePointer;
 }
 
+// Whether either end of [p, p + bytes) lies in page-locked host memory.
+bool pinned_end(const void* p, size_t bytes)
+{
+    for (const void* q : {p, static_cast<const void*>(static_cast<const char*>(p) + (bytes - 1))}) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            continue;
+        }
+        if (a.type == cudaMemoryTypeHost) return true;
+    }
+    return false;
+}
+
+// Host-buffer closest hit for ranges that are only partly page-locked (an end in a
+// pinned region, the rest not inside it): the copy engine accepts such a range
+// neither as pinned nor as pageable memory, so each chunk is copied on the host
+// into page-locked bounce buffers of the context and moved from there; chunk by
+// chunk on one stream.
+int trace_via_bounce(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_ray* rays, uint64_t n, pico_hit* hits)
+{
+    const uint64_t chunk = n < (1ull << 20) ? n : (1ull << 20);
+    cudaError_t e = cudaSuccess;
+    if (ctx->bounce_rays < chunk) {
+        if (ctx->bounce_in) cudaFreeHost(ctx->bounce_in);
+        if (ctx->bounce_out) cudaFreeHost(ctx->bounce_out);
+        ctx->bounce_in = ctx->bounce_out = nullptr;
+        ctx->bounce_rays = 0;
+        e = cudaHostAlloc(&ctx->bounce_in, chunk * sizeof(pico_ray), cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaHostAlloc(&ctx->bounce_out, chunk * sizeof(pico_hit), cudaHostAllocDefault);
+        if (e == cudaSuccess) ctx->bounce_rays = chunk;
+    }
+    if (e == cudaSuccess) e = ctx->buf_a.reserve(chunk * sizeof(pico_ray));
+    if (e == cudaSuccess) e = ctx->buf_c.reserve(chunk * sizeof(pico_hit));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "bounce buffers");
+    cudaStream_t st = ctx->stream;
+    pico_ray* dr = static_cast<pico_ray*>(ctx->buf_a.ptr);
+    pico_hit* dh = static_cast<pico_hit*>(ctx->buf_c.ptr);
+    for (uint64_t off = 0; off < n && e == cudaSuccess; off += chunk) {
+        const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
+        std::memcpy(ctx->bounce_in, rays + off, m * sizeof(pico_ray));
+        e = cudaMemcpyAsync(dr, ctx->bounce_in, m * sizeof(pico_ray), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = launch_trace(scene->view, dr, m, dh, ctx->status, false, scene_order(ctx, scene), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->bounce_out, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) std::memcpy(hits + off, ctx->bounce_out, m * sizeof(pico_hit));
+    }
+    if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
+    return take_device_status(ctx, st);
+}
+
 }  // namespace
+
+extern "C" int pico_gpu_host_buffer_in_place(pico_gpu_ctx* ctx, const void* p, uint64_t bytes, int32_t* in_place)
+{
+    if (!ctx || !in_place || (bytes && !p)) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    const DeviceScope device_scope(ctx->device);
+    *in_place = (bytes && mapped_range(p, (size_t)bytes, ctx->device)) ? 1 : 0;
+    return PICO_OK;
+}
 
 extern "C" {
 
@@ -321,11 +430,12 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
                            pico_hit* hits)
 {
     if (!ctx || !scene || (n && (!rays || !hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     if (n == 0) return PICO_OK;
     {
-        const void* mr = mapped_range(rays, n * sizeof(pico_ray), ctx->device);
-        void* mh = mr ? mapped_range(hits, n * sizeof(pico_hit), ctx->device) : nullptr;
+        const size_t rb = n * sizeof(pico_ray), hb = n * sizeof(pico_hit);
+        const void* mr = mapped_range(rays, rb, ctx->device);
+        void* mh = mapped_range(hits, hb, ctx->device);
         if (mr && mh) {
             cudaError_t e = launch_trace(scene->view, static_cast<const pico_ray*>(mr), n, static_cast<pico_hit*>(mh),
                                          ctx->status, false, scene_order(ctx, scene), ctx->stream);
@@ -333,6 +443,7 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
             if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
             return take_device_status(ctx, ctx->stream);
         }
+        if ((!mr && pinned_end(rays, rb)) || (!mh && pinned_end(hits, hb))) return trace_via_bounce(ctx, scene, rays, n, hits);
     }
     // 1M-ray chunks alternate between two streams: each chunk's copies overlap the
     // other stream's traversal, and only the first upload and the last download
@@ -360,17 +471,17 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
     if (e == cudaSuccess) e = cudaStreamSynchronize(streams[0]);
     if (e == cudaSuccess) e = cudaStreamSynchronize(streams[1]);
     if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
-    int st = take_device_status(ctx, ctx->stream);
-    if (st == PICO_OK) {
-        int err2 = 0;
-        e = cudaMemcpy(&err2, &ctx->status2()->trace_error, sizeof(int), cudaMemcpyDeviceToHost);
-        if (e != cudaSuccess) return cuda_error(ctx, e, "status read");
-        if (err2) {
-            cudaMemset(&ctx->status2()->trace_error, 0, sizeof(int));
-            st = set_error(ctx, (err2 & kTraceStackOverflow) ? PICO_ERR_STACK_OVERFLOW : PICO_ERR_TIMEOUT,
-                           "traversal error");
-        }
-    }
+    // both streams' latched statuses are read and cleared, whatever the first holds,
+    // so that no error of this call is left for the next one to report
+    int err2 = 0;
+    e = cudaMemcpy(&err2, &ctx->status2()->trace_error, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && err2) e = cudaMemset(&ctx->status2()->trace_error, 0, sizeof(int));
+    const int st = take_device_status(ctx, ctx->stream);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "status read");
+    if (st == PICO_OK && err2)
+        return set_error(ctx, (err2 & kTraceStackOverflow) ? PICO_ERR_STACK_OVERFLOW : PICO_ERR_TIMEOUT,
+                         (err2 & kTraceStackOverflow) ? "a ray exceeded the traversal stack"
+                                                      : "a traversal exceeded its iteration bound");
     return st;
 }
 

@@ -114,13 +114,16 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 // (they write disjoint path fields and both finish before the next shade), so a
 // depth pays one launch and one tail.  kThreads per CTA (64, 128 or 256): the
 // block shape batched renders tune; the register budget is the same 896 threads
-// per SM for every shape.
-template <int kOrder, int kThreads>
+// per SM for every shape.  kCount: the same traversal, also adding its work
+// (nodes, triangles, instance entries) to `counters` (measurement only).
+template <int kOrder, int kThreads, bool kCount = false>
 __global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneView sc, PathBatch b, const uint32_t* q,
                                                        const uint32_t* count, const uint32_t* sq,
                                                        const uint32_t* scount, unsigned long long* work, int* err,
-                                                       unsigned long long* tally, unsigned long long* stally)
+                                                       unsigned long long* tally, unsigned long long* stally,
+                                                       unsigned long long* counters)
 {
+    TraceCounters cnt{0, 0, 0, 0};
     const unsigned lane = threadIdx.x & 31u;
     const uint32_t n0 = *count, n1 = sq ? *scount : 0u;
     const uint64_t n = (uint64_t)n0 + n1;
@@ -141,7 +144,7 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneV
                 // physical estimator: an occlusion query bounded by the light sample's distance
                 const float4 c = b.scontrib[i];
                 bool occluded = true;
-                const int s = trace_occluded<kOrder>(sc, b.sorg[i], b.sdir[i], c.w, occluded);
+                const int s = trace_occluded<kOrder, kCount>(sc, b.sorg[i], b.sdir[i], c.w, occluded, &cnt);
                 if (s != kTraceOk) atomicOr(err, s);
                 if (s == kTraceOk && !occluded) {
                     float4 p = b.pay[i];
@@ -150,13 +153,14 @@ __global__ void __launch_bounds__(kThreads, 896 / kThreads) extend_kernel(SceneV
                 }
             } else {
                 TraceHit h;
-                const int s = trace_closest<false, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
-                                                           shadow ? b.sdir[i] : b.dir[i], h, nullptr);
+                const int s = trace_closest<kCount, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
+                                                            shadow ? b.sdir[i] : b.dir[i], h, &cnt);
                 if (s != kTraceOk) atomicOr(err, s);
                 extend_finish(sc, b, i, h, s, shadow);
             }
         }
     }
+    if (kCount) flush_counters(cnt, counters);
 }
 
 __global__ void __launch_bounds__(kRenderThreads) shade_kernel(SceneView sc, PathBatch b, int cur, uint32_t depth,
@@ -608,6 +612,7 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         float* var = b.variance + 3 * (size_t)pixel;
         uint32_t cnt = b.count[pixel];
         uint32_t taken = b.taken[pixel];
+        const uint32_t taken0 = taken;
         for (uint32_t s = 0; s < spb && taken < max_samples; ++s) {
             const float4 x4 = b.samples[(size_t)s * b.npix + slot];
             float x[3] = {x4.x, x4.y, x4.z};
@@ -637,6 +642,19 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         if (taken >= max_samples) b.done[pixel] = 1;
         b.count[pixel] = cnt;
         b.taken[pixel] = taken;
+        if (b.sample_tally) atomicAdd(b.sample_tally, (unsigned long long)(taken - taken0));
+    }
+}
+
+// The image state of a render into caller buffers (pico_gpu_render_device).
+__global__ void __launch_bounds__(kRenderThreads) prepare_image_kernel(const uint32_t* count, uint32_t npx,
+                                                                      uint32_t max_samples, uint32_t* pix_list,
+                                                                      uint32_t* done, uint32_t* taken)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += gridDim.x * blockDim.x) {
+        pix_list[p] = p;
+        done[p] = count[p] >= max_samples ? 1u : 0u;
+        taken[p] = 0;
     }
 }
 
@@ -687,37 +705,72 @@ static unsigned grid_for(uint32_t n, int threads)
 
 // Persistent grid of a closest-hit launch: `ctas_per_sm` CTAs per SM (0 or more
 // than fit: as many as fit).
-template <int kOrder, int kThreads>
+template <int kOrder, int kThreads, bool kCount = false>
 static unsigned extend_grid(uint32_t ctas_per_sm)
 {
     static int per_sm = 0;
     if (!per_sm) {
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder, kThreads>, kThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, extend_kernel<kOrder, kThreads, kCount>, kThreads, 0);
         if (per_sm < 1) per_sm = 1;
     }
     const int k = (ctas_per_sm > 0 && (int)ctas_per_sm < per_sm) ? (int)ctas_per_sm : per_sm;
     return (unsigned)(sm_count() * k);
 }
 
+// One closest-hit launch; with counters, the counting variant (128 threads per CTA).
 template <int kOrder>
 static void launch_extend(const SceneView& sc, PathBatch& b, const uint32_t* q, const uint32_t* count,
                           const uint32_t* sq, const uint32_t* scount, DeviceStatus* status,
-                          unsigned long long* tally, cudaStream_t st)
+                          unsigned long long* tally, unsigned long long* counters, cudaStream_t st)
 {
     unsigned long long* stally = &status->rays[2];
+    if (counters) {
+        extend_kernel<kOrder, 128, true><<<extend_grid<kOrder, 128, true>(b.extend_ctas), 128, 0, st>>>(
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally, counters);
+        return;
+    }
     switch (b.extend_threads) {
     case 64:
         extend_kernel<kOrder, 64><<<extend_grid<kOrder, 64>(b.extend_ctas), 64, 0, st>>>(
-            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally, nullptr);
         break;
     case 256:
         extend_kernel<kOrder, 256><<<extend_grid<kOrder, 256>(b.extend_ctas), 256, 0, st>>>(
-            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally, nullptr);
         break;
     default:
         extend_kernel<kOrder, 128><<<extend_grid<kOrder, 128>(b.extend_ctas), 128, 0, st>>>(
-            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally);
+            sc, b, q, count, sq, scount, &status->work, &status->trace_error, tally, stally, nullptr);
     }
+}
+
+cudaError_t LaunchTimer::record(cudaStream_t st)
+{
+    if (used == events.size()) {
+        cudaEvent_t ev = nullptr;
+        const cudaError_t e = cudaEventCreate(&ev);
+        if (e != cudaSuccess) return e;
+        events.push_back(ev);
+    }
+    return cudaEventRecord(events[used++], st);
+}
+
+cudaError_t LaunchTimer::total(double& ms, uint64_t& launches) const
+{
+    ms = 0.0;
+    launches = used / 2;
+    for (size_t k = 0; k + 1 < used; k += 2) {
+        float t = 0.0f;
+        const cudaError_t e = cudaEventElapsedTime(&t, events[k], events[k + 1]);
+        if (e != cudaSuccess) return e;
+        ms += t;
+    }
+    return cudaSuccess;
+}
+
+LaunchTimer::~LaunchTimer()
+{
+    for (cudaEvent_t ev : events) cudaEventDestroy(ev);
 }
 
 __global__ void stamp_kernel(unsigned long long* dst)
@@ -735,8 +788,11 @@ cudaError_t launch_stamp(unsigned long long* dst, cudaStream_t st)
 
 // The extend / shade / shadow loop of one batch whose camera rays are queued.
 static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t max_depth, bool physical,
-                                  const NrcShadeArgs& nrc, DeviceStatus* status, int order, cudaStream_t st)
+                                  const NrcShadeArgs& nrc, DeviceStatus* status, int order, cudaStream_t st,
+                                  const RenderProbe* probe = nullptr)
 {
+    LaunchTimer* timer = probe ? probe->timer : nullptr;
+    unsigned long long* counters = probe ? probe->counters : nullptr;
     cudaError_t e = cudaSuccess;
     const bool trace_last =
         sc.sky_kind != PICO_SKY_CONSTANT || sc.sky[0] != 0.0f || sc.sky[1] != 0.0f || sc.sky[2] != 0.0f;
@@ -747,10 +803,12 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
         unsigned long long* tally = &status->rays[depth == 0 ? 0 : 1];
         // this depth's segments, and from depth 1 on the previous shade's shadow rays
         const uint32_t* sq = depth > 0 ? b.shadow_queue : nullptr;
+        if (timer && (e = timer->record(st)) != cudaSuccess) return e;
         with_variant(order, sc, [&](auto v) {
             launch_extend<decltype(v)::value>(sc, b, b.queue[cur], &b.counters[cur], sq, &b.counters[2], status,
-                                              tally, st);
+                                              tally, counters, st);
         });
+        if (timer && (e = timer->record(st)) != cudaSuccess) return e;
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
@@ -786,8 +844,9 @@ cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const Camer
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
                                 int estimator, DeviceStatus* status, int order, cudaStream_t st,
-                                const NrcShadeArgs* nrc)
+                                const NrcShadeArgs* nrc, const RenderProbe* probe)
 {
+    b.sample_tally = &status->rays[3];
     const bool physical = estimator != PICO_ESTIMATOR_REFERENCE;
     NrcShadeArgs off{};
     off.mode = kNrcOff;
@@ -796,7 +855,7 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     if (e == cudaSuccess && na.mode != kNrcOff) e = cudaMemsetAsync(na.count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
     raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
-    e = run_depth_loop(sc, b, max_depth, physical, na, status, order, st);
+    e = run_depth_loop(sc, b, max_depth, physical, na, status, order, st, probe);
     if (e != cudaSuccess) return e;
     if (na.mode == kNrcTerminate) {
         e = nrc::launch_infer(na.geo, na.table, na.weights, na.queries, na.capacity, nullptr, b.thr, b.pay, na.err, st,
@@ -806,6 +865,15 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
     accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,
                                                                                     physical);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prepare_image(const uint32_t* count, uint32_t npx, uint32_t max_samples, uint32_t* pix_list,
+                                 uint32_t* done, uint32_t* taken, cudaStream_t st)
+{
+    if (npx == 0) return cudaSuccess;
+    prepare_image_kernel<<<grid_for(npx, kRenderThreads), kRenderThreads, 0, st>>>(count, npx, max_samples, pix_list,
+                                                                                  done, taken);
     return cudaGetLastError();
 }
 

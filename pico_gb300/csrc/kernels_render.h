@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace pico {
 
 // Camera::generate_ray inputs plus host-precomputed glm quantities.
@@ -39,6 +41,26 @@ struct PathBatch {
     float4* samples;                   // per path: final radiance
     // image state (W*H entries)
     float* pixels; float* variance; uint32_t* count; uint32_t* taken; uint32_t* done;
+    unsigned long long* sample_tally;  // samples added to the image (set by launch_render_batch)
+};
+
+// Measurement hooks of a render's closest-hit launches: CUDA events recorded on
+// the launching stream before and after each one (timer), or work counters
+// (count: the counting kernel variant adds nodes, triangles, instance entries
+// and nodes inside instances to `counters`).  Both are off in ordinary renders.
+struct LaunchTimer {
+    std::vector<cudaEvent_t> events;   // before / after pairs, reused across renders
+    size_t used = 0;
+    cudaError_t record(cudaStream_t st);
+    // Sum of the recorded launches' durations (ms) and their number; the events
+    // must have completed.
+    cudaError_t total(double& ms, uint64_t& launches) const;
+    void reset() { used = 0; }
+    ~LaunchTimer();
+};
+struct RenderProbe {
+    LaunchTimer* timer;
+    unsigned long long* counters;      // 4 counters, or null
 };
 
 // What the physical shade step does for the radiance cache.
@@ -71,7 +93,11 @@ struct NrcShadeArgs {
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
                                 int estimator, DeviceStatus* status, int order, cudaStream_t st,
-                                const NrcShadeArgs* nrc = nullptr);
+                                const NrcShadeArgs* nrc = nullptr, const RenderProbe* probe = nullptr);
+// The image state of a render into caller device buffers: every pixel listed in
+// order, done where count >= max_samples, nothing taken yet.
+cudaError_t launch_prepare_image(const uint32_t* count, uint32_t npx, uint32_t max_samples, uint32_t* pix_list,
+                                 uint32_t* done, uint32_t* taken, cudaStream_t st);
 // The radiance cache's training paths of one sample pass: n full-depth physical
 // paths from pseudo-random pixels of the W x H image (path slots 0 .. n-1 of b),
 // recording every shaded vertex (kNrcRecord), then the records' targets

@@ -154,7 +154,7 @@ int pico_gpu_nrc_create(pico_gpu_ctx* ctx, const pico_nrc_config* cfg, pico_gpu_
     *out = nullptr;
     std::string why;
     if (!valid_config(*cfg, why)) return set_error(ctx, PICO_ERR_INVALID_ARG, why);
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     auto* c = new (std::nothrow) pico_gpu_nrc();
     if (!c) return set_error(ctx, PICO_ERR_OUT_OF_MEMORY, "host allocation");
     c->ctx = ctx;
@@ -209,7 +209,7 @@ int pico_gpu_nrc_create(pico_gpu_ctx* ctx, const pico_nrc_config* cfg, pico_gpu_
 void pico_gpu_nrc_free(pico_gpu_nrc* c)
 {
     if (!c) return;
-    cudaSetDevice(c->ctx->device);
+    const DeviceScope device_scope(c->ctx->device);
     if (c->ctx->cache == c) c->ctx->cache = nullptr;
     for (void* p : c->allocations) cudaFree(p);
     delete c;
@@ -219,7 +219,7 @@ int pico_gpu_nrc_set_params(pico_gpu_nrc* c, const float* mlp, const float* grid
 {
     if (!c || !mlp || !grid) return PICO_ERR_INVALID_ARG;
     pico_gpu_ctx* ctx = c->ctx;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     std::vector<float> w(mlp, mlp + kMlpParams);
     for (int o = kOutputs; o < kWidth; ++o)
@@ -245,7 +245,7 @@ int pico_gpu_nrc_set_params(pico_gpu_nrc* c, const float* mlp, const float* grid
 int pico_gpu_nrc_get_params(pico_gpu_nrc* c, float* mlp, float* grid)
 {
     if (!c) return PICO_ERR_INVALID_ARG;
-    cudaSetDevice(c->ctx->device);
+    const DeviceScope device_scope(c->ctx->device);
     cudaStream_t st = c->ctx->stream;
     cudaError_t e = cudaSuccess;
     if (mlp) e = cudaMemcpyAsync(mlp, c->master, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, st);
@@ -285,7 +285,7 @@ int pico_gpu_nrc_encode(pico_gpu_nrc* c, const pico_nrc_query* q, uint64_t n, fl
     if (!c || (n && (!q || !out))) return PICO_ERR_INVALID_ARG;
     if (n > kMaxQueries) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "too many queries");
     pico_gpu_ctx* ctx = c->ctx;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     cudaError_t e = ctx->buf_a.reserve(n * sizeof(pico_nrc_query) + 16);
     if (e == cudaSuccess) e = ctx->buf_b.reserve(n * kWidth * sizeof(float) + 16);
@@ -303,7 +303,7 @@ int pico_gpu_nrc_infer_device(pico_gpu_nrc* c, const pico_nrc_query* d_q, uint64
 {
     if (!c || (n && (!d_q || !d_rgb))) return PICO_ERR_INVALID_ARG;
     if (n > kMaxQueries) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "too many queries");
-    cudaSetDevice(c->ctx->device);
+    const DeviceScope device_scope(c->ctx->device);
     cudaError_t e = launch_infer(c->geo, c->table, c->image, reinterpret_cast<const float4*>(d_q), (uint32_t)n, d_rgb,
                                  nullptr, nullptr, c->err, static_cast<cudaStream_t>(stream), nullptr,
                                  (int)c->cfg.infer_groups);
@@ -316,7 +316,7 @@ int pico_gpu_nrc_infer(pico_gpu_nrc* c, const pico_nrc_query* q, uint64_t n, flo
     if (!c || (n && (!q || !rgb))) return PICO_ERR_INVALID_ARG;
     if (n > kMaxQueries) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "too many queries");
     pico_gpu_ctx* ctx = c->ctx;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     cudaError_t e = ctx->buf_a.reserve(n * sizeof(pico_nrc_query) + 16);
     if (e == cudaSuccess) e = ctx->buf_b.reserve(n * 3 * sizeof(float) + 16);
@@ -335,7 +335,7 @@ int pico_gpu_nrc_train_device(pico_gpu_nrc* c, const pico_nrc_query* d_q, const 
 {
     if (!c || (n && (!d_q || !d_targets))) return PICO_ERR_INVALID_ARG;
     if (n > kMaxTrainBatch) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "a training batch holds at most 2^20 records");
-    cudaSetDevice(c->ctx->device);
+    const DeviceScope device_scope(c->ctx->device);
     TrainBatch b{reinterpret_cast<const float4*>(d_q), reinterpret_cast<const float4*>(d_targets), (uint32_t)n, 0, 1};
     return train_step(c, b, apply != 0, static_cast<cudaStream_t>(stream));
 }
@@ -346,7 +346,7 @@ int pico_gpu_nrc_train(pico_gpu_nrc* c, const pico_nrc_query* q, const float* ta
     if (!c || (n && (!q || !targets))) return PICO_ERR_INVALID_ARG;
     if (n > kMaxTrainBatch) return set_error(c->ctx, PICO_ERR_INVALID_ARG, "a training batch holds at most 2^20 records");
     pico_gpu_ctx* ctx = c->ctx;
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     std::vector<float> t4(n * 4, 0.0f);
     for (uint64_t i = 0; i < n; ++i)
@@ -370,7 +370,7 @@ int pico_gpu_nrc_train(pico_gpu_nrc* c, const pico_nrc_query* q, const float* ta
 int pico_gpu_nrc_gradients(pico_gpu_nrc* c, float* mlp_grad, float* grid_grad)
 {
     if (!c) return PICO_ERR_INVALID_ARG;
-    cudaSetDevice(c->ctx->device);
+    const DeviceScope device_scope(c->ctx->device);
     cudaStream_t st = c->ctx->stream;
     cudaError_t e = cudaSuccess;
     if (mlp_grad) e = cudaMemcpyAsync(mlp_grad, c->grad, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, st);

@@ -176,7 +176,7 @@ int pico_gpu_encode_hdr(pico_gpu_ctx* ctx, const float* pixels, uint32_t W, uint
                         size_t capacity, size_t* length)
 {
     if (!ctx || !pixels || !length) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     const size_t n3 = (size_t)W * H * 3;
     void* d = nullptr;
     cudaError_t e = cudaMalloc(&d, n3 * sizeof(float) + 16);

@@ -5,10 +5,12 @@
 // copied in, advanced by up to max_samples samples per pixel with the
 // reference's running mean / variance and early-exit rule, and copied back.
 // Pixels whose count already reaches max_samples are skipped, as the
-// reference's tile loop skips them.  Samples run as batches of at most 4M
+// reference's tile loop skips them.  Samples run as batches of at most 16M
 // paths (pixels x samples), each pixel's samples in order across batches; the
 // cancel flag is polled between batches.  When requested, the a-trous pass
 // then runs on the result and replaces it (Scene.cpp:212-234).
+// pico_gpu_render_device does the same on caller device buffers, asynchronously
+// on the caller's stream (no host copies, no cancel flag).
 #include "nrc_internal.h"
 #include "render_internal.h"
 
@@ -74,6 +76,8 @@ void free_render_buffers(pico_gpu_ctx* ctx)
 {
     delete ctx->render;
     ctx->render = nullptr;
+    delete ctx->extend_timer;
+    ctx->extend_timer = nullptr;
 }
 
 cudaError_t reserve_paths(RenderBuffers& r, size_t n)
@@ -223,16 +227,11 @@ int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_n
     return nrc::take_status(c, st);
 }
 
-}  // namespace
-
-extern "C" {
-
-int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
-                    const pico_render_config* cfg, float* pixels, uint32_t* sample_count, float* variance,
-                    const volatile int32_t* should_quit)
+// Checks shared by the render entry points.
+int validate_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                    const pico_render_config* cfg)
 {
-    if (!ctx || !scene || !cfg || !valid_camera(camera) || !pixels || !sample_count || !variance)
-        return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (!ctx || !scene || !cfg || !valid_camera(camera)) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (cfg->width != camera->resolution[0] || cfg->height != camera->resolution[1])
         return set_error(ctx, PICO_ERR_INVALID_ARG, "render size differs from the camera resolution");
     if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && cfg->estimator != PICO_ESTIMATOR_PHYSICAL &&
@@ -242,11 +241,96 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         return set_error(ctx, PICO_ERR_UNSUPPORTED, "the physical estimator has no Transparent or Fresnel lobes");
     if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE && !ctx->cache)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "no radiance cache attached (pico_gpu_set_radiance_cache)");
-    cudaSetDevice(ctx->device);
+    return PICO_OK;
+}
+
+// With a cancel flag, a render's batches take at most this many samples per pixel,
+// so that a cancel is seen after at most one such batch (on small images a batch
+// could otherwise hold hundreds of samples per pixel).
+constexpr uint32_t kCancelSamplesPerBatch = 16;
+
+// The sample batches of a reference or physical render over the first `nactive`
+// pixels of r.pix_list, advancing the image buffers (pixels, variance, count) and
+// r's taken / done state on st.  With a cancel flag the host polls it before each
+// batch (and waits for the previous one); without one nothing waits for the device.
+int run_sample_batches(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_render_config* cfg,
+                       const CameraView& cam, RenderBuffers& r, size_t nactive, float* pixels, float* variance,
+                       uint32_t* count, const volatile int32_t* should_quit, cudaStream_t st, bool& cancelled)
+{
+    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, kMaxPaths);
+    uint32_t spb_cap = kMaxPaths / chunk_pix;
+    if (should_quit) spb_cap = std::min(spb_cap, kCancelSamplesPerBatch);
+    const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, spb_cap));
+    cudaError_t e = reserve_paths(r, (size_t)chunk_pix * spb_max);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
+    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr};
+    const RenderProbe* pp = (probe.timer || probe.counters) ? &probe : nullptr;
+    for (size_t p0 = 0; p0 < nactive && !cancelled; p0 += chunk_pix) {
+        const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, nactive - p0);
+        for (uint32_t s0 = 0; s0 < cfg->max_samples; s0 += spb_max) {
+            if (should_quit && *should_quit) { cancelled = true; break; }
+            const uint32_t spb = std::min(spb_max, cfg->max_samples - s0);
+            PathBatch b = make_batch(r, npix * spb, npix, cfg->width, as<uint32_t>(r.pix_list) + p0);
+            b.pixels = pixels;
+            b.variance = variance;
+            b.count = count;
+            e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
+                                    cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene), st,
+                                    nullptr, pp);
+            if (e == cudaSuccess && should_quit) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
+        }
+    }
+    return PICO_OK;
+}
+
+// Scene.cpp:212-234 after the samples: the a-trous pass on the G-buffer replaces
+// the image, then the tone map runs in place.
+int finish_image(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const CameraView& cam, const pico_render_config* cfg,
+                 RenderBuffers& r, float* pixels, cudaStream_t st)
+{
+    const uint32_t W = cfg->width, H = cfg->height;
+    const size_t n3 = (size_t)W * H * 3;
+    cudaError_t e = cudaSuccess;
+    if (cfg->denoise) {
+        for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
+            if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
+        if (e == cudaSuccess)
+            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status,
+                               scene_order(ctx, scene), st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
+        const int status = run_atrous(ctx, r, pixels, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
+                                      as<float>(r.out), st);
+        if (status != PICO_OK) return status;
+        e = cudaMemcpyAsync(pixels, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "denoise copy");
+    }
+    if (cfg->tonemap) {
+        // in place on the (denoised) buffer, which then replaces the caller's pixels (Scene.cpp:225-234)
+        e = r.tonemap.reserve(sizeof(unsigned));
+        if (e == cudaSuccess) e = launch_reinhard(pixels, W, H, as<unsigned>(r.tonemap), st);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "tone mapping");
+    }
+    return PICO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                    const pico_render_config* cfg, float* pixels, uint32_t* sample_count, float* variance,
+                    const volatile int32_t* should_quit)
+{
+    int status = validate_render(ctx, scene, camera, cfg);
+    if (status != PICO_OK) return status;
+    if (!pixels || !sample_count || !variance) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
     const uint32_t W = cfg->width, H = cfg->height;
     const size_t npx = (size_t)W * H;
+    ctx->stats_on_device = false;
 
     cudaError_t e = r.pixels.reserve(npx * 3 * sizeof(float));
     if (e == cudaSuccess) e = r.variance.reserve(npx * 3 * sizeof(float));
@@ -276,53 +360,18 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
 
     const CameraView cam = make_camera_view(*camera);
     bool cancelled = false;
-    if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE) {
-        if (!active.empty() && cfg->max_samples > 0) {
-            const int status = render_with_cache(ctx, scene, ctx->cache, cfg, cam, r, active.size(), should_quit,
-                                                 cancelled);
-            if (status != PICO_OK) return status;
-        }
-    } else if (!active.empty() && cfg->max_samples > 0) {
-        const uint32_t chunk_pix = (uint32_t)std::min<size_t>(active.size(), kMaxPaths);
-        const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, kMaxPaths / chunk_pix));
-        e = reserve_paths(r, (size_t)chunk_pix * spb_max);
-        if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
-        for (size_t p0 = 0; p0 < active.size() && !cancelled; p0 += chunk_pix) {
-            const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, active.size() - p0);
-            for (uint32_t s0 = 0; s0 < cfg->max_samples; s0 += spb_max) {
-                if (should_quit && *should_quit) { cancelled = true; break; }
-                const uint32_t spb = std::min(spb_max, cfg->max_samples - s0);
-                PathBatch b = make_batch(r, npix * spb, npix, W, as<uint32_t>(r.pix_list) + p0);
-                e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
-                                        cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene),
-                                        st);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-                if (e != cudaSuccess) return cuda_error(ctx, e, "render batch");
-            }
-        }
+    if (!active.empty() && cfg->max_samples > 0) {
+        status = cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE
+                     ? render_with_cache(ctx, scene, ctx->cache, cfg, cam, r, active.size(), should_quit, cancelled)
+                     : run_sample_batches(ctx, scene, cfg, cam, r, active.size(), as<float>(r.pixels),
+                                          as<float>(r.variance), as<uint32_t>(r.count), should_quit, st, cancelled);
+        if (status != PICO_OK) return status;
     }
-    int status = take_device_status(ctx, st);
+    status = take_device_status(ctx, st);
+    if (status != PICO_OK) return status;
+    status = finish_image(ctx, scene, cam, cfg, r, as<float>(r.pixels), st);
     if (status != PICO_OK) return status;
 
-    if (cfg->denoise) {
-        const size_t n3 = npx * 3;
-        for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
-            if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
-        if (e == cudaSuccess)
-            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status, scene_order(ctx, scene), st);
-        if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
-        status = run_atrous(ctx, r, as<float>(r.pixels), as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
-                            as<float>(r.out), st);
-        if (status != PICO_OK) return status;
-        e = cudaMemcpyAsync(r.pixels.ptr, r.out.ptr, n3 * sizeof(float), cudaMemcpyDeviceToDevice, st);
-        if (e != cudaSuccess) return cuda_error(ctx, e, "denoise copy");
-    }
-    if (cfg->tonemap) {
-        // in place on the (denoised) buffer, which then replaces the caller's pixels (Scene.cpp:225-234)
-        e = r.tonemap.reserve(sizeof(unsigned));
-        if (e == cudaSuccess) e = launch_reinhard(as<float>(r.pixels), W, H, as<unsigned>(r.tonemap), st);
-        if (e != cudaSuccess) return cuda_error(ctx, e, "tone mapping");
-    }
     e = cudaMemcpyAsync(pixels, r.pixels.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(variance, r.variance.ptr, npx * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(sample_count, r.count.ptr, npx * sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -342,10 +391,100 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
     return cancelled ? set_error(ctx, PICO_ERR_CANCELLED, "render cancelled") : PICO_OK;
 }
 
-int pico_gpu_render_stats(const pico_gpu_ctx* ctx, uint64_t* out5)
+int pico_gpu_render_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
+                           const pico_render_config* cfg, float* d_pixels, uint32_t* d_count, float* d_variance,
+                           void* stream)
 {
-    if (!ctx || !out5) return PICO_ERR_INVALID_ARG;
+    int status = validate_render(ctx, scene, camera, cfg);
+    if (status != PICO_OK) return status;
+    if (!d_pixels || !d_count || !d_variance) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE)
+        return set_error(ctx, PICO_ERR_UNSUPPORTED, "device-buffer renders take the reference or physical estimator");
+    const size_t npx = (size_t)cfg->width * cfg->height;
+    if (npx > 0xffffffffull) return set_error(ctx, PICO_ERR_INVALID_ARG, "image larger than 2^32 pixels");
+    const DeviceScope device_scope(ctx->device);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    RenderBuffers& r = *render_buffers(ctx);
+    cudaError_t e = cudaSuccess;
+    for (DeviceBuffer* b : {&r.taken, &r.done, &r.pix_list})
+        if (e == cudaSuccess) e = b->reserve(npx * sizeof(uint32_t));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "image state");
+    e = launch_prepare_image(d_count, (uint32_t)npx, cfg->max_samples, as<uint32_t>(r.pix_list), as<uint32_t>(r.done),
+                             as<uint32_t>(r.taken), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->rays, 0, sizeof(ctx->status->rays), st);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render set-up");
+    const CameraView cam = make_camera_view(*camera);
+    bool cancelled = false;
+    if (npx > 0 && cfg->max_samples > 0) {
+        status = run_sample_batches(ctx, scene, cfg, cam, r, npx, d_pixels, d_variance, d_count, nullptr, st,
+                                    cancelled);
+        if (status != PICO_OK) return status;
+    }
+    status = finish_image(ctx, scene, cam, cfg, r, d_pixels, st);
+    if (status != PICO_OK) return status;
+    ctx->stats_on_device = true;
+    ctx->stats_stream = st;
+    ctx->stats_gbuffer_rays = cfg->denoise ? npx : 0;
+    return PICO_OK;
+}
+
+int pico_gpu_render_stats(const pico_gpu_ctx* cctx, uint64_t* out5)
+{
+    if (!cctx || !out5) return PICO_ERR_INVALID_ARG;
+    pico_gpu_ctx* ctx = const_cast<pico_gpu_ctx*>(cctx);
+    if (ctx->stats_on_device) {
+        // the tallies of the last pico_gpu_render_device call, once its stream has them
+        const DeviceScope device_scope(ctx->device);
+        unsigned long long rays[4] = {0, 0, 0, 0};
+        cudaError_t e = cudaStreamSynchronize(ctx->stats_stream);
+        if (e == cudaSuccess) e = cudaMemcpy(rays, ctx->status->rays, sizeof(rays), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_error(ctx, e, "render stats");
+        ctx->render_stats[0] = rays[3];
+        ctx->render_stats[1] = rays[0];
+        ctx->render_stats[2] = rays[1];
+        ctx->render_stats[3] = rays[2];
+        ctx->render_stats[4] = ctx->stats_gbuffer_rays;
+        ctx->stats_on_device = false;
+    }
     for (int k = 0; k < 5; ++k) out5[k] = ctx->render_stats[k];
+    return PICO_OK;
+}
+
+int pico_gpu_set_render_probe(pico_gpu_ctx* ctx, int32_t time_extend, int32_t count_work)
+{
+    if (!ctx) return PICO_ERR_INVALID_ARG;
+    const DeviceScope device_scope(ctx->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render probe");
+    if (time_extend) {
+        if (!ctx->extend_timer) ctx->extend_timer = new LaunchTimer();
+        ctx->extend_timer->reset();
+    } else {
+        delete ctx->extend_timer;
+        ctx->extend_timer = nullptr;
+    }
+    ctx->count_work = count_work != 0;
+    e = cudaMemset(ctx->status->counters, 0, sizeof(ctx->status->counters));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render probe");
+    return PICO_OK;
+}
+
+int pico_gpu_render_probe_read(pico_gpu_ctx* ctx, uint64_t* out4, double* extend_ms)
+{
+    if (!ctx || !out4 || !extend_ms) return PICO_ERR_INVALID_ARG;
+    const DeviceScope device_scope(ctx->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long c[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(c, ctx->status->counters, sizeof c, cudaMemcpyDeviceToHost);
+    double ms = 0.0;
+    uint64_t launches = 0;
+    if (e == cudaSuccess && ctx->extend_timer) e = ctx->extend_timer->total(ms, launches);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render probe");
+    out4[0] = launches;
+    out4[1] = c[0];
+    out4[2] = c[1];
+    out4[3] = c[2];
+    *extend_ms = ms;
     return PICO_OK;
 }
 
@@ -354,7 +493,7 @@ int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, con
 {
     if (!ctx || !scene || !valid_camera(camera) || !normals || !positions || !diffuse)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
     const uint32_t W = camera->resolution[0], H = camera->resolution[1];
@@ -378,8 +517,9 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
 {
     if (!ctx || !d_pixels || !d_normals || !d_positions || !d_diffuse || !d_out)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    if (d_out == d_pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "output must not alias the input");
-    cudaSetDevice(ctx->device);
+    if (atrous_output_aliases(d_out, d_pixels, d_normals, d_positions, d_diffuse, (size_t)width * height * 3))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "the output must not overlap an input");
+    const DeviceScope device_scope(ctx->device);
     return run_atrous(ctx, *render_buffers(ctx), d_pixels, d_normals, d_positions, d_diffuse, width, height, d_out,
                       static_cast<cudaStream_t>(stream));
 }
@@ -389,7 +529,7 @@ int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals
 {
     if (!ctx || !pixels || !normals || !positions || !diffuse || !out)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
     const size_t n3 = (size_t)W * H * 3;
@@ -413,7 +553,7 @@ int pico_gpu_atrous(pico_gpu_ctx* ctx, const float* pixels, const float* normals
 int pico_gpu_tonemap_device(pico_gpu_ctx* ctx, float* d_pixels, uint32_t width, uint32_t height, void* stream)
 {
     if (!ctx || !d_pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     RenderBuffers& r = *render_buffers(ctx);
     cudaError_t e = r.tonemap.reserve(sizeof(unsigned));
     if (e == cudaSuccess)
@@ -425,7 +565,7 @@ int pico_gpu_tonemap_device(pico_gpu_ctx* ctx, float* d_pixels, uint32_t width, 
 int pico_gpu_tonemap(pico_gpu_ctx* ctx, float* pixels, uint32_t width, uint32_t height)
 {
     if (!ctx || !pixels) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
-    cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
     const size_t n3 = (size_t)width * height * 3;

@@ -30,6 +30,9 @@ namespace pico {
 // tail: a 1080p render at 64 spp measured 159 / 206 / 267 / 279 / 286 Msamples/s
 // with batches of 2^19 / 2^20 / 2^22 / 2^23 / 2^24 paths (physical estimator).
 constexpr uint32_t kMaxPaths = 1u << 24;
+// Device bytes of path state per path that reserve_paths allocates: twelve float4
+// arrays, six uint32 arrays and the 64-bit random state.
+constexpr size_t kPathStateBytes = 12 * 16 + 6 * 4 + 8;
 
 template <class T>
 T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }

@@ -50,21 +50,7 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
             write_hit(sc, h, s, hits + i);
         }
     }
-    if (kCount) {
-        // one atomic per warp per counter
-        for (int off = 16; off > 0; off >>= 1) {
-            cnt.nodes += __shfl_down_sync(0xffffffffu, cnt.nodes, off);
-            cnt.tris += __shfl_down_sync(0xffffffffu, cnt.tris, off);
-            cnt.insts += __shfl_down_sync(0xffffffffu, cnt.insts, off);
-            cnt.blas_nodes += __shfl_down_sync(0xffffffffu, cnt.blas_nodes, off);
-        }
-        if (lane == 0) {
-            atomicAdd(&status->counters[0], cnt.nodes);
-            atomicAdd(&status->counters[1], cnt.tris);
-            atomicAdd(&status->counters[2], cnt.insts);
-            atomicAdd(&status->counters[3], cnt.blas_nodes);
-        }
-    }
+    if (kCount) flush_counters(cnt, status->counters);
 }
 
 int sm_count()

@@ -531,21 +531,40 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
 // semantics: exactly when the closest hit is nearer than tmax).  The near-first
 // walk bounds its search by tmax and stops at the first such instance; the
 // reference order runs the closest hit.
-template <int kVariant>
+template <int kVariant, bool kCount = false>
 __device__ __forceinline__ int trace_occluded(const SceneView& sc, const float4 o, const float4 d, float tmax,
-                                              bool& occluded)
+                                              bool& occluded, TraceCounters* cnt = nullptr)
 {
     constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
     TraceHit h;
     int s;
     if ((kVariant & kReferenceOrder) != 0) {
-        s = trace_reference_order<false, kImplicit>(sc, o, d, h, nullptr);
+        s = trace_reference_order<kCount, kImplicit>(sc, o, d, h, cnt);
         occluded = h.rank != kNoHit && h.t < tmax;
     } else {
-        s = trace_near_first<false, kImplicit, true>(sc, o, d, h, nullptr, tmax);
+        s = trace_near_first<kCount, kImplicit, true>(sc, o, d, h, cnt, tmax);
         occluded = h.rank != kNoHit;
     }
     return s;
+}
+
+// Adds a thread's work counters to counters[0..3] (nodes, triangles, instance
+// entries, nodes inside instances) with one atomic per warp and counter; the
+// whole warp must call it.
+__device__ __forceinline__ void flush_counters(TraceCounters c, unsigned long long* counters)
+{
+    for (int off = 16; off > 0; off >>= 1) {
+        c.nodes += __shfl_down_sync(0xffffffffu, c.nodes, off);
+        c.tris += __shfl_down_sync(0xffffffffu, c.tris, off);
+        c.insts += __shfl_down_sync(0xffffffffu, c.insts, off);
+        c.blas_nodes += __shfl_down_sync(0xffffffffu, c.blas_nodes, off);
+    }
+    if ((threadIdx.x & 31u) == 0) {
+        atomicAdd(&counters[0], c.nodes);
+        atomicAdd(&counters[1], c.tris);
+        atomicAdd(&counters[2], c.insts);
+        atomicAdd(&counters[3], c.blas_nodes);
+    }
 }
 
 // Calls f(std::integral_constant<int, V>) for the kernel variant V of (order, scene).

@@ -1,17 +1,19 @@
-"""Small drivers that run one part of the library on synthetic inputs, for profiling.
+"""Small drivers that run one part of the library on synthetic inputs, for profiling
+(the commands of the ncu summaries under profiles/; a bench helper, not part of the
+package).
 
-    python -m pico_gb300.drivers cache [--queries N] [--records N] [--reps K]
+    python profile_drivers.py cache [--queries N] [--records N] [--reps K]
         radiance-cache inference over N queries and K training steps over N records
         (uniformly random positions over a 400 x 125 x 400 box, seeded)
-    python -m pico_gb300.drivers cache-render [--passes K]
+    python profile_drivers.py cache-render [--passes K]
         a 1920x1080 render of the lit field through the radiance cache
-    python -m pico_gb300.drivers render [--estimator E] [--passes K]
+    python profile_drivers.py render [--estimator E] [--passes K]
         a 1920x1080 render of the lit field, K samples per pixel, estimator E
         (0 the reference's, 1 the physical one)
-    python -m pico_gb300.drivers cornell [--passes K]
+    python profile_drivers.py cornell [--passes K]
         K renders of the Cornell box at 256x256, 16 spp, depth 5, denoised
         (after one warm-up render)
-    python -m pico_gb300.drivers batch [--renders N] [--scale S]
+    python profile_drivers.py batch [--renders N] [--scale S]
         N renders of the batched-rendering workload (resolutions times S) in one
         CUDA-graph launch, physical estimator, 2^22-path wavefront, 64-thread
         closest-hit CTAs, 8 branches
@@ -19,10 +21,14 @@
 from __future__ import annotations
 
 import argparse
+import sys
+from pathlib import Path
 
 import numpy as np
 
-import pico_gb300
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+
+import pico_gb300  # noqa: E402
 from pico_gb300 import RadianceCache, scenes
 from pico_gb300.types import NRC_QUERY_DTYPE
 

@@ -1,13 +1,13 @@
 """Generates the golden vectors in this directory from the Pico reference itself.
 
 Runs the reference's own code through oracle/_ref/libpico_ref.so (built from
-the Pico source tree by `make -C oracle ref`) on seeded inputs and stores
+the Pico source tree named by PICO_REFERENCE) on seeded inputs and stores
 inputs and outputs as .npz files.  The reference has no tests or fixtures of
 its own, so these files are the pins for the oracle restatement: the CPU test
 suite checks the oracle against them bit for bit, and the GPU tests check the
 kernels against the oracle.
 
-    python tests/golden/make_golden.py
+    PICO_REFERENCE=<Pico source tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
