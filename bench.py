@@ -327,11 +327,42 @@ def bench_radiance_cache(ctx, args, torch, local, plain_series):
                            "train_paths": st["train_paths"], "train_records": st["train_records"],
                            "train_steps": st["train_steps"], "cache_queries": st["queries"]})
             c.free()
+    # the cache's error floor and pass cost without training: a cache trained over 256 passes,
+    # copied into a cache that does not train (no training paths, no optimiser steps), renders N
+    # passes; the time leaves out the training, so this bounds what any online schedule can reach
+    frozen = []
+    if j is not None:
+        trained = RadianceCache(ctx, **cfg)
+        trained.attach()
+        gs.render(cam, args.render_depth, 256, seed=880, estimator=2)
+        mlp, grid = trained.params()
+        trained.free()
+        fz = RadianceCache(ctx, **cfg, train_paths=0, max_train_steps=0)
+        fz.set_params(mlp, grid)
+        fz.attach()
+        gs.render(cam, args.render_depth, 2, seed=881, estimator=2)   # warm-up
+        for n in (16, 32, 64, 128):
+            t0 = time.perf_counter()
+            pix, _, _ = gs.render(cam, args.render_depth, n, seed=900 + n, estimator=2)
+            secs = time.perf_counter() - t0
+            frozen.append({"passes": n, "seconds": secs, "relmse": j.relmse(pix)})
+        fz.free()
     out = {"workload": f"lit field 1920x1080, depth {args.render_depth}, radiance cache (16-level hash grid 2^19, "
                        f"SH4, 5 x 64 ReLU, bf16 tcgen05), 65536 training paths and up to 4 Adam steps of 65536 "
                        f"records per pass, paths end after 1 bounce (2 behind roughness < 0.1)",
            "timing": "wall clock around pico_gpu_render (host buffers in and out), fresh cache per render",
-           "series": series, "clocks": clocks.summary()}
+           "series": series, "clocks": clocks.summary(),
+           "pretrained_frozen": {"series": frozen,
+                                 "note": "a cache trained over a 256-pass render, copied into a cache that does not "
+                                         "train, renders N passes: its relMSE approaches the trained cache's error "
+                                         "floor, its time is the pass cost without training (training excluded)"}}
+    if len(frozen) >= 2:
+        # relMSE ~ a / N + floor, least squares over the series
+        A = np.array([[1.0 / f["passes"], 1.0] for f in frozen])
+        a, floor = np.linalg.lstsq(A, np.array([f["relmse"] for f in frozen]), rcond=None)[0]
+        out["pretrained_frozen"]["fit"] = {"variance_term": float(a), "floor": float(floor),
+                                           "ms_per_pass": float(np.mean([f["seconds"] / f["passes"] for f in frozen])
+                                                                * 1e3)}
     plain = {p["spp"]: p for p in plain_series or []}
     if j is not None and 256 in plain:
         target, budget = plain[256]["relmse"], plain[256]["seconds"]

@@ -190,6 +190,25 @@ const char* pico_gpu_last_error(const pico_gpu_ctx* ctx);
  * it returns depends on its own visit order. */
 enum pico_traversal_order { PICO_ORDER_NEAR_FIRST = 0, PICO_ORDER_REFERENCE = 1 };
 int pico_gpu_set_traversal_order(pico_gpu_ctx* ctx, int order);
+/* The bounds every traversal of this context's calls runs under (the reference
+ * recurses without bounds, Core/BVH.cpp:27-63, depth limited to 32 only at build
+ * time, Core/BVH.hpp:129): at most max_iterations steps per ray walk (0: the
+ * default 2^24) and at most stack_entries entries of the 96-entry traversal stack
+ * (0: all 96).  A walk that needs more stops, and the call returns
+ * PICO_ERR_TIMEOUT or PICO_ERR_STACK_OVERFLOW; nothing waits or faults.  Smaller
+ * bounds are a debugging aid and for tests of those error paths; the defaults
+ * never bind on scenes of the reference's depth limit. */
+int pico_gpu_set_traversal_limits(pico_gpu_ctx* ctx, uint32_t max_iterations, uint32_t stack_entries);
+/* The ray / triangle test of every closest-hit query in a context.
+ * MOLLER_TRUMBORE (the default) is the reference's Mesh_Intersector::intersects
+ * (Core/LowerLevelMeshBVH.cpp:165-207, epsilon 1e-7) in its float operation order,
+ * which gives the reference's hits bit for bit.  WATERTIGHT has no counterpart in
+ * the reference: the test of Woop, Benthin and Wald (JCGT 2013), under which a ray
+ * through an edge or vertex shared by two triangles always hits one of them
+ * (Moeller-Trumbore can let such rays through the crack); away from edges it finds
+ * the same triangles, with t, u, v equal up to rounding. */
+enum pico_triangle_test { PICO_TRIANGLE_MOLLER_TRUMBORE = 0, PICO_TRIANGLE_WATERTIGHT = 1 };
+int pico_gpu_set_triangle_test(pico_gpu_ctx* ctx, int test);
 
 /* ---- scene -------------------------------------------------------------- */
 int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out);
@@ -197,6 +216,17 @@ void pico_gpu_scene_free(pico_gpu_scene* scene);
 /* Sizes of the flattened scene: [0] TLAS nodes, [1] BLAS nodes, [2] triangles,
  * [3] instances, [4] device bytes, [5] lights. */
 int pico_gpu_scene_info(const pico_gpu_scene* scene, uint64_t* out6);
+/* The binary BVH pico_gpu_scene_upload builds before flattening it (host only, no
+ * device needed), in the layout of the reference's BVH<T,2>::m_nodes
+ * (Core/BVH.hpp:52-81, built by Core/BVH.cpp:73-197): which = -1 the TLAS over
+ * instances, else the BLAS of mesh `which`.  Per node, in the order the builder
+ * pushes them (children before their parent): boxes[6] (min xyz, max xyz),
+ * links[4] (child 0, child 1, 0xffffffff for none; first, count of its leaf items
+ * in `values`); values lists every leaf's items (triangle or instance indices) in
+ * node order.  *nnodes and *nvalues receive the sizes; NULL arrays are skipped, so
+ * a first call with NULL arrays sizes the second. */
+int pico_gpu_reference_bvh(const pico_scene_desc* desc, int32_t which, float* boxes, uint32_t* links,
+                           uint32_t* values, uint32_t* nnodes, uint32_t* nvalues);
 
 /* ---- closest hit (UpperLevelBVH::get_closest_intersection) --------------- */
 /* rays / hits are host buffers.  When each lies inside one page-locked, mapped
@@ -286,7 +316,7 @@ int pico_gpu_atrous_device(pico_gpu_ctx* ctx, const float* d_pixels, const float
  * must not allocate device memory during their denoise step: a frame loop that
  * overlaps streams (cudaFree, and often cudaMalloc, synchronises the whole
  * device) or a process whose device memory belongs to another allocator.  On
- * success it allocates nothing: its scratch is a fixed 48 MiB + 2 MiB device
+ * success it allocates nothing: its scratch is a fixed 48 MiB + 5.5 MiB device
  * array per device, so images are limited to 2,097,152 pixels (1920 x 1080
  * fits) and 65,535 rows; larger ones return PICO_ERR_INVALID_ARG with a
  * message, and so does an output that overlaps an input.  The caller's current

@@ -46,9 +46,13 @@ SIGNATURES = {
     "pico_gpu_status_string": (C.c_char_p, [C.c_int]),
     "pico_gpu_last_error": (C.c_char_p, [_vp]),
     "pico_gpu_set_traversal_order": (C.c_int, [_vp, C.c_int]),
+    "pico_gpu_set_traversal_limits": (C.c_int, [_vp, _u32, _u32]),
+    "pico_gpu_set_triangle_test": (C.c_int, [_vp, C.c_int]),
     "pico_gpu_scene_upload": (C.c_int, [_vp, C.POINTER(CSceneDesc), C.POINTER(_vp)]),
     "pico_gpu_scene_free": (None, [_vp]),
     "pico_gpu_scene_info": (C.c_int, [_vp, C.POINTER(_u64)]),
+    "pico_gpu_reference_bvh": (C.c_int, [C.POINTER(CSceneDesc), _i32, _vp, _vp, _vp, C.POINTER(_u32),
+                                         C.POINTER(_u32)]),
     "pico_gpu_trace_closest": (C.c_int, [_vp, _vp, _vp, _u64, _vp]),
     "pico_gpu_trace_closest_device": (C.c_int, [_vp, _vp, _vp, _u64, _vp, _vp]),
     "pico_gpu_host_buffer_in_place": (C.c_int, [_vp, _vp, _u64, C.POINTER(_i32)]),
@@ -123,6 +127,25 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
     return lib
 
 
+def reference_bvh(scene: SceneData, which: int):
+    """pico_gpu_reference_bvh (host only): the binary BVH the upload builds, in the reference's
+    layout -- which = -1 the TLAS, else mesh `which`'s BLAS -- as (boxes (n, 6), links (n, 4), values)."""
+    lib = load_library()
+    m = MarshalledScene(scene)
+    nn, nv = C.c_uint32(0), C.c_uint32(0)
+    st = lib.pico_gpu_reference_bvh(C.byref(m.desc), which, None, None, None, C.byref(nn), C.byref(nv))
+    if st != PICO_OK:
+        raise PicoError(st, "reference_bvh")
+    boxes = np.empty((nn.value, 6), np.float32)
+    links = np.empty((nn.value, 4), np.uint32)
+    values = np.empty(max(nv.value, 1), np.uint32)
+    st = lib.pico_gpu_reference_bvh(C.byref(m.desc), which, boxes.ctypes.data, links.ctypes.data, values.ctypes.data,
+                                    C.byref(nn), C.byref(nv))
+    if st != PICO_OK:
+        raise PicoError(st, "reference_bvh")
+    return boxes, links, values[:nv.value]
+
+
 def _f32(a: np.ndarray):
     return a.ctypes.data_as(_fp)
 
@@ -157,6 +180,15 @@ class Context:
     def set_traversal_order(self, order: int):
         """0: near-first (default), 1: the reference's child order (exact in near-tie cases)."""
         self.check(self.lib.pico_gpu_set_traversal_order(self.handle, order), "set_traversal_order")
+
+    def set_traversal_limits(self, max_iterations: int = 0, stack_entries: int = 0):
+        """Bounds of every ray walk of this context (0: the defaults, 2^24 steps and 96 stack entries)."""
+        self.check(self.lib.pico_gpu_set_traversal_limits(self.handle, max_iterations, stack_entries),
+                   "set_traversal_limits")
+
+    def set_triangle_test(self, test: int):
+        """0: the reference's Moeller-Trumbore (default), 1: the watertight test (Woop et al. 2013)."""
+        self.check(self.lib.pico_gpu_set_triangle_test(self.handle, test), "set_triangle_test")
 
     def host_buffer_in_place(self, ptr: int, nbytes: int) -> bool:
         """Whether trace_closest reads / writes the host range [ptr, ptr + nbytes) in place (it lies in one

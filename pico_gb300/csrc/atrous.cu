@@ -1,15 +1,21 @@
 // A-trous denoiser (Util::atrous_denoise, Util/Denoisers.cpp:107-126; blend_pixel :18-101).
 //
 // Five levels with tap spacing 1, 2, 4, 8, 16 over a 5x5 kernel (the reference's
-// table, including its 0.09563 entry at index 17).  Each level runs two kernels:
+// table, including its 0.09563 entry at index 17).  Per 64x64 tile (the
+// reference's Tiler tiles, clamped at the right and bottom edges) and level the
+// blend needs the maximum luminance and the min / max |position| over every
+// pixel some tap of the tile reads.  That set is rows x columns, each a union of
+// five shifted copies of the tile's range, clamped.  The positions are the same
+// at every level, so two launches first reduce all five levels' |position|
+// ranges, separably (per image row over each tile column's footprint columns,
+// then per tile over its footprint rows), reading the positions once; then each
+// level runs two kernels:
 //
-//   stats  one CTA per 64x64 tile (the reference's Tiler tiles, clamped at the
-//          right and bottom edges): the maximum luminance and the min / max
-//          |position| over every pixel some tap of the tile reads.  That set is
-//          rows x columns, each a union of five shifted copies of the tile's
-//          range, clamped; the CTA walks the distinct members once instead of
-//          25 taps per pixel.  max / min are exact, so the order is free, and
-//          the selects keep std::max / std::min's NaN behaviour.
+//   stats  the maximum luminance of the level's input colour over the tile's
+//          footprint (four CTAs per tile, each a quarter of the footprint rows),
+//          walking the distinct members once instead of 25 taps per pixel.
+//          max / min are exact, so the order is free, and the selects keep
+//          std::max / std::min's NaN behaviour.
 //   blend  one thread per pixel: 25 taps, weights
 //          w = k[u] * min(exp(-|dn|^2/0.25),1) * min(exp(-|dp|^2/range^2),1)
 //                   * min(exp(-|dalbedo|^2/white^2),1),
@@ -76,11 +82,11 @@ __device__ __forceinline__ float luminance(float r, float g, float b)
     return add(add(mul(r, 0.2126f), mul(g, 0.587f)), mul(b, 0.114f));
 }
 
-__global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float* __restrict__ pix,
-                                                                      const float* __restrict__ pos, uint32_t W,
-                                                                      uint32_t H, int s, float4* __restrict__ parts)
+// Maximum luminance over this CTA's quarter of a tile's footprint rows (a partial
+// record per CTA; tile_stats combines the four).
+__global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float* __restrict__ pix, uint32_t W,
+                                                                      uint32_t H, int s, float* __restrict__ parts)
 {
-    using namespace ex;
     const int tiles_x = (int)((W + kTile - 1) / kTile);
     const int tile = (int)(blockIdx.x / kStatsSplit), part = (int)(blockIdx.x % kStatsSplit);
     const int tx = tile % tiles_x, ty = tile / tiles_x;
@@ -96,11 +102,7 @@ __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float
     const int ncols = list_spans(span[0], span[1], nspan[0], cols);
     const int nrows = list_spans(span[2], span[3], nspan[1], rows);
     __syncthreads();
-    // maximum luminance and min / max |position| over this CTA's share of the
-    // footprint rows; max / min are exact, so the visiting order and the split are
-    // free, and the selects keep std::max / std::min's NaN behaviour
-    const float kInf = __int_as_float(0x7f800000);
-    float white = 0.0f, mind = kInf, maxd = -kInf;
+    float white = 0.0f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int kWarps = kStatsThreads / 32;
     for (int r = part * kWarps + warp; r < nrows; r += kStatsSplit * kWarps) {
@@ -109,44 +111,123 @@ __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float
             const size_t f = rb + (size_t)cols[c];
             const float l = luminance(__ldg(pix + 3 * f), __ldg(pix + 3 * f + 1), __ldg(pix + 3 * f + 2));
             white = (white < l) ? l : white;
-            const float len = length(v3(__ldg(pos + 3 * f), __ldg(pos + 3 * f + 1), __ldg(pos + 3 * f + 2)));
-            mind = (len < mind) ? len : mind;
-            maxd = (maxd < len) ? len : maxd;
         }
     }
     for (int off = 16; off > 0; off >>= 1) {
         const float w2 = __shfl_down_sync(0xffffffffu, white, off);
-        const float a2 = __shfl_down_sync(0xffffffffu, mind, off);
-        const float b2 = __shfl_down_sync(0xffffffffu, maxd, off);
         white = (white < w2) ? w2 : white;
-        mind = (a2 < mind) ? a2 : mind;
-        maxd = (maxd < b2) ? b2 : maxd;
     }
-    __shared__ float sw[kWarps], sa[kWarps], sb[kWarps];
-    if (lane == 0) { sw[warp] = white; sa[warp] = mind; sb[warp] = maxd; }
+    __shared__ float sw[kWarps];
+    if (lane == 0) sw[warp] = white;
     __syncthreads();
     if (threadIdx.x == 0) {
-        for (int w = 1; w < kWarps; ++w) {
-            white = (white < sw[w]) ? sw[w] : white;
-            mind = (sa[w] < mind) ? sa[w] : mind;
-            maxd = (maxd < sb[w]) ? sb[w] : maxd;
-        }
-        parts[blockIdx.x] = make_float4(white, mind, maxd, 0.0f);
+        for (int w = 1; w < kWarps; ++w) white = (white < sw[w]) ? sw[w] : white;
+        parts[blockIdx.x] = white;
     }
 }
 
-// A tile's white point and |position| range from its kStatsSplit partial records.
-__device__ __forceinline__ float2 tile_stats(const float4* __restrict__ parts, int tile)
+// The min / max |position| over each level's footprint of each tile, in two
+// separable steps (the footprint is a set of rows times a set of columns):
+//   row_range   one warp per (image row, tile column): |position| of the columns
+//               any level's footprint of that tile column can reach ([x0 - 32,
+//               x1 + 32], clamped) is read once, then reduced over each level's
+//               column spans: rrow[(level * H + y) * tiles_x + tx] = (min, max);
+//   tile_range  one warp per (tile, level): the row ranges reduced over the
+//               level's row spans: range[level * tiles + tile] = (min, max).
+// min / max are exact, so the grouping is free, and the selects keep std::min /
+// std::max's NaN behaviour (a NaN |position| never replaces a bound).
+constexpr int kRowWarps = 4;
+__device__ __forceinline__ bool in_spans(int c, const int* lo, const int* hi, int m)
 {
-    float4 t = parts[tile * kStatsSplit];
+    bool in = false;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) in |= (i < m) && lo[i] <= c && c <= hi[i];
+    return in;
+}
+
+__global__ void __launch_bounds__(32 * kRowWarps) atrous_row_range_kernel(const float* __restrict__ pos, uint32_t W,
+                                                                        uint32_t H, float2* __restrict__ rrow)
+{
+    using namespace ex;
+    const int tiles_x = (int)((W + kTile - 1) / kTile);
+    const int lane = threadIdx.x & 31;
+    const long long task = (long long)blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+    if (task >= (long long)H * tiles_x) return;   // the whole warp leaves together
+    const int y = (int)(task / tiles_x), tx = (int)(task % tiles_x);
+    const int x0 = tx * kTile, x1 = min(x0 + kTile, (int)W) - 1;
+    const int rx0 = max(x0 - 32, 0), rx1 = min(x1 + 32, (int)W - 1);
+    float len[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int c = rx0 + lane + 32 * k;
+        len[k] = 0.0f;
+        if (c <= rx1) {
+            const size_t f = 3 * ((size_t)y * W + (size_t)c);
+            len[k] = length(v3(__ldg(pos + f), __ldg(pos + f + 1), __ldg(pos + f + 2)));
+        }
+    }
+    const float kInf = __int_as_float(0x7f800000);
+    for (int level = 0; level < 5; ++level) {
+        int lo[5], hi[5];
+        const int m = tap_spans(x0, x1, 1 << level, (int)W, lo, hi);
+        float mind = kInf, maxd = -kInf;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int c = rx0 + lane + 32 * k;
+            if (c <= rx1 && in_spans(c, lo, hi, m)) {
+                mind = (len[k] < mind) ? len[k] : mind;
+                maxd = (maxd < len[k]) ? len[k] : maxd;
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            const float a2 = __shfl_down_sync(0xffffffffu, mind, off);
+            const float b2 = __shfl_down_sync(0xffffffffu, maxd, off);
+            mind = (a2 < mind) ? a2 : mind;
+            maxd = (maxd < b2) ? b2 : maxd;
+        }
+        if (lane == 0) rrow[((size_t)level * H + y) * tiles_x + tx] = make_float2(mind, maxd);
+    }
+}
+
+__global__ void __launch_bounds__(32 * 5) atrous_tile_range_kernel(const float2* __restrict__ rrow, uint32_t W,
+                                                                   uint32_t H, float2* __restrict__ range)
+{
+    const int tiles_x = (int)((W + kTile - 1) / kTile);
+    const int tiles = tiles_x * (int)((H + kTile - 1) / kTile);
+    const int tile = (int)blockIdx.x, level = (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int tx = tile % tiles_x, y0 = (tile / tiles_x) * kTile;
+    const int y1 = min(y0 + kTile, (int)H) - 1;
+    int lo[5], hi[5];
+    const int m = tap_spans(y0, y1, 1 << level, (int)H, lo, hi);
+    const float kInf = __int_as_float(0x7f800000);
+    float mind = kInf, maxd = -kInf;
+    for (int i = 0; i < m; ++i)
+        for (int r = lo[i] + lane; r <= hi[i]; r += 32) {
+            const float2 v = rrow[((size_t)level * H + r) * tiles_x + tx];
+            mind = (v.x < mind) ? v.x : mind;
+            maxd = (maxd < v.y) ? v.y : maxd;
+        }
+    for (int off = 16; off > 0; off >>= 1) {
+        const float a2 = __shfl_down_sync(0xffffffffu, mind, off);
+        const float b2 = __shfl_down_sync(0xffffffffu, maxd, off);
+        mind = (a2 < mind) ? a2 : mind;
+        maxd = (maxd < b2) ? b2 : maxd;
+    }
+    if (lane == 0) range[level * tiles + tile] = make_float2(mind, maxd);
+}
+
+// A tile's white point (from its kStatsSplit partial records) and |position| range.
+__device__ __forceinline__ float2 tile_stats(const float* __restrict__ parts, const float2* __restrict__ range,
+                                             int tile)
+{
+    float w = parts[tile * kStatsSplit];
 #pragma unroll
     for (int k = 1; k < kStatsSplit; ++k) {
-        const float4 p = parts[tile * kStatsSplit + k];
-        t.x = (t.x < p.x) ? p.x : t.x;
-        t.y = (p.y < t.y) ? p.y : t.y;
-        t.z = (t.z < p.z) ? p.z : t.z;
+        const float p = parts[tile * kStatsSplit + k];
+        w = (w < p) ? p : w;
     }
-    return make_float2(t.x, __fsub_rn(t.z, t.y));
+    const float2 r = range[tile];
+    return make_float2(w, __fsub_rn(r.y, r.x));
 }
 
 // One thread per pixel, 25 taps.  The reference's weight
@@ -162,13 +243,13 @@ __global__ void __launch_bounds__(256) atrous_blend_kernel(const float* __restri
                                                            const float* __restrict__ nrm,
                                                            const float* __restrict__ pos,
                                                            const float* __restrict__ dif, uint32_t W, uint32_t H,
-                                                           int s, const float4* __restrict__ stats,
-                                                           float* __restrict__ dst)
+                                                           int s, const float* __restrict__ stats,
+                                                           const float2* __restrict__ range, float* __restrict__ dst)
 {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
     if (x >= W) return;
     const int tiles_x = (int)((W + kTile - 1) / kTile);
-    const float2 st = tile_stats(stats, (int)((y / kTile) * tiles_x + x / kTile));
+    const float2 st = tile_stats(stats, range, (int)((y / kTile) * tiles_x + x / kTile));
     const float ip = __frcp_rn(__fmul_rn(st.y, st.y));   // 1 / range^2 (inf for a zero range)
     const float iw = __frcp_rn(__fmul_rn(st.x, st.x));   // 1 / white^2
     const Idx c = ((Idx)y * W + x) * 3;
@@ -237,8 +318,8 @@ __device__ __forceinline__ void blend_tap(const float4 t0, const float4 t1, cons
 template <typename Idx>
 __global__ void __launch_bounds__(kBlendThreads) atrous_blend_tiled_kernel(
     const float* __restrict__ src, const float* __restrict__ nrm, const float* __restrict__ pos,
-    const float* __restrict__ dif, uint32_t W, uint32_t H, int s, const float4* __restrict__ stats,
-    float* __restrict__ dst)
+    const float* __restrict__ dif, uint32_t W, uint32_t H, int s, const float* __restrict__ stats,
+    const float2* __restrict__ range, float* __restrict__ dst)
 {
     __shared__ float4 rec[kFootY * kFootX * 3];   // [row][column parity][column / 2] records
     const int rx = (int)(blockIdx.x % (uint32_t)s), tx = (int)(blockIdx.x / (uint32_t)s);
@@ -262,8 +343,8 @@ __global__ void __launch_bounds__(kBlendThreads) atrous_blend_tiled_kernel(
     if (y >= (int)H || x0 >= (int)W) return;
     const int tiles_x = (int)((W + kTile - 1) / kTile);
     const int x1c = x1 < (int)W ? x1 : x0;
-    const float2 st0 = tile_stats(stats, (y / kTile) * tiles_x + x0 / kTile);
-    const float2 st1 = tile_stats(stats, (y / kTile) * tiles_x + x1c / kTile);
+    const float2 st0 = tile_stats(stats, range, (y / kTile) * tiles_x + x0 / kTile);
+    const float2 st1 = tile_stats(stats, range, (y / kTile) * tiles_x + x1c / kTile);
     const float ip0 = __frcp_rn(__fmul_rn(st0.y, st0.y)), iw0 = __frcp_rn(__fmul_rn(st0.x, st0.x));
     const float ip1 = __frcp_rn(__fmul_rn(st1.y, st1.y)), iw1 = __frcp_rn(__fmul_rn(st1.x, st1.x));
     float c0[9], c1[9];
@@ -310,13 +391,23 @@ cudaError_t launch_atrous(const float* pixels, const float* normals, const float
 {
     if (W == 0 || H == 0) return cudaSuccess;
     const uint32_t tiles = ((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile);
-    float4* stats = reinterpret_cast<float4*>(tile_stats);
+    // scratch (atrous_stats_floats): per tile kStatsSplit white-point partials, then five
+    // (min, max) |position| ranges per tile, then five (min, max) per image row and tile column
+    float* parts = tile_stats;
+    float2* range = reinterpret_cast<float2*>(tile_stats + (size_t)tiles * kStatsSplit);
+    float2* rrow = range + (size_t)5 * tiles;
+    const uint32_t tiles_x = (W + kTile - 1) / kTile;
+    const uint64_t row_tasks = (uint64_t)H * tiles_x;
+    atrous_row_range_kernel<<<(unsigned)((row_tasks + kRowWarps - 1) / kRowWarps), 32 * kRowWarps, 0, st>>>(
+        positions, W, H, rrow);
+    atrous_tile_range_kernel<<<tiles, 32 * 5, 0, st>>>(rrow, W, H, range);
     const float* src = pixels;
     for (int level = 0; level < 5; ++level) {
         // ping-pong: in -> A -> B -> A -> B -> out
         float* dst = level == 4 ? out : ((level % 2 == 0) ? scratch_a : scratch_b);
         const int s = 1 << level;
-        atrous_stats_kernel<<<tiles * kStatsSplit, kStatsThreads, 0, st>>>(src, positions, W, H, s, stats);
+        const float2* lrange = range + (size_t)level * tiles;
+        atrous_stats_kernel<<<tiles * kStatsSplit, kStatsThreads, 0, st>>>(src, W, H, s, parts);
         const bool small = (uint64_t)W * H * 3 < (1ull << 32);
         if (s <= kTiledMaxSpacing) {
             // one CTA per kLatX x kLatY tile of each of the s x s sub-lattices
@@ -324,18 +415,18 @@ cudaError_t launch_atrous(const float* pixels, const float* normals, const float
             dim3 grid(((lw + kLatX - 1) / kLatX) * s, ((lh + kLatY - 1) / kLatY) * s);
             if (small)
                 atrous_blend_tiled_kernel<uint32_t><<<grid, kBlendThreads, 0, st>>>(src, normals, positions, diffuse,
-                                                                                   W, H, s, stats, dst);
+                                                                                   W, H, s, parts, lrange, dst);
             else
                 atrous_blend_tiled_kernel<size_t><<<grid, kBlendThreads, 0, st>>>(src, normals, positions, diffuse, W,
-                                                                                 H, s, stats, dst);
+                                                                                 H, s, parts, lrange, dst);
         } else {
             dim3 grid((W + 255) / 256, H);
             if (small)
-                atrous_blend_kernel<uint32_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats,
-                                                                    dst);
+                atrous_blend_kernel<uint32_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, parts,
+                                                                    lrange, dst);
             else
-                atrous_blend_kernel<size_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, stats,
-                                                                  dst);
+                atrous_blend_kernel<size_t><<<grid, 256, 0, st>>>(src, normals, positions, diffuse, W, H, s, parts,
+                                                                  lrange, dst);
         }
         src = dst;
     }

@@ -17,7 +17,7 @@
 //   * at most kNoAllocMaxPixels = 2,097,152 pixels (1920 x 1080 fits) and
 //     65,535 rows per call; larger images are rejected with
 //     PICO_ERR_INVALID_ARG and a message in the context, before any launch;
-//   * the array takes 48 MiB + 2 MiB of device memory on each device;
+//   * the array takes 48 MiB + 5.5 MiB of device memory on each device;
 //   * the output must not overlap any input (the last level writes it while it
 //     still reads the colour and the G-buffer): rejected with PICO_ERR_INVALID_ARG;
 //   * every call on a device shares that one array, so calls whose kernels
@@ -43,14 +43,19 @@ constexpr uint32_t kNoAllocMaxRows = 65535;            // the blend kernel's gri
 // row of 2^21 pixels is the worst case); from 65 rows on it has at most 2^21 / 65
 // columns, so at most 505 tiles per tile row and far fewer than 2^15 in all.
 constexpr size_t kNoAllocMaxTiles = kNoAllocMaxPixels / 64;
-static_assert(kNoAllocMaxTiles == 32768, "statistics region of 2 MiB");
+static_assert(kNoAllocMaxTiles == 32768, "32,768 statistics tiles");
 constexpr size_t kNoAllocImageFloats = 3 * kNoAllocMaxPixels;
-constexpr size_t kNoAllocFloats = 2 * kNoAllocImageFloats + pico::kAtrousStatsFloatsPerTile * kNoAllocMaxTiles;
+// The statistics (pico::atrous_stats_floats): 14 floats per tile, and 10 per image row and
+// tile column, of which an accepted image has at most 2^21 / 64 + 65,535 (H * ceil(W / 64)
+// <= W * H / 64 + H).
+constexpr size_t kNoAllocStatsFloats = 14 * kNoAllocMaxTiles + 10 * (kNoAllocMaxPixels / 64 + kNoAllocMaxRows);
+constexpr size_t kNoAllocFloats = 2 * kNoAllocImageFloats + kNoAllocStatsFloats;
 constexpr int kNoAllocMaxDevices = 64;
 
 }  // namespace
 
-// Ping-pong image A, ping-pong image B, then the per-tile statistics records (float4).
+// Ping-pong image A, ping-pong image B, then the per-tile statistics (white-point
+// partials and per-level |position| ranges).
 static __device__ __align__(256) float pico_atrous_noalloc_scratch[kNoAllocFloats];
 
 namespace {
@@ -89,7 +94,8 @@ extern "C" int pico_gpu_atrous_device_noalloc(pico_gpu_ctx* ctx, const float* d_
         return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     const size_t npx = (size_t)width * height;
     const size_t tiles = (size_t)((width + 63) / 64) * ((height + 63) / 64);
-    if (npx > kNoAllocMaxPixels || height > kNoAllocMaxRows || tiles > kNoAllocMaxTiles)
+    if (npx > kNoAllocMaxPixels || height > kNoAllocMaxRows || tiles > kNoAllocMaxTiles ||
+        atrous_stats_floats(width, height) > kNoAllocStatsFloats)
         return set_error(ctx, PICO_ERR_INVALID_ARG,
                          "a-trous without allocation: the image exceeds the fixed scratch "
                          "(at most 2,097,152 pixels and 65,535 rows)");
@@ -98,7 +104,8 @@ extern "C" int pico_gpu_atrous_device_noalloc(pico_gpu_ctx* ctx, const float* d_
     if (npx == 0) return PICO_OK;
     if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "a-trous without allocation: device index above 63");
-    cudaError_t e = cudaSetDevice(ctx->device);
+    const DeviceScope device_scope(ctx->device);   // the caller's current device comes back on return
+    cudaError_t e = device_scope.status;
     float* scratch = nullptr;
     if (e == cudaSuccess) e = scratch_for_device(ctx->device, &scratch);
     if (e == cudaSuccess)

@@ -294,7 +294,7 @@ cudaError_t enqueue(pico_gpu_ctx* ctx, const pico_render_item& it, BatchSlot& im
             b.done = as<uint32_t>(image.r.done);
             b.extend_ctas = p.extend_ctas;
             b.extend_threads = p.extend_threads;
-            e = launch_render_batch(it.scene->view, b, pr.cam, cfg.seed, spb, cfg.max_ray_depth, cfg.max_samples,
+            e = launch_render_batch(traversal_view(ctx, it.scene), b, pr.cam, cfg.seed, spb, cfg.max_ray_depth, cfg.max_samples,
                                     cfg.max_variance, (int)cfg.estimator, status, order, st);
         }
     }

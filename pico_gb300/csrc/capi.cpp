@@ -129,6 +129,26 @@ int pico_gpu_set_traversal_order(pico_gpu_ctx* ctx, int order)
     return PICO_OK;
 }
 
+int pico_gpu_set_traversal_limits(pico_gpu_ctx* ctx, uint32_t max_iterations, uint32_t stack_entries)
+{
+    if (!ctx) return PICO_ERR_INVALID_ARG;
+    if (max_iterations == 0) max_iterations = kTraceMaxIter;
+    if (stack_entries == 0) stack_entries = kTraceStack;
+    if (stack_entries > (uint32_t)kTraceStack)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "the traversal stack has 96 entries");
+    ctx->max_iterations = max_iterations;
+    ctx->stack_entries = stack_entries;
+    return PICO_OK;
+}
+
+int pico_gpu_set_triangle_test(pico_gpu_ctx* ctx, int test)
+{
+    if (!ctx || (test != PICO_TRIANGLE_MOLLER_TRUMBORE && test != PICO_TRIANGLE_WATERTIGHT))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "unknown triangle test");
+    ctx->triangle_test = test;
+    return PICO_OK;
+}
+
 int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_gpu_scene** out)
 {
     if (!ctx || !desc || !out) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
@@ -214,6 +234,9 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     v.has_implicit = implicit ? 1u : 0u;
     v.sky_kind = fs.sky_kind; v.sky_w = fs.sky_w; v.sky_h = fs.sky_h; v.sky_pixels = skypx;
     v.use_sun = fs.use_sun;
+    v.max_iterations = kTraceMaxIter;
+    v.stack_entries = kTraceStack;
+    v.watertight = 0;
     for (int a = 0; a < 3; ++a) { v.sun_dir[a] = fs.sun_dir[a]; v.sun_col[a] = fs.sun_col[a]; }
     {
         bool finite = true;
@@ -234,6 +257,24 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     s->info[0] = fs.tlas_nodes; s->info[1] = fs.blas_nodes; s->info[2] = fs.tris.size();
     s->info[3] = fs.insts.size(); s->info[4] = total; s->info[5] = fs.lights.size();
     *out = s;
+    return PICO_OK;
+}
+
+int pico_gpu_reference_bvh(const pico_scene_desc* desc, int32_t which, float* boxes, uint32_t* links,
+                           uint32_t* values, uint32_t* nnodes, uint32_t* nvalues)
+{
+    if (!desc || !nnodes || !nvalues) return PICO_ERR_INVALID_ARG;
+    if (which < -1 || which >= (int64_t)desc->nmeshes) return PICO_ERR_INVALID_ARG;
+    FlatScene fs;
+    fs.keep_trees = true;
+    const std::string why = build_flat_scene(*desc, fs);
+    if (!why.empty()) return why.find("not supported") != std::string::npos ? PICO_ERR_UNSUPPORTED : PICO_ERR_INVALID_ARG;
+    const TreeDump& t = which < 0 ? fs.tlas_tree : fs.blas_trees[which];
+    *nnodes = (uint32_t)(t.links.size() / 4);
+    *nvalues = (uint32_t)t.values.size();
+    if (boxes) std::memcpy(boxes, t.boxes.data(), t.boxes.size() * sizeof(float));
+    if (links) std::memcpy(links, t.links.data(), t.links.size() * sizeof(uint32_t));
+    if (values) std::memcpy(values, t.values.data(), t.values.size() * sizeof(uint32_t));
     return PICO_OK;
 }
 
@@ -258,7 +299,7 @@ int pico_gpu_trace_closest_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene
     if (!ctx || !scene || (n && (!d_rays || !d_hits))) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
     if (reinterpret_cast<uintptr_t>(d_rays) % 16 != 0) return set_error(ctx, PICO_ERR_INVALID_ARG, "rays not 16-byte aligned");
     const DeviceScope device_scope(ctx->device);
-    const cudaError_t e = launch_trace(scene->view, d_rays, n, d_hits, ctx->status, false,
+    const cudaError_t e = launch_trace(traversal_view(ctx, scene), d_rays, n, d_hits, ctx->status, false,
                                        scene_order(ctx, scene), static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_error(ctx, e, "trace launch");
     return PICO_OK;
@@ -282,7 +323,7 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const p
     cudaError_t e = ctx->buf_e.reserve(sizeof(pico_hit) * (n ? n : 1));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->counters, 0, sizeof(ctx->status->counters), st);
     if (e == cudaSuccess)
-        e = launch_trace(scene->view, d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, scene_order(ctx, scene), st);
+        e = launch_trace(traversal_view(ctx, scene), d_rays, n, static_cast<pico_hit*>(ctx->buf_e.ptr), ctx->status, true, scene_order(ctx, scene), st);
     unsigned long long c[4] = {0, 0, 0, 0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(c, ctx->status->counters, sizeof c, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -400,7 +441,7 @@ int trace_via_bounce(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_
         const uint64_t m = (n - off) < chunk ? (n - off) : chunk;
         std::memcpy(ctx->bounce_in, rays + off, m * sizeof(pico_ray));
         e = cudaMemcpyAsync(dr, ctx->bounce_in, m * sizeof(pico_ray), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = launch_trace(scene->view, dr, m, dh, ctx->status, false, scene_order(ctx, scene), st);
+        if (e == cudaSuccess) e = launch_trace(traversal_view(ctx, scene), dr, m, dh, ctx->status, false, scene_order(ctx, scene), st);
         if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->bounce_out, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e == cudaSuccess) std::memcpy(hits + off, ctx->bounce_out, m * sizeof(pico_hit));
@@ -437,7 +478,7 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
         const void* mr = mapped_range(rays, rb, ctx->device);
         void* mh = mapped_range(hits, hb, ctx->device);
         if (mr && mh) {
-            cudaError_t e = launch_trace(scene->view, static_cast<const pico_ray*>(mr), n, static_cast<pico_hit*>(mh),
+            cudaError_t e = launch_trace(traversal_view(ctx, scene), static_cast<const pico_ray*>(mr), n, static_cast<pico_hit*>(mh),
                                          ctx->status, false, scene_order(ctx, scene), ctx->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
             if (e != cudaSuccess) return cuda_error(ctx, e, "trace");
@@ -464,7 +505,7 @@ int pico_gpu_trace_closest(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
         pico_hit* dh = static_cast<pico_hit*>(hbuf[s]->ptr);
         e = cudaMemcpyAsync(dr, rays + off, m * sizeof(pico_ray), cudaMemcpyHostToDevice, streams[s]);
         if (e == cudaSuccess)
-            e = launch_trace(scene->view, dr, m, dh, s ? ctx->status2() : ctx->status, false, scene_order(ctx, scene), streams[s]);
+            e = launch_trace(traversal_view(ctx, scene), dr, m, dh, s ? ctx->status2() : ctx->status, false, scene_order(ctx, scene), streams[s]);
         if (e == cudaSuccess)
             e = cudaMemcpyAsync(hits + off, dh, m * sizeof(pico_hit), cudaMemcpyDeviceToHost, streams[s]);
     }

@@ -85,6 +85,9 @@ struct pico_gpu_ctx {
     size_t bounce_rays = 0;
     RenderBuffers* render = nullptr;            // wavefront path state and image buffers
     int order = PICO_ORDER_NEAR_FIRST;          // traversal order of every trace in this context
+    uint32_t max_iterations = pico::kTraceMaxIter;   // pico_gpu_set_traversal_limits
+    uint32_t stack_entries = pico::kTraceStack;
+    int triangle_test = PICO_TRIANGLE_MOLLER_TRUMBORE;   // pico_gpu_set_triangle_test
     uint64_t render_stats[5] = {0, 0, 0, 0, 0}; // tallies of the last pico_gpu_render call
     // the last render was pico_gpu_render_device: its tallies are read from the
     // device (after its stream) when asked for
@@ -120,6 +123,15 @@ namespace pico {
 inline int scene_order(const pico_gpu_ctx* ctx, const pico_gpu_scene* scene)
 {
     return scene->needs_reference_order ? PICO_ORDER_REFERENCE : ctx->order;
+}
+// The scene's view with the context's traversal bounds, as every launch takes it.
+inline SceneView traversal_view(const pico_gpu_ctx* ctx, const pico_gpu_scene* scene)
+{
+    SceneView v = scene->view;
+    v.max_iterations = ctx->max_iterations;
+    v.stack_entries = ctx->stack_entries;
+    v.watertight = ctx->triangle_test == PICO_TRIANGLE_WATERTIGHT ? 1u : 0u;
+    return v;
 }
 int set_error(pico_gpu_ctx* ctx, int code, const std::string& msg);
 int cuda_error(pico_gpu_ctx* ctx, cudaError_t e, const char* what);

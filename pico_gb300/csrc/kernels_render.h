@@ -110,9 +110,15 @@ cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const Camer
 cudaError_t launch_stamp(unsigned long long* dst, cudaStream_t st);
 cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t W, uint32_t H, float* normals,
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st);
-// Floats of a-trous scratch per 64 x 64 tile: four partial statistics records
-// (white point, min |position|, max |position|, unused) per level.
-constexpr size_t kAtrousStatsFloatsPerTile = 16;
+// Floats of a-trous statistics scratch for a W x H image (beyond its two ping-pong
+// images): per 64 x 64 tile four partial white points (one per CTA of a level's
+// statistics launch) and the five levels' (min, max) |position| ranges, then per
+// image row and tile column the five levels' (min, max) row ranges.
+inline size_t atrous_stats_floats(uint32_t W, uint32_t H)
+{
+    const size_t tx = (W + 63) / 64, ty = (H + 63) / 64;
+    return tx * ty * (4 + 5 * 2) + (size_t)5 * 2 * H * tx;
+}
 cudaError_t launch_atrous(const float* pixels, const float* normals, const float* positions, const float* diffuse,
                           uint32_t W, uint32_t H, float* scratch_a, float* scratch_b, float* tile_stats, float* out,
                           cudaStream_t st);

@@ -124,4 +124,9 @@ struct SceneView {
     const void* sky_pixels;             // uchar4 cube faces or float4 equirectangular texels
     uint32_t use_sun;
     float sun_dir[3], sun_col[3];
+    // traversal bounds of the launching context (pico_gpu_set_traversal_limits):
+    // iterations of one walk, and entries of its stack in use (at most the 96 it has)
+    uint32_t max_iterations;
+    uint32_t stack_entries;
+    uint32_t watertight;                // the launching context's triangle test is the watertight one
 };

@@ -119,10 +119,9 @@ int run_atrous(pico_gpu_ctx* ctx, RenderBuffers& r, const float* d_pix, const fl
                const float* d_d, uint32_t W, uint32_t H, float* d_out, cudaStream_t st)
 {
     const size_t n = (size_t)W * H * 3;
-    const size_t tiles = (size_t)((W + 63) / 64) * ((H + 63) / 64);
     cudaError_t e = r.ga.reserve(n * sizeof(float));
     if (e == cudaSuccess) e = r.gb.reserve(n * sizeof(float));
-    if (e == cudaSuccess) e = r.stats.reserve(tiles * kAtrousStatsFloatsPerTile * sizeof(float));
+    if (e == cudaSuccess) e = r.stats.reserve(atrous_stats_floats(W, H) * sizeof(float));
     if (e == cudaSuccess)
         e = launch_atrous(d_pix, d_n, d_p, d_d, W, H, as<float>(r.ga), as<float>(r.gb), as<float>(r.stats), d_out, st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "a-trous");
@@ -177,7 +176,7 @@ int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_n
         na.mode = kNrcRecord;
         na.capacity = (uint32_t)rec_cap;
         PathBatch tb = make_batch(r, ntrain, 0, W, nullptr);
-        cudaError_t te = launch_training_paths(scene->view, tb, cam, train_seed, (uint32_t)c->train_passes, ntrain,
+        cudaError_t te = launch_training_paths(traversal_view(ctx, scene), tb, cam, train_seed, (uint32_t)c->train_passes, ntrain,
                                                W, H, max_depth, na, as<float4>(r.nrc_tgt), ctx->status, order, st);
         uint32_t nrec = 0;
         if (te == cudaSuccess) te = cudaMemcpyAsync(&nrec, na.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -214,7 +213,7 @@ int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_n
         for (size_t p0 = 0; p0 < nactive; p0 += chunk_pix) {
             const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, nactive - p0);
             PathBatch b = make_batch(r, npix, npix, W, as<uint32_t>(r.pix_list) + p0);
-            e = launch_render_batch(scene->view, b, cam, cfg->seed, 1, max_depth, cfg->max_samples,
+            e = launch_render_batch(traversal_view(ctx, scene), b, cam, cfg->seed, 1, max_depth, cfg->max_samples,
                                     cfg->max_variance, PICO_ESTIMATOR_RADIANCE_CACHE, ctx->status, order, st, &na);
             uint32_t nq = 0;
             if (e == cudaSuccess) e = cudaMemcpyAsync(&nq, na.count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
@@ -274,7 +273,7 @@ int run_sample_batches(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pic
             b.pixels = pixels;
             b.variance = variance;
             b.count = count;
-            e = launch_render_batch(scene->view, b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
+            e = launch_render_batch(traversal_view(ctx, scene), b, cam, cfg->seed, spb, cfg->max_ray_depth, cfg->max_samples,
                                     cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene), st,
                                     nullptr, pp);
             if (e == cudaSuccess && should_quit) e = cudaStreamSynchronize(st);
@@ -296,7 +295,7 @@ int finish_image(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const CameraVie
         for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd, &r.out})
             if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
         if (e == cudaSuccess)
-            e = launch_gbuffer(scene->view, cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status,
+            e = launch_gbuffer(traversal_view(ctx, scene), cam, W, H, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), ctx->status,
                                scene_order(ctx, scene), st);
         if (e != cudaSuccess) return cuda_error(ctx, e, "denoiser inputs");
         const int status = run_atrous(ctx, r, pixels, as<float>(r.gn), as<float>(r.gp), as<float>(r.gd), W, H,
@@ -502,7 +501,7 @@ int pico_gpu_denoiser_inputs(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, con
     for (DeviceBuffer* b : {&r.gn, &r.gp, &r.gd})
         if (e == cudaSuccess) e = b->reserve(n3 * sizeof(float));
     if (e == cudaSuccess)
-        e = launch_gbuffer(scene->view, make_camera_view(*camera), W, H, as<float>(r.gn), as<float>(r.gp),
+        e = launch_gbuffer(traversal_view(ctx, scene), make_camera_view(*camera), W, H, as<float>(r.gn), as<float>(r.gp),
                            as<float>(r.gd), ctx->status, scene_order(ctx, scene), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(normals, r.gn.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(positions, r.gp.ptr, n3 * sizeof(float), cudaMemcpyDeviceToHost, st);

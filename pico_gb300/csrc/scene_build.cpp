@@ -87,6 +87,19 @@ struct RefBvh {
     uint32_t root = kInvalid;
 };
 
+TreeDump dump_tree(const RefBvh& b)
+{
+    TreeDump t;
+    for (const RefNode& n : b.nodes) {
+        t.boxes.insert(t.boxes.end(), {n.box.lo.x, n.box.lo.y, n.box.lo.z, n.box.hi.x, n.box.hi.y, n.box.hi.z});
+        const bool leaf = n.child[0] == kInvalid && n.child[1] == kInvalid;
+        t.links.insert(t.links.end(), {n.child[0], n.child[1], leaf ? (uint32_t)t.values.size() : 0u,
+                                       leaf ? (uint32_t)n.values.size() : 0u});
+        t.values.insert(t.values.end(), n.values.begin(), n.values.end());
+    }
+    return t;
+}
+
 int longest_axis(const float s[3])
 {
     const float a = std::fabs(s[0]), b = std::fabs(s[1]), c = std::fabs(s[2]);
@@ -534,6 +547,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
     // ---- BLAS per mesh -------------------------------------------------------
     struct MeshRoot { uint32_t ref; Box box; uint32_t tri_base; };
     std::vector<MeshRoot> roots(desc.nmeshes);
+    if (fs.keep_trees) fs.blas_trees.assign(desc.nmeshes, TreeDump{});
     for (uint32_t mi = 0; mi < desc.nmeshes; ++mi) {
         const pico_mesh& m = desc.meshes[mi];
         if (m.shape != PICO_SHAPE_TRIANGLES) {
@@ -567,6 +581,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         }
         RefBvh bvh;
         SahBuilder(bvh).build(items);
+        if (fs.keep_trees) fs.blas_trees[mi] = dump_tree(bvh);
         const uint32_t tri_base = (uint32_t)fs.tris.size();
         const size_t before = fs.nodes.size();
         auto place = [&](const std::vector<uint32_t>& values) -> uint32_t {
@@ -615,6 +630,7 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
     }
     RefBvh tlas;
     SahBuilder(tlas).build(items);
+    if (fs.keep_trees) fs.tlas_tree = dump_tree(tlas);
     const size_t before = fs.nodes.size();
     auto place = [&](const std::vector<uint32_t>& values) -> uint32_t {
         const uint32_t first = (uint32_t)fs.insts.size();

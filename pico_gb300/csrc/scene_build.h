@@ -10,8 +10,24 @@
 
 namespace pico {
 
+// A binary BVH in the reference's own layout (BVH<T,2>::m_nodes, Core/BVH.hpp:52-81):
+// nodes in the order the builder pushed them (children before their parent), per
+// node its box (lo xyz, hi xyz), its two child indices (0xffffffff: none) and its
+// leaf items as (first, count) into `values`, which lists every leaf's items in
+// node order.
+struct TreeDump {
+    std::vector<float> boxes;
+    std::vector<uint32_t> links;   // child 0, child 1, first, count per node
+    std::vector<uint32_t> values;
+};
+
 // Host image of everything pico_gpu_scene_upload copies to the device.
 struct FlatScene {
+    // kept only when keep_trees is set before build_flat_scene: the reference-layout
+    // trees the device nodes are flattened from (one per mesh, then the TLAS)
+    bool keep_trees = false;
+    std::vector<TreeDump> blas_trees;
+    TreeDump tlas_tree;
     std::vector<GpuNode> nodes;           // TLAS nodes first, then every BLAS
     std::vector<GpuTri> tris;
     std::vector<GpuTriShade> tri_shade;

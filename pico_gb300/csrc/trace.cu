@@ -91,7 +91,8 @@ cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, 
     const float4* r = reinterpret_cast<const float4*>(rays);
     return with_variant(order, sc, [&](auto v) {
         constexpr int V = decltype(v)::value;
-        return count ? launch_trace_t<true, V>(sc, r, n, hits, status, stream)
+        // the counting variant (measurement only) always reads the bounds at run time
+        return count ? launch_trace_t<true, V | kBounded>(sc, r, n, hits, status, stream)
                      : launch_trace_t<false, V>(sc, r, n, hits, status, stream);
     });
 }

@@ -27,8 +27,6 @@
 
 namespace pico {
 
-constexpr int kTraceStack = 96;
-constexpr uint32_t kTraceMaxIter = 1u << 24;
 constexpr uint32_t kNoHit = 0xffffffffu;
 constexpr uint32_t kImplicitTri = 0xfffffffeu;   // TraceHit::tri of a hit on an implicit shape
 
@@ -111,6 +109,67 @@ __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, 
     return false;
 }
 
+// Watertight ray / triangle test (Woop, Benthin and Wald, "Watertight Ray/Triangle
+// Intersection", JCGT 2(1), 2013), the opt-in alternative to the reference's
+// Moeller-Trumbore.  The vertices are translated to the ray origin and sheared so
+// that the ray runs along +z of its dominant axis (the other two axes swapped when
+// that component is negative, which keeps the winding); three 2D edge functions
+// then decide coverage.  Every product and difference is rounded once and shared
+// vertices are stored bit-identically, so the edge function of an edge shared by
+// two triangles comes out exactly negated in the other; one that is exactly 0 is
+// recomputed in double precision.  A ray through a shared edge or vertex therefore
+// hits at least one of the triangles meeting there.  Both sides count (no back-face
+// culling) and hits at t <= 1e-7 are rejected, as the reference's test does; (u, v)
+// are the weights of v1 and v2, the Moeller-Trumbore meaning.
+__device__ __forceinline__ float pick3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
+
+__device__ __forceinline__ bool intersect_triangle_wt(const GpuTri* tri, float ox, float oy, float oz, float dx,
+                                                      float dy, float dz, float& t_out, float& u_out, float& v_out)
+{
+    using namespace ex;
+    const float4* p = reinterpret_cast<const float4*>(tri);
+    const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    const float mx = fabsf(dx), my = fabsf(dy), mz = fabsf(dz);
+    const int kz = (mx > my) ? ((mx > mz) ? 0 : 2) : ((my > mz) ? 1 : 2);
+    const int kx0 = kz == 2 ? 0 : kz + 1, ky0 = kx0 == 2 ? 0 : kx0 + 1;
+    const float dkz = pick3(dx, dy, dz, kz);
+    const int kx = dkz < 0.0f ? ky0 : kx0, ky = dkz < 0.0f ? kx0 : ky0;
+    const float sx = __fdiv_rn(pick3(dx, dy, dz, kx), dkz), sy = __fdiv_rn(pick3(dx, dy, dz, ky), dkz);
+    const float sz = __frcp_rn(dkz);
+    const float A[3] = {sub(a.x, ox), sub(a.y, oy), sub(a.z, oz)};
+    const float B[3] = {sub(b.x, ox), sub(b.y, oy), sub(b.z, oz)};
+    const float C[3] = {sub(c.x, ox), sub(c.y, oy), sub(c.z, oz)};
+    const float akz = pick3(A[0], A[1], A[2], kz), bkz = pick3(B[0], B[1], B[2], kz), ckz = pick3(C[0], C[1], C[2], kz);
+    const float ax = sub(pick3(A[0], A[1], A[2], kx), mul(sx, akz)), ay = sub(pick3(A[0], A[1], A[2], ky), mul(sy, akz));
+    const float bx = sub(pick3(B[0], B[1], B[2], kx), mul(sx, bkz)), by = sub(pick3(B[0], B[1], B[2], ky), mul(sy, bkz));
+    const float cx = sub(pick3(C[0], C[1], C[2], kx), mul(sx, ckz)), cy = sub(pick3(C[0], C[1], C[2], ky), mul(sy, ckz));
+    float U = sub(mul(cx, by), mul(cy, bx));
+    float V = sub(mul(ax, cy), mul(ay, cx));
+    float W = sub(mul(bx, ay), mul(by, ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = (float)((double)cx * (double)by - (double)cy * (double)bx);
+        V = (float)((double)ax * (double)cy - (double)ay * (double)cx);
+        W = (float)((double)bx * (double)ay - (double)by * (double)ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    const float det = add(add(U, V), W);
+    if (det == 0.0f) return false;
+    const float T = add(add(mul(U, mul(sz, akz)), mul(V, mul(sz, bkz))), mul(W, mul(sz, ckz)));
+    const float rcp = __frcp_rn(det);
+    const float t = mul(T, rcp);
+    if (!(t > 0.0000001f)) return false;
+    t_out = t; u_out = mul(V, rcp); v_out = mul(W, rcp);
+    return true;
+}
+
+template <bool kWatertight>
+__device__ __forceinline__ bool intersect(const GpuTri* tri, float ox, float oy, float oz, float dx, float dy, float dz,
+                                          float& t, float& u, float& v)
+{
+    if (kWatertight) return intersect_triangle_wt(tri, ox, oy, oz, dx, dy, dz, t, u, v);
+    return intersect_triangle(tri, ox, oy, oz, dx, dy, dz, t, u, v);
+}
+
 // Traversal orders.  kNearFirst enters the nearer child first, breaks equal
 // distances by rank, walks a refitted TLAS whose boxes bound each instance's
 // transformed vertices (tighter than the reference's transformed mesh AABB,
@@ -127,11 +186,17 @@ __device__ __forceinline__ bool intersect_triangle(const GpuTri* tri, float ox, 
 enum TraversalOrder : int { kNearFirst = 0, kReferenceOrder = 1 };
 
 // Kernel variants: a traversal order, plus kWithImplicit when the scene holds implicit
-// shapes (the instance-entry check for them is compiled out otherwise).
+// shapes (the instance-entry check for them is compiled out otherwise), plus kBounded
+// when the launching context set traversal bounds other than the defaults
+// (pico_gpu_set_traversal_limits): only those walks read the bounds at run time, so
+// the default kernels keep their compile-time bounds and their register allocation.
 constexpr int kWithImplicit = 2;
-__host__ __device__ constexpr int traversal_variant(int order, bool implicit)
+constexpr int kBounded = 4;
+constexpr int kWatertight = 8;   // the watertight triangle test (pico_gpu_set_triangle_test)
+__host__ __device__ constexpr int traversal_variant(int order, bool implicit, bool bounded, bool watertight)
 {
-    return (order == kReferenceOrder ? kReferenceOrder : kNearFirst) | (implicit ? kWithImplicit : 0);
+    return (order == kReferenceOrder ? kReferenceOrder : kNearFirst) | (implicit ? kWithImplicit : 0) |
+           (bounded ? kBounded : 0) | (watertight ? kWatertight : 0);
 }
 
 // Object-space ray of an instance (transform_ray, Core/AABB.cpp:43-52) and its BLAS root.
@@ -236,11 +301,13 @@ __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t ra
 // kAnyHit: only hits at a world distance below tmax count, and the walk returns
 // at the first instance whose candidate is one (an occlusion query: a hit is
 // reported exactly when the closest hit lies below tmax).
-template <bool kCount, bool kImplicit, bool kAnyHit = false>
+template <bool kCount, bool kImplicit, bool kAnyHit = false, bool kRuntimeBounds = false, bool kWT = false>
 __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
                                                 TraceCounters* cnt, float tmax = INFINITY)
 {
     using namespace ex;
+    const uint32_t max_iter = kRuntimeBounds ? sc.max_iterations : kTraceMaxIter;
+    const int max_stack = kRuntimeBounds ? (int)sc.stack_entries : kTraceStack;
     const float kInf = __int_as_float(0x7f800000);
     const float kMaxFinite = __int_as_float(0x7f7fffff);
     uint32_t stack[kTraceStack];
@@ -279,7 +346,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         if (h && tm < kInf) ref = axis ? sc.tlas_root_ref : sc.tlas_fast_root_ref;
     }
     for (uint32_t iter = 0;; ++iter) {
-        if (iter >= kTraceMaxIter) return kTraceIterLimit;
+        if (iter >= max_iter) return kTraceIterLimit;
         if (ref == PICO_REF_DONE) break;
         if (!pico_is_leaf(ref)) {
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
@@ -303,7 +370,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             const bool v1 = h1 && t1 <= limit;
             if (v0 && v1) {
                 const bool swap = t1 < t0;
-                if (sp >= kTraceStack) return kTraceStackOverflow;
+                if (sp >= max_stack) return kTraceStackOverflow;
                 stack[sp++] = swap ? n3.x : n3.y;
                 ref = swap ? n3.y : n3.x;
             } else if (v0) {
@@ -343,7 +410,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
                 const uint32_t tri = first + k;
                 float t, u, v;
                 if (kCount) cnt->tris++;
-                if (intersect_triangle(sc.tris + tri, cx, cy, cz, qdx, qdy, qdz, t, u, v) &&
+                if (intersect<kWT>(sc.tris + tri, cx, cy, cz, qdx, qdy, qdz, t, u, v) &&
                     (t < lt || (t == lt && tri < ltri))) {
                     lt = t; ltri = tri; lu = u; lv = v;
                 }
@@ -354,7 +421,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         }
         // TLAS leaf: search the instance of item `first`; the rest of the leaf waits on the stack.
         if (count > 1) {
-            if (sp >= kTraceStack) return kTraceStackOverflow;
+            if (sp >= max_stack) return kTraceStackOverflow;
             stack[sp++] = pico_leaf_ref(first + 1, count - 1);
         }
         const uint32_t rank = __ldg(sc.tlas_items + first);
@@ -388,7 +455,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
         }
-        if (sp >= kTraceStack) return kTraceStackOverflow;
+        if (sp >= max_stack) return kTraceStackOverflow;
         stack[sp++] = PICO_REF_END_BLAS;
         in_blas = true;
         cx = q.ox; cy = q.oy; cz = q.oz; cix = q.ix; ciy = q.iy; ciz = q.iz;
@@ -406,11 +473,13 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // missed; -inf: nothing to test).
 struct StackEntry { uint32_t ref; float tmin; };
 
-template <bool kCount, bool kImplicit>
+template <bool kCount, bool kImplicit, bool kRuntimeBounds = false, bool kWT = false>
 __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const float4 o, const float4 d,
                                                      TraceHit& best, TraceCounters* cnt)
 {
     using namespace ex;
+    const uint32_t max_iter = kRuntimeBounds ? sc.max_iterations : kTraceMaxIter;
+    const int max_stack = kRuntimeBounds ? (int)sc.stack_entries : kTraceStack;
     const float kInf = __int_as_float(0x7f800000);
     const float kNan = __int_as_float(0x7fffffff);
     StackEntry stack[kTraceStack];
@@ -438,7 +507,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
         if (h && tm < kInf) ref = sc.tlas_root_ref;
     }
     for (uint32_t iter = 0;; ++iter) {
-        if (iter >= kTraceMaxIter) return kTraceIterLimit;
+        if (iter >= max_iter) return kTraceIterLimit;
         if (ref == PICO_REF_DONE) break;
         if (!pico_is_leaf(ref)) {
             const float4* np = reinterpret_cast<const float4*>(sc.nodes + ref);
@@ -452,7 +521,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
             // child 1 waits on the stack and is tested when reached
             if (n3.y != PICO_REF_EMPTY) {
-                if (sp >= kTraceStack) return kTraceStackOverflow;
+                if (sp >= max_stack) return kTraceStackOverflow;
                 stack[sp++] = StackEntry{n3.y, h1 ? t1 : kNan};
             }
             ref = (n3.x != PICO_REF_EMPTY && h0 && t0 < (in_blas ? lt : best.t)) ? n3.x : pop();
@@ -479,7 +548,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
                 const uint32_t tri = first + k;
                 float t, u, v;
                 if (kCount) cnt->tris++;
-                if (intersect_triangle(sc.tris + tri, q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, t, u, v) && t < lt) {
+                if (intersect<kWT>(sc.tris + tri, q.ox, q.oy, q.oz, q.dx, q.dy, q.dz, t, u, v) && t < lt) {
                     lt = t; ltri = tri; lu = u; lv = v;
                 }
             }
@@ -487,7 +556,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             continue;
         }
         if (count > 1) {
-            if (sp >= kTraceStack) return kTraceStackOverflow;
+            if (sp >= max_stack) return kTraceStackOverflow;
             stack[sp++] = StackEntry{pico_leaf_ref(first + 1, count - 1), -kInf};
         }
         const uint32_t rank = __ldg(sc.tlas_items + first);   // the identity on the reference's tree
@@ -508,7 +577,7 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             ref = pop();
             continue;
         }
-        if (sp >= kTraceStack) return kTraceStackOverflow;
+        if (sp >= max_stack) return kTraceStackOverflow;
         stack[sp++] = StackEntry{PICO_REF_END_BLAS, -kInf};
         in_blas = true;
         cur = rank;
@@ -523,8 +592,11 @@ __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o
                                              TraceCounters* cnt)
 {
     constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
-    if ((kVariant & kReferenceOrder) != 0) return trace_reference_order<kCount, kImplicit>(sc, o, d, best, cnt);
-    return trace_near_first<kCount, kImplicit>(sc, o, d, best, cnt);
+    constexpr bool kRuntime = (kVariant & kBounded) != 0;
+    constexpr bool kWT = (kVariant & kWatertight) != 0;
+    if ((kVariant & kReferenceOrder) != 0)
+        return trace_reference_order<kCount, kImplicit, kRuntime, kWT>(sc, o, d, best, cnt);
+    return trace_near_first<kCount, kImplicit, false, kRuntime, kWT>(sc, o, d, best, cnt);
 }
 
 // Whether anything lies at a world distance below tmax along the ray (closest-hit
@@ -536,13 +608,15 @@ __device__ __forceinline__ int trace_occluded(const SceneView& sc, const float4 
                                               bool& occluded, TraceCounters* cnt = nullptr)
 {
     constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
+    constexpr bool kRuntime = (kVariant & kBounded) != 0;
+    constexpr bool kWT = (kVariant & kWatertight) != 0;
     TraceHit h;
     int s;
     if ((kVariant & kReferenceOrder) != 0) {
-        s = trace_reference_order<kCount, kImplicit>(sc, o, d, h, cnt);
+        s = trace_reference_order<kCount, kImplicit, kRuntime, kWT>(sc, o, d, h, cnt);
         occluded = h.rank != kNoHit && h.t < tmax;
     } else {
-        s = trace_near_first<kCount, kImplicit, true>(sc, o, d, h, cnt, tmax);
+        s = trace_near_first<kCount, kImplicit, true, kRuntime, kWT>(sc, o, d, h, cnt, tmax);
         occluded = h.rank != kNoHit;
     }
     return s;
@@ -567,15 +641,33 @@ __device__ __forceinline__ void flush_counters(TraceCounters c, unsigned long lo
     }
 }
 
+// Whether a launch with this view reads its traversal bounds at run time.
+__host__ __device__ inline bool bounded_view(const SceneView& sc)
+{
+    return sc.max_iterations != kTraceMaxIter || sc.stack_entries != (uint32_t)kTraceStack;
+}
+
 // Calls f(std::integral_constant<int, V>) for the kernel variant V of (order, scene).
 template <class F>
 __host__ auto with_variant(int order, const SceneView& sc, F&& f)
 {
-    switch (traversal_variant(order, sc.has_implicit != 0)) {
+    switch (traversal_variant(order, sc.has_implicit != 0, bounded_view(sc), sc.watertight != 0)) {
     case 0: return f(std::integral_constant<int, 0>{});
     case 1: return f(std::integral_constant<int, 1>{});
     case 2: return f(std::integral_constant<int, 2>{});
-    default: return f(std::integral_constant<int, 3>{});
+    case 3: return f(std::integral_constant<int, 3>{});
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 5: return f(std::integral_constant<int, 5>{});
+    case 6: return f(std::integral_constant<int, 6>{});
+    case 7: return f(std::integral_constant<int, 7>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 9: return f(std::integral_constant<int, 9>{});
+    case 10: return f(std::integral_constant<int, 10>{});
+    case 11: return f(std::integral_constant<int, 11>{});
+    case 12: return f(std::integral_constant<int, 12>{});
+    case 13: return f(std::integral_constant<int, 13>{});
+    case 14: return f(std::integral_constant<int, 14>{});
+    default: return f(std::integral_constant<int, 15>{});
     }
 }
 

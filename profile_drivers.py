@@ -13,6 +13,13 @@ package).
     python profile_drivers.py cornell [--passes K]
         K renders of the Cornell box at 256x256, 16 spp, depth 5, denoised
         (after one warm-up render)
+    python profile_drivers.py trace [--reps K] [--rays N]
+        K closest-hit passes over the instance-field batch (4096 level-4 icospheres,
+        N rays: half primary rays of a 4096^2 pinhole, half cosine bounce rays),
+        device buffers, after one warm-up pass
+    python profile_drivers.py atrous [--reps K]
+        K a-trous calls on 1920x1080 device buffers (seeded values), a 512 MiB L2
+        flush before each, after one warm-up call
     python profile_drivers.py batch [--renders N] [--scale S]
         N renders of the batched-rendering workload (resolutions times S) in one
         CUDA-graph launch, physical estimator, 2^22-path wavefront, 64-thread
@@ -101,6 +108,42 @@ def cornell(passes: int) -> None:
     ctx.close()
 
 
+def trace(reps: int, nrays: int) -> None:
+    import torch
+    ctx = pico_gb300.Context(0)
+    scene = scenes.instance_field(n_instances=4096, level=4, seed=12345)
+    rays = scenes.field_rays(scene, n_total=nrays, resolution=4096, seed=7)
+    gs = ctx.upload(scene)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(len(rays) * 20, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(reps + 1):
+        gs.trace_closest_device(d_rays.data_ptr(), len(rays), d_hits.data_ptr(), s)
+    gs.check(s)
+    print(f"trace driver: {reps + 1} passes of {len(rays)} rays")
+    gs.free()
+    ctx.close()
+
+
+def atrous(reps: int) -> None:
+    import torch
+    ctx = pico_gb300.Context(0)
+    W, H = 1920, 1080
+    rng = np.random.default_rng(5)
+    bufs = [torch.from_numpy(a).cuda() for a in (
+        rng.gamma(1.0, 1.0, (H, W, 3)).astype(np.float32), rng.normal(size=(H, W, 3)).astype(np.float32),
+        (rng.normal(size=(H, W, 3)) * 3).astype(np.float32), rng.random((H, W, 3)).astype(np.float32))]
+    out = torch.empty_like(bufs[0])
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    for _ in range(reps + 1):
+        flush.fill_(1)
+        ctx.atrous_device(*[b.data_ptr() for b in bufs], W, H, out.data_ptr(), s)
+    torch.cuda.synchronize()
+    print(f"atrous driver: {reps + 1} calls")
+    ctx.close()
+
+
 def batch(renders: int, scale: float) -> None:
     ctx = pico_gb300.Context(0)
     work = scenes.batch_workload(renders, size_scale=scale)
@@ -116,7 +159,8 @@ def batch(renders: int, scale: float) -> None:
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["cache", "cache-render", "render", "batch", "cornell"])
+    ap.add_argument("what", choices=["cache", "cache-render", "render", "batch", "cornell", "trace", "atrous"])
+    ap.add_argument("--rays", type=int, default=1 << 24)
     ap.add_argument("--renders", type=int, default=16)
     ap.add_argument("--scale", type=float, default=0.5)
     ap.add_argument("--queries", type=int, default=1 << 21)
@@ -133,6 +177,10 @@ def main() -> None:
         render(a.estimator, a.passes)
     elif a.what == "cornell":
         cornell(a.passes)
+    elif a.what == "trace":
+        trace(a.reps, a.rays)
+    elif a.what == "atrous":
+        atrous(a.reps)
     else:
         batch(a.renders, a.scale)
 

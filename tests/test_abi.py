@@ -75,3 +75,22 @@ def test_init_without_a_device_fails_cleanly(lib):
     st = lib.pico_gpu_init(0, C.byref(h))
     assert st in (-7, -2), st
     assert not h.value
+
+
+@pytest.mark.parametrize("prefix", ["cornell", "field"])
+def test_product_sah_matches_the_reference_node_for_node(lib, prefix):
+    """The BVHs pico_gpu_scene_upload builds (before flattening) equal the reference's own
+    BVH<T,2> nodes, generated from the reference's code (tests/golden/trace.npz): the same
+    boxes bit for bit, children, leaf ranges and leaf items, for every BLAS and the TLAS."""
+    import sys
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "tests" / "golden"))
+    from scene_io import load_scene
+    z = np.load(ROOT / "tests" / "golden" / "trace.npz")
+    scene = load_scene(z, prefix)
+    trees = [(f"{prefix}_blas{mi}", mi) for mi in range(len(scene.meshes))] + [(f"{prefix}_tlas", -1)]
+    for key, which in trees:
+        boxes, links, values = pico_gb300.reference_bvh(scene, which)
+        np.testing.assert_array_equal(boxes.view(np.uint32), z[f"{key}_boxes"].view(np.uint32), err_msg=key)
+        np.testing.assert_array_equal(links, z[f"{key}_links"], err_msg=key)
+        np.testing.assert_array_equal(values, z[f"{key}_values"], err_msg=key)
