@@ -611,6 +611,7 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
                                                                    float max_variance, bool physical)
 {
     using namespace ex;
+    uint32_t added = 0;   // samples this thread added to its pixels
     for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < b.npix; slot += gridDim.x * blockDim.x) {
         const uint32_t pixel = b.pix_list[slot];
         if (b.done[pixel]) continue;
@@ -648,7 +649,12 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         if (taken >= max_samples) b.done[pixel] = 1;
         b.count[pixel] = cnt;
         b.taken[pixel] = taken;
-        if (b.sample_tally) atomicAdd(b.sample_tally, (unsigned long long)(taken - taken0));
+        added += taken - taken0;
+    }
+    if (b.sample_tally) {
+        // one atomic per warp: every thread of the block gets here
+        const uint32_t warp_total = __reduce_add_sync(0xffffffffu, added);
+        if ((threadIdx.x & 31u) == 0 && warp_total) atomicAdd(b.sample_tally, (unsigned long long)warp_total);
     }
 }
 
@@ -702,10 +708,14 @@ __global__ void __launch_bounds__(128) gbuffer_kernel(SceneView sc, CameraView c
 }
 
 // ---------------------------------------------------------------- launchers
-static unsigned grid_for(uint32_t n, int threads)
+// Grid of a grid-stride loop over n items: enough blocks for the items, at most one
+// full wave of the kernel's resident blocks.  Every block runs the same number of
+// rounds, so a partial second wave would take as long as a full one.
+template <class Kernel>
+static unsigned grid_for(Kernel* kernel, uint32_t n, int threads)
 {
     const uint64_t want = ((uint64_t)n + threads - 1) / threads;
-    const uint64_t cap = (uint64_t)sm_count() * 8;
+    const uint64_t cap = (uint64_t)sm_count() * (uint64_t)resident_blocks((const void*)kernel, threads);
     return (unsigned)(want < 1 ? 1 : (want > cap ? cap : want));
 }
 
@@ -828,10 +838,10 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
         if (physical)
-            shade_physical_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth,
+            shade_physical_kernel<<<grid_for(shade_physical_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth,
                                                                                          max_depth, nrc);
         else
-            shade_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
+            shade_kernel<<<grid_for(shade_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
                                                                                     trace_last);
         cur ^= 1;
     }
@@ -848,10 +858,10 @@ cudaError_t launch_training_paths(const SceneView& sc, PathBatch& b, const Camer
     cudaError_t e = cudaMemsetAsync(t.counters, 0, 4 * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(nrc.count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    train_raygen_kernel<<<grid_for(n, kRenderThreads), kRenderThreads, 0, st>>>(t, cam, seed, frame, W, W * H);
+    train_raygen_kernel<<<grid_for(train_raygen_kernel, n, kRenderThreads), kRenderThreads, 0, st>>>(t, cam, seed, frame, W, W * H);
     e = run_depth_loop(sc, t, max_depth, true, nrc, status, order, st);
     if (e != cudaSuccess) return e;
-    nrc_targets_kernel<<<grid_for(nrc.capacity, kRenderThreads), kRenderThreads, 0, st>>>(
+    nrc_targets_kernel<<<grid_for(nrc_targets_kernel, nrc.capacity, kRenderThreads), kRenderThreads, 0, st>>>(
         nrc.queries, nrc.rec_tp, t.pay, nrc.count, nrc.capacity, targets);
     return cudaGetLastError();
 }
@@ -869,7 +879,7 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     cudaError_t e = cudaMemsetAsync(b.counters, 0, 4 * sizeof(uint32_t), st);
     if (e == cudaSuccess && na.mode != kNrcOff) e = cudaMemsetAsync(na.count, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return e;
-    raygen_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
+    raygen_kernel<<<grid_for(raygen_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(b, cam, seed, physical);
     e = run_depth_loop(sc, b, max_depth, physical, na, status, order, st, probe);
     if (e != cudaSuccess) return e;
     if (na.mode == kNrcTerminate) {
@@ -877,8 +887,8 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
                               na.count, na.infer_groups);
         if (e != cudaSuccess) return e;
     }
-    finish_kernel<<<grid_for(b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
-    accumulate_kernel<<<grid_for(b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,
+    finish_kernel<<<grid_for(finish_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(b);
+    accumulate_kernel<<<grid_for(accumulate_kernel, b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,
                                                                                     physical);
     return cudaGetLastError();
 }
@@ -887,7 +897,7 @@ cudaError_t launch_prepare_image(const uint32_t* count, uint32_t npx, uint32_t m
                                  uint32_t* done, uint32_t* taken, cudaStream_t st)
 {
     if (npx == 0) return cudaSuccess;
-    prepare_image_kernel<<<grid_for(npx, kRenderThreads), kRenderThreads, 0, st>>>(count, npx, max_samples, pix_list,
+    prepare_image_kernel<<<grid_for(prepare_image_kernel, npx, kRenderThreads), kRenderThreads, 0, st>>>(count, npx, max_samples, pix_list,
                                                                                   done, taken);
     return cudaGetLastError();
 }
@@ -896,7 +906,7 @@ cudaError_t launch_gbuffer(const SceneView& sc, const CameraView& cam, uint32_t 
                            float* positions, float* diffuse, DeviceStatus* status, int order, cudaStream_t st)
 {
     with_variant(order, sc, [&](auto v) {
-        gbuffer_kernel<decltype(v)::value><<<grid_for(W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions,
+        gbuffer_kernel<decltype(v)::value><<<grid_for(gbuffer_kernel<decltype(v)::value>, W * H, 128), 128, 0, st>>>(sc, cam, W, H, normals, positions,
                                                                                  diffuse, &status->trace_error);
     });
     return cudaGetLastError();

@@ -19,6 +19,9 @@ struct DeviceStatus {
 };
 
 int sm_count();
+// Blocks of `threads` threads of `kernel` resident on one SM at once (at least 1), cached per
+// kernel and block size.
+int resident_blocks(const void* kernel, int threads);
 
 cudaError_t launch_trace(const SceneView& sc, const pico_ray* rays, uint64_t n, pico_hit* hits,
                          DeviceStatus* status, bool count, int order, cudaStream_t stream);

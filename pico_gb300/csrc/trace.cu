@@ -10,6 +10,10 @@
 #include "kernels.h"
 #include "traverse.cuh"
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace pico {
 
 constexpr int kTraceThreads = 128;
@@ -63,6 +67,23 @@ int sm_count()
         if (sms <= 0) sms = 1;
     }
     return sms;
+}
+
+int resident_blocks(const void* kernel, int threads)
+{
+    static std::mutex mu;
+    static std::map<std::pair<const void*, int>, int> cache;
+    const std::pair<const void*, int> key(kernel, threads);
+    std::lock_guard<std::mutex> lock(mu);
+    const auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) != cudaSuccess || n < 1) {
+        cudaGetLastError();   // a failed query leaves no error behind for the next launch check
+        n = 1;
+    }
+    cache.emplace(key, n);
+    return n;
 }
 
 template <bool kCount, int kOrder>

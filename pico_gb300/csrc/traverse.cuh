@@ -76,6 +76,76 @@ __device__ __forceinline__ float slab_fast(float lox, float hix, float loy, floa
     return tmin;
 }
 
+// max / min that return NaN when either input is NaN (PTX max.NaN / min.NaN).
+__device__ __forceinline__ float max_nan(float a, float b)
+{
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float min_nan(float a, float b)
+{
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+// One axis of slab_robust: the entry and exit distances of the face pair [lo - e, hi + e], each
+// rounded outwards (entry down, exit up), then widened by 2^-23 of its magnitude for the error of
+// the rounded reciprocal r (within 2^-24 of 1 / d).  An infinite r (a zero direction component)
+// becomes +-2^64: the ray is taken as nearly parallel, which still meets a slab it lies in and
+// puts a slab it lies outside beyond any finite distance (or at an infinite one, a miss).
+__device__ __forceinline__ void robust_axis(float lo, float hi, float o, float r, float e, float& tn, float& tf)
+{
+    const float lo_w = __fsub_rd(lo, e), hi_w = __fadd_ru(hi, e);
+    const float rr = fabsf(r) == __int_as_float(0x7f800000) ? copysignf(0x1p64f, r) : r;
+    const bool pos = rr >= 0.0f;
+    const float n = __fmul_rd(pos ? __fsub_rd(lo_w, o) : __fsub_ru(hi_w, o), rr);
+    const float f = __fmul_ru(pos ? __fsub_ru(hi_w, o) : __fsub_rd(lo_w, o), rr);
+    tn = __fmaf_rd(-fabsf(n), 0x1p-23f, n);
+    tf = __fmaf_ru(fabsf(f), 0x1p-23f, f);
+}
+
+// The watertight variant's box test (after Ize, "Robust BVH Ray Traversal", JCGT 2(2), 2013): it
+// never rejects a box that the exact ray meets, nor one holding a triangle that the watertight
+// test can report hit.  That test decides coverage from the vertices translated to the ray origin
+// and sheared, rounding each step once, so what it counts as a hit can lie a few ulps of the
+// coordinates in play (the origin's and the vertices') off the exact triangle; every face of the
+// box moves outwards by 2^-18 of the largest such magnitude (omag: the ray origin's, plus the
+// box's own), far above that error.  A vertex shared by a closed fan lies on the faces of the
+// fan's sub-boxes, where the exact slab arithmetic can reject every one of them.  NaN in a box
+// (an empty child) gives a NaN entry distance and a miss.
+__device__ __forceinline__ float slab_robust(float lox, float hix, float loy, float hiy, float loz, float hiz,
+                                             float ox, float oy, float oz, float ix, float iy, float iz, float omag,
+                                             bool& hit)
+{
+    const float bmag = fmaxf(fmaxf(fmaxf(fabsf(lox), fabsf(hix)), fmaxf(fabsf(loy), fabsf(hiy))),
+                             fmaxf(fabsf(loz), fabsf(hiz)));
+    const float e = __fmul_ru(__fadd_ru(omag, bmag), 0x1p-18f);
+    float n1, f1, n2, f2, n3, f3;
+    robust_axis(lox, hix, ox, ix, e, n1, f1);
+    robust_axis(loy, hiy, oy, iy, e, n2, f2);
+    robust_axis(loz, hiz, oz, iz, e, n3, f3);
+    const float tmin = max_nan(max_nan(n1, n2), n3);
+    const float tmax = min_nan(min_nan(f1, f2), f3);
+    hit = tmax >= 0.0f && tmin <= tmax;
+    return tmin;
+}
+
+// The box test of a traversal: slab_robust in the watertight variant, else the
+// reference's slab arithmetic (its NaN-free form where `fast`).
+template <bool kWT>
+__device__ __forceinline__ float box_test(float lox, float hix, float loy, float hiy, float loz, float hiz, float ox,
+                                          float oy, float oz, float ix, float iy, float iz, float omag, bool fast,
+                                          bool& hit)
+{
+    if constexpr (kWT) return slab_robust(lox, hix, loy, hiy, loz, hiz, ox, oy, oz, ix, iy, iz, omag, hit);
+    if (fast) return slab_fast(lox, hix, loy, hiy, loz, hiz, ox, oy, oz, ix, iy, iz, hit);
+    return slab(lox, hix, loy, hiy, loz, hiz, ox, oy, oz, ix, iy, iz, hit);
+}
+
+__device__ __forceinline__ float max_abs3(float a, float b, float c) { return fmaxf(fmaxf(fabsf(a), fabsf(b)), fabsf(c)); }
+
 __device__ __forceinline__ bool all_finite(float a, float b, float c, float d, float e, float f)
 {
     return isfinite(a) && isfinite(b) && isfinite(c) && isfinite(d) && isfinite(e) && isfinite(f);
@@ -323,6 +393,8 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
     // finite float so that one comparison also rejects boxes at +inf.
     float cx = o.x, cy = o.y, cz = o.z, cix = wix, ciy = wiy, ciz = wiz;
     bool cfast = wfast;
+    const float wmag = kWT ? max_abs3(o.x, o.y, o.z) : 0.0f;   // the box slack's origin term (watertight only)
+    float cmag = wmag;
     float limit = kAnyHit ? fminf(tmax, kMaxFinite) : kMaxFinite;
     float qdx = 0.0f, qdy = 0.0f, qdz = 0.0f;   // object-space direction of the instance being searched
     float gl = kInf, lt = kInf, lu = 0.0f, lv = 0.0f;
@@ -342,7 +414,8 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             hi[a] = axis ? sc.tlas_hi[a] : sc.tlas_fast_hi[a];
         }
         bool h;
-        const float tm = slab(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], o.x, o.y, o.z, wix, wiy, wiz, h);
+        const float tm = box_test<kWT>(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2], o.x, o.y, o.z, wix, wiy, wiz, wmag,
+                                       false, h);
         if (h && tm < kInf) ref = axis ? sc.tlas_root_ref : sc.tlas_fast_root_ref;
     }
     for (uint32_t iter = 0;; ++iter) {
@@ -358,7 +431,10 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             }
             bool h0, h1;
             float t0, t1;
-            if (cfast) {
+            if constexpr (kWT) {
+                t0 = slab_robust(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, cx, cy, cz, cix, ciy, ciz, cmag, h0);
+                t1 = slab_robust(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, cx, cy, cz, cix, ciy, ciz, cmag, h1);
+            } else if (cfast) {
                 t0 = slab_fast(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, cx, cy, cz, cix, ciy, ciz, h0);
                 t1 = slab_fast(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, cx, cy, cz, cix, ciy, ciz, h1);
             } else {
@@ -396,6 +472,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             cx = o.x; cy = o.y; cz = o.z;
             cix = __frcp_rn(d.x); ciy = __frcp_rn(d.y); ciz = __frcp_rn(d.z);
             cfast = wfast;
+            cmag = wmag;
             limit = fminf(best.t, kMaxFinite);
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
@@ -449,8 +526,9 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             gl = (best.t * 1.001f + omag) * inv_len;
         }
         bool h;
-        const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
-                              q.oy, q.oz, q.ix, q.iy, q.iz, h);
+        const float qmag = kWT ? max_abs3(q.ox, q.oy, q.oz) : 0.0f;
+        const float tm = box_test<kWT>(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z,
+                                       q.ox, q.oy, q.oz, q.ix, q.iy, q.iz, qmag, false, h);
         if (!(h && tm < kInf && tm <= gl)) {
             ref = sp ? stack[--sp] : PICO_REF_DONE;
             continue;
@@ -461,6 +539,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
         cx = q.ox; cy = q.oy; cz = q.oz; cix = q.ix; ciy = q.iy; ciz = q.iz;
         qdx = q.dx; qdy = q.dy; qdz = q.dz;
         cfast = sc.finite_boxes && all_finite(q.ox, q.oy, q.oz, q.ix, q.iy, q.iz);
+        cmag = qmag;
         limit = fminf(gl, kMaxFinite);   // lt starts at +inf
         cur = rank;
         lt = kInf; ltri = kNoHit;
@@ -499,11 +578,13 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
         return PICO_REF_DONE;
     };
 
+    const float wmag = kWT ? max_abs3(o.x, o.y, o.z) : 0.0f;   // the box slack's origin term (watertight only)
+    float qmag = 0.0f;
     uint32_t ref = PICO_REF_DONE;
     {
         bool h;
-        const float tm = slab(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2], sc.tlas_hi[2],
-                              o.x, o.y, o.z, wix, wiy, wiz, h);
+        const float tm = box_test<kWT>(sc.tlas_lo[0], sc.tlas_hi[0], sc.tlas_lo[1], sc.tlas_hi[1], sc.tlas_lo[2],
+                                       sc.tlas_hi[2], o.x, o.y, o.z, wix, wiy, wiz, wmag, false, h);
         if (h && tm < kInf) ref = sc.tlas_root_ref;
     }
     for (uint32_t iter = 0;; ++iter) {
@@ -516,9 +597,10 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             if (kCount) cnt->nodes++;
             const float rx = in_blas ? q.ox : o.x, ry = in_blas ? q.oy : o.y, rz = in_blas ? q.oz : o.z;
             const float rix = in_blas ? q.ix : wix, riy = in_blas ? q.iy : wiy, riz = in_blas ? q.iz : wiz;
+            const float rmag = in_blas ? qmag : wmag;
             bool h0, h1;
-            const float t0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, h0);
-            const float t1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, h1);
+            const float t0 = box_test<kWT>(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, rx, ry, rz, rix, riy, riz, rmag, false, h0);
+            const float t1 = box_test<kWT>(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, rx, ry, rz, rix, riy, riz, rmag, false, h1);
             // child 1 waits on the stack and is tested when reached
             if (n3.y != PICO_REF_EMPTY) {
                 if (sp >= max_stack) return kTraceStackOverflow;
@@ -570,9 +652,10 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
             continue;
         }
         q = to_object(sc.insts + rank, o, d);
+        if (kWT) qmag = max_abs3(q.ox, q.oy, q.oz);
         bool h;
-        const float tm = slab(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z, q.ox,
-                              q.oy, q.oz, q.ix, q.iy, q.iz, h);
+        const float tm = box_test<kWT>(q.root_lo.x, q.root_hi.x, q.root_lo.y, q.root_hi.y, q.root_lo.z, q.root_hi.z,
+                                       q.ox, q.oy, q.oz, q.ix, q.iy, q.iz, qmag, false, h);
         if (!(h && tm < kInf)) {
             ref = pop();
             continue;

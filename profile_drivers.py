@@ -7,8 +7,8 @@ package).
         (uniformly random positions over a 400 x 125 x 400 box, seeded)
     python profile_drivers.py cache-render [--passes K]
         a 1920x1080 render of the lit field through the radiance cache
-    python profile_drivers.py render [--estimator E] [--passes K]
-        a 1920x1080 render of the lit field, K samples per pixel, estimator E
+    python profile_drivers.py render [--estimator E] [--passes K] [--width W --height H]
+        a render of the lit field (1920x1080 by default), K samples per pixel, estimator E
         (0 the reference's, 1 the physical one)
     python profile_drivers.py cornell [--passes K]
         K renders of the Cornell box at 256x256, 16 spp, depth 5, denoised
@@ -88,10 +88,10 @@ def cache_render(passes: int) -> None:
     ctx.close()
 
 
-def render(estimator: int, passes: int) -> None:
+def render(estimator: int, passes: int, width: int, height: int) -> None:
     ctx = pico_gb300.Context(0)
     gs = ctx.upload(scenes.lit_field())
-    gs.render(scenes.lit_field_camera(1920, 1080), 8, passes, seed=99, estimator=estimator)
+    gs.render(scenes.lit_field_camera(width, height), 8, passes, seed=99, estimator=estimator)
     print("render driver:", ctx.render_stats())
     gs.free()
     ctx.close()
@@ -161,6 +161,8 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["cache", "cache-render", "render", "batch", "cornell", "trace", "atrous"])
     ap.add_argument("--rays", type=int, default=1 << 24)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--renders", type=int, default=16)
     ap.add_argument("--scale", type=float, default=0.5)
     ap.add_argument("--queries", type=int, default=1 << 21)
@@ -174,7 +176,7 @@ def main() -> None:
     elif a.what == "cache-render":
         cache_render(a.passes)
     elif a.what == "render":
-        render(a.estimator, a.passes)
+        render(a.estimator, a.passes, a.width, a.height)
     elif a.what == "cornell":
         cornell(a.passes)
     elif a.what == "trace":

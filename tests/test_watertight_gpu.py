@@ -5,11 +5,15 @@ ray through the crack between two triangles that share an edge or a vertex: each
 triangle rounds its own barycentrics and both can reject a ray that passes exactly
 between them.  The watertight test (Woop, Benthin and Wald, JCGT 2013) evaluates
 the shared edge's function bit-identically, negated, in both triangles, so such a
-ray always hits one of them.  Checked here on rays aimed at points of shared
-edges (quads split along a diagonal) and at shared vertices (closed triangle fans
-around an interior vertex), in both traversal orders; and away from edges the
-watertight test finds the same triangles as the reference's test, with distances
-equal to 1e-5.
+ray always hits one of them; and the variant's box tests are conservative (a
+vertex shared by a closed fan lies on the faces of the fan's sub-boxes, where the
+reference's slab arithmetic can reject every one of them).  Checked here on rays
+aimed at points of shared edges (quads split along a diagonal) and at shared
+vertices (closed triangle fans around an interior vertex), in both traversal
+orders; and away from edges the watertight variant finds the same triangles as
+the reference's test, with distances equal up to rounding (1e-5 relative, or
+4e-7 of the coordinates' magnitude: the world distance is taken between points
+whose coordinates carry that much rounding).
 """
 import numpy as np
 import pytest
@@ -71,14 +75,18 @@ def shared_edge_scene(nquads, per, seed):
 
 def shared_vertex_scene(nfans, per, seed, k=7):
     """Closed fans of k triangles around an interior vertex, in general position; `per` rays per
-    fan aimed exactly at that vertex."""
+    fan aimed exactly at that vertex.  The ring's angles are even or jittered, every angular gap
+    below pi: a gap above pi would fold its triangle over to the other side, and the fan would no
+    longer cover the plane around the vertex (rays passing on the open side miss rightly)."""
     rng = np.random.default_rng(seed)
     s = SceneData(materials=[Material(diffuse=(0.5, 0.5, 0.5))])
     targets, normals, owner = [], [], []
     for f in range(nfans):
         c = rng.uniform(-300.0, 300.0, 3)
         a, b, n = frame(rng)
-        ang = np.sort(rng.uniform(0, 2 * np.pi, k)) if f % 2 else np.linspace(0, 2 * np.pi, k, endpoint=False)
+        jitter = rng.uniform(-0.45, 0.45, k) if f % 2 else np.zeros(k)
+        ang = (np.arange(k) + jitter) * (2 * np.pi / k)
+        assert np.diff(np.append(ang, ang[0] + 2 * np.pi)).max() < np.pi
         rad = rng.uniform(0.5, 2.0, k)
         ring = c + (rad * np.cos(ang))[:, None] * a + (rad * np.sin(ang))[:, None] * b
         p = np.vstack([c, ring]).astype(np.float32)
@@ -116,7 +124,7 @@ def test_no_ray_passes_between_adjacent_triangles(ctx, order, make):
     assert wt_miss == 0, wt_miss
     # where both hit, the distances agree (the hit point is the same up to rounding)
     both = (mt["inst"] == owner)
-    np.testing.assert_allclose(wt["t"][both], mt["t"][both], rtol=1e-5)
+    np.testing.assert_allclose(wt["t"][both], mt["t"][both], rtol=1e-5, atol=300 * 4e-7)   # |coordinates| < 302
 
 
 def test_watertight_finds_the_reference_triangles_away_from_edges(ctx, oracle):
@@ -131,9 +139,11 @@ def test_watertight_finds_the_reference_triangles_away_from_edges(ctx, oracle):
         same = (got["inst"] == want["inst"]) & (got["prim"] == want["prim"])
         assert same.mean() > 0.999, same.mean()
         hit = same & (want["inst"] != pico_gb300.MISS)
-        np.testing.assert_allclose(got["t"][hit], want["t"][hit], rtol=1e-5)
-        np.testing.assert_allclose(got["u"][hit], want["u"][hit], atol=1e-4)
-        np.testing.assert_allclose(got["v"][hit], want["v"][hit], atol=1e-4)
+        np.testing.assert_allclose(got["t"][hit], want["t"][hit], rtol=1e-5, atol=60 * 4e-7)   # |coordinates| < 60
+        # barycentrics lose digits as the ray grazes the triangle (both forms divide by a determinant
+        # that goes to zero); the largest difference seen over 24,544 hits was 2.6e-4
+        np.testing.assert_allclose(got["u"][hit], want["u"][hit], atol=1e-3)
+        np.testing.assert_allclose(got["v"][hit], want["v"][hit], atol=1e-3)
 
 
 def test_watertight_render_runs_and_the_setting_is_checked(ctx):
