@@ -257,8 +257,8 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                          const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
-/* The render runs in batches of up to 2^24 paths (pixels x samples; 224 bytes of
- * path state each, 3.8 GB at the limit).  With a cancel flag (should_quit not
+/* The render runs in batches of up to 2^24 paths (pixels x samples; 208 bytes of
+ * path state each, 3.5 GB at the limit).  With a cancel flag (should_quit not
  * NULL) it polls *should_quit before every batch and a batch takes at most 16
  * samples per pixel: a 1080p render at 64 spp is eight batches of 8 samples per
  * pixel, about 30 ms each on a GB300, which bounds how soon a cancel is seen. */

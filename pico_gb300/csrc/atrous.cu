@@ -137,11 +137,14 @@ __global__ void __launch_bounds__(kStatsThreads) atrous_stats_kernel(const float
 // min / max are exact, so the grouping is free, and the selects keep std::min /
 // std::max's NaN behaviour (a NaN |position| never replaces a bound).
 constexpr int kRowWarps = 4;
-__device__ __forceinline__ bool in_spans(int c, const int* lo, const int* hi, int m)
+// Whether column (or row) c is read by a tap of the stencil (offsets -2..2 times s, clamped to
+// [0, n - 1]) from some pixel of [a, b]: the union tap_spans lists, tested tap by tap so that
+// everything stays in registers (span arrays indexed at run time would live in local memory).
+__device__ __forceinline__ bool tapped(int c, int a, int b, int s, int n)
 {
     bool in = false;
 #pragma unroll
-    for (int i = 0; i < 5; ++i) in |= (i < m) && lo[i] <= c && c <= hi[i];
+    for (int k = -2; k <= 2; ++k) in |= clampi(a + k * s, 0, n - 1) <= c && c <= clampi(b + k * s, 0, n - 1);
     return in;
 }
 
@@ -156,25 +159,38 @@ __global__ void __launch_bounds__(32 * kRowWarps) atrous_row_range_kernel(const 
     const int y = (int)(task / tiles_x), tx = (int)(task % tiles_x);
     const int x0 = tx * kTile, x1 = min(x0 + kTile, (int)W) - 1;
     const int rx0 = max(x0 - 32, 0), rx1 = min(x1 + 32, (int)W - 1);
+    // the span's positions (at most 128 pixels, 384 floats) staged through shared memory with
+    // consecutive lanes reading consecutive floats, all twelve loads in flight before the first
+    // store, then |position| of columns rx0 + lane + 32 k
+    __shared__ float stage[kRowWarps][3 * 128];
+    float* st = stage[threadIdx.x >> 5];
+    const int nf = 3 * (rx1 - rx0 + 1);
+    const float* row = pos + 3 * ((size_t)y * W + (size_t)rx0);
+    float v[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) v[k] = (lane + 32 * k < nf) ? __ldg(row + lane + 32 * k) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 12; ++k) st[lane + 32 * k] = v[k];
+    __syncwarp();
     float len[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        const int c = rx0 + lane + 32 * k;
-        len[k] = 0.0f;
-        if (c <= rx1) {
-            const size_t f = 3 * ((size_t)y * W + (size_t)c);
-            len[k] = length(v3(__ldg(pos + f), __ldg(pos + f + 1), __ldg(pos + f + 2)));
-        }
+        const int j = lane + 32 * k;
+        len[k] = (rx0 + j <= rx1) ? length(v3(st[3 * j], st[3 * j + 1], st[3 * j + 2])) : 0.0f;
     }
     const float kInf = __int_as_float(0x7f800000);
+    // A tile column at least 16 wide (all but a narrow last one) has overlapping taps at every
+    // spacing up to 16: its columns are then the one range [x0 - 2 s, x1 + 2 s], clamped.
+    const bool wide = x1 - x0 + 1 >= 16;
+#pragma unroll
     for (int level = 0; level < 5; ++level) {
-        int lo[5], hi[5];
-        const int m = tap_spans(x0, x1, 1 << level, (int)W, lo, hi);
+        const int s = 1 << level;
+        const int lo = max(x0 - 2 * s, 0), hi = min(x1 + 2 * s, (int)W - 1);
         float mind = kInf, maxd = -kInf;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             const int c = rx0 + lane + 32 * k;
-            if (c <= rx1 && in_spans(c, lo, hi, m)) {
+            if (c >= lo && c <= hi && (wide || tapped(c, x0, x1, s, (int)W))) {
                 mind = (len[k] < mind) ? len[k] : mind;
                 maxd = (maxd < len[k]) ? len[k] : maxd;
             }
@@ -197,12 +213,12 @@ __global__ void __launch_bounds__(32 * 5) atrous_tile_range_kernel(const float2*
     const int tile = (int)blockIdx.x, level = (int)(threadIdx.x >> 5), lane = threadIdx.x & 31;
     const int tx = tile % tiles_x, y0 = (tile / tiles_x) * kTile;
     const int y1 = min(y0 + kTile, (int)H) - 1;
-    int lo[5], hi[5];
-    const int m = tap_spans(y0, y1, 1 << level, (int)H, lo, hi);
+    const int s = 1 << level;
     const float kInf = __int_as_float(0x7f800000);
     float mind = kInf, maxd = -kInf;
-    for (int i = 0; i < m; ++i)
-        for (int r = lo[i] + lane; r <= hi[i]; r += 32) {
+    // the rows between the first and the last tap, those some tap reads
+    for (int r = max(y0 - 2 * s, 0) + lane; r <= min(y1 + 2 * s, (int)H - 1); r += 32)
+        if (tapped(r, y0, y1, s, (int)H)) {
             const float2 v = rrow[((size_t)level * H + r) * tiles_x + tx];
             mind = (v.x < mind) ? v.x : mind;
             maxd = (maxd < v.y) ? v.y : maxd;

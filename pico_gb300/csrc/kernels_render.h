@@ -38,7 +38,6 @@ struct PathBatch {
     uint32_t* queue[2];
     uint32_t* shadow_queue;
     uint32_t* counters;                // [0], [1]: path queues, [2]: shadow queue
-    float4* samples;                   // per path: final radiance
     // image state (W*H entries)
     float* pixels; float* variance; uint32_t* count; uint32_t* taken; uint32_t* done;
     unsigned long long* sample_tally;  // samples added to the image (set by launch_render_batch)

@@ -84,7 +84,7 @@ cudaError_t reserve_paths(RenderBuffers& r, size_t n)
 {
     cudaError_t e = cudaSuccess;
     for (DeviceBuffer* b : {&r.org, &r.dir, &r.thr, &r.pay, &r.hit, &r.sorg, &r.sdir, &r.scontrib, &r.senergy,
-                            &r.samples, &r.ior_lo, &r.ior_hi})
+                            &r.ior_lo, &r.ior_hi})
         if (e == cudaSuccess) e = b->reserve(n * sizeof(float4));
     for (DeviceBuffer* b : {&r.hit_tri, &r.depth, &r.ior_n, &r.q0, &r.q1, &r.sq})
         if (e == cudaSuccess) e = b->reserve(n * sizeof(uint32_t));
@@ -105,7 +105,6 @@ PathBatch make_batch(RenderBuffers& r, uint32_t n, uint32_t npix, uint32_t W, co
     b.sorg = as<float4>(r.sorg); b.sdir = as<float4>(r.sdir); b.scontrib = as<float4>(r.scontrib);
     b.senergy = as<float4>(r.senergy); b.queue[0] = as<uint32_t>(r.q0); b.queue[1] = as<uint32_t>(r.q1);
     b.shadow_queue = as<uint32_t>(r.sq); b.counters = as<uint32_t>(r.counters);
-    b.samples = as<float4>(r.samples);
     b.pixels = as<float>(r.pixels); b.variance = as<float>(r.variance); b.count = as<uint32_t>(r.count);
     b.taken = as<uint32_t>(r.taken); b.done = as<uint32_t>(r.done);
     return b;
@@ -324,6 +323,8 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
     int status = validate_render(ctx, scene, camera, cfg);
     if (status != PICO_OK) return status;
     if (!pixels || !sample_count || !variance) return set_error(ctx, PICO_ERR_INVALID_ARG, "null argument");
+    if ((size_t)cfg->width * cfg->height > 0xffffffffull)
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "image larger than 2^32 pixels");
     const DeviceScope device_scope(ctx->device);
     cudaStream_t st = ctx->stream;
     RenderBuffers& r = *render_buffers(ctx);
@@ -337,32 +338,46 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
         if (e == cudaSuccess) e = b->reserve(npx * sizeof(uint32_t));
     if (e != cudaSuccess) return cuda_error(ctx, e, "image buffers");
 
-    std::vector<uint32_t> active, done(npx, 0u);
-    active.reserve(npx);
+    // The radiance cache's passes take the pixels still sampling as a compacted list built
+    // here; the other estimators list every pixel on the device (prepare_image_kernel) and
+    // skip the finished ones there, with no host pass over the image.
+    const bool host_list = cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE;
+    std::vector<uint32_t> active, done;
     uint64_t samples_before = 0;
-    for (size_t p = 0; p < npx; ++p) {
-        samples_before += sample_count[p];
-        if (sample_count[p] >= cfg->max_samples) done[p] = 1;
-        else active.push_back((uint32_t)p);
+    if (host_list) {
+        done.assign(npx, 0u);
+        active.reserve(npx);
+        for (size_t p = 0; p < npx; ++p) {
+            samples_before += sample_count[p];
+            if (sample_count[p] >= cfg->max_samples) done[p] = 1;
+            else active.push_back((uint32_t)p);
+        }
     }
     for (uint64_t& v : ctx->render_stats) v = 0;
     e = cudaMemcpyAsync(r.pixels.ptr, pixels, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.variance.ptr, variance, npx * 3 * sizeof(float), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(r.count.ptr, sample_count, npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(r.done.ptr, done.data(), npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(r.taken.ptr, 0, npx * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->status->rays, 0, sizeof(ctx->status->rays), st);
-    if (e == cudaSuccess && !active.empty())
-        e = cudaMemcpyAsync(r.pix_list.ptr, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (host_list) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(r.done.ptr, done.data(), npx * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(r.taken.ptr, 0, npx * sizeof(uint32_t), st);
+        if (e == cudaSuccess && !active.empty())
+            e = cudaMemcpyAsync(r.pix_list.ptr, active.data(), active.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);   // the host vectors end with this call
+    } else if (e == cudaSuccess) {
+        e = launch_prepare_image(as<uint32_t>(r.count), (uint32_t)npx, cfg->max_samples, as<uint32_t>(r.pix_list),
+                                 as<uint32_t>(r.done), as<uint32_t>(r.taken), st);
+    }
     if (e != cudaSuccess) return cuda_error(ctx, e, "render upload");
 
     const CameraView cam = make_camera_view(*camera);
     bool cancelled = false;
-    if (!active.empty() && cfg->max_samples > 0) {
-        status = cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE
-                     ? render_with_cache(ctx, scene, ctx->cache, cfg, cam, r, active.size(), should_quit, cancelled)
-                     : run_sample_batches(ctx, scene, cfg, cam, r, active.size(), as<float>(r.pixels),
+    const size_t nactive = host_list ? active.size() : npx;
+    if (nactive > 0 && cfg->max_samples > 0) {
+        status = host_list
+                     ? render_with_cache(ctx, scene, ctx->cache, cfg, cam, r, nactive, should_quit, cancelled)
+                     : run_sample_batches(ctx, scene, cfg, cam, r, nactive, as<float>(r.pixels),
                                           as<float>(r.variance), as<uint32_t>(r.count), should_quit, st, cancelled);
         if (status != PICO_OK) return status;
     }
@@ -378,9 +393,13 @@ int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
     if (e == cudaSuccess) e = cudaMemcpyAsync(rays, ctx->status->rays, sizeof(rays), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_error(ctx, e, "render download");
-    uint64_t samples_after = 0;
-    for (size_t p = 0; p < npx; ++p) samples_after += sample_count[p];
-    ctx->render_stats[0] = samples_after - samples_before;
+    if (host_list) {
+        uint64_t samples_after = 0;
+        for (size_t p = 0; p < npx; ++p) samples_after += sample_count[p];
+        ctx->render_stats[0] = samples_after - samples_before;
+    } else {
+        ctx->render_stats[0] = rays[3];   // the samples accumulate added, tallied on the device
+    }
     ctx->render_stats[1] = rays[0];
     ctx->render_stats[2] = rays[1];
     ctx->render_stats[3] = rays[2];

@@ -7,7 +7,7 @@
 // Path state and image buffers of one render, grown on demand.
 struct RenderBuffers {
     pico::DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, ior_n, ior_lo, ior_hi, sorg, sdir, scontrib,
-        senergy, q0, q1, sq, counters, samples;
+        senergy, q0, q1, sq, counters;
     pico::DeviceBuffer pixels, variance, count, taken, done, pix_list;
     pico::DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
     // radiance cache: terminal queries / training records, record throughput and
@@ -16,7 +16,7 @@ struct RenderBuffers {
     ~RenderBuffers()
     {
         for (pico::DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
-                                      &sorg, &sdir, &scontrib, &senergy, &q0, &q1, &sq, &counters, &samples, &pixels,
+                                      &sorg, &sdir, &scontrib, &senergy, &q0, &q1, &sq, &counters, &pixels,
                                       &variance, &count, &taken, &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats,
                                       &out, &tonemap, &nrc_q, &nrc_tp, &nrc_tgt, &nrc_prev, &nrc_count})
             b->release();
@@ -25,14 +25,14 @@ struct RenderBuffers {
 
 namespace pico {
 
-// Paths of one batch of a single render (pixels x samples; about 210 B of path
-// state each, 3.5 GB at the limit).  Larger batches amortise each launch and its
+// Paths of one batch of a single render (pixels x samples; 208 B of path state
+// each, 3.5 GB at the limit).  Larger batches amortise each launch and its
 // tail: a 1080p render at 64 spp measured 159 / 206 / 267 / 279 / 286 Msamples/s
 // with batches of 2^19 / 2^20 / 2^22 / 2^23 / 2^24 paths (physical estimator).
 constexpr uint32_t kMaxPaths = 1u << 24;
-// Device bytes of path state per path that reserve_paths allocates: twelve float4
+// Device bytes of path state per path that reserve_paths allocates: eleven float4
 // arrays, six uint32 arrays and the 64-bit random state.
-constexpr size_t kPathStateBytes = 12 * 16 + 6 * 4 + 8;
+constexpr size_t kPathStateBytes = 11 * 16 + 6 * 4 + 8;
 
 template <class T>
 T* as(DeviceBuffer& b) { return static_cast<T*>(b.ptr); }
