@@ -218,6 +218,27 @@ ATROUS_BYTES_PER_PIXEL_LEVEL = 60   # 4 x 12 B in (colour, normal, position, alb
 L2_FLUSH_BYTES = 512 << 20
 
 
+class PinnedImage:
+    """Pinned host image buffers of one resolution, reused by every wall-clock render measurement
+    (as the headline's end-to-end leg): pico_gpu_render from and into page-locked memory, without a
+    cancel flag.  `render` returns its wall time; the image stays in .pix until the next render."""
+
+    def __init__(self, torch, cam):
+        W, H = cam.resolution
+        self._keep = [torch.zeros((H, W, 3), dtype=torch.float32).pin_memory(),
+                      torch.zeros((H, W, 3), dtype=torch.float32).pin_memory(),
+                      torch.zeros((H, W), dtype=torch.int32).pin_memory()]
+        self.pix, self.var = self._keep[0].numpy(), self._keep[1].numpy()
+        self.cnt = self._keep[2].numpy().view(np.uint32)
+
+    def render(self, gs, cam, depth, spp, seed, **kw):
+        self.cnt.fill(0)
+        t0 = time.perf_counter()
+        gs.render(cam, depth, spp, seed=seed, pixels=self.pix, sample_count=self.cnt, variance=self.var,
+                  cancellable=False, **kw)
+        return time.perf_counter() - t0
+
+
 def bench_render(ctx, args, torch, local, estimator=0, with_cpu=True):
     """1080p render of the lit field through pico_gpu_render (host buffers in and out, denoised):
     wall time per render, samples added and rays traced (camera, bounce, shadow, G-buffer).
@@ -225,14 +246,13 @@ def bench_render(ctx, args, torch, local, estimator=0, with_cpu=True):
     scene = scenes.lit_field()
     cam = scenes.lit_field_camera(1920, 1080)
     gs = ctx.upload(scene)
-    gs.render(cam, args.render_depth, 2, seed=99, denoise=True, estimator=estimator)          # warm-up
+    img = PinnedImage(torch, cam)
+    img.render(gs, cam, args.render_depth, 2, 99, denoise=True, estimator=estimator)          # warm-up
     runs = []
     with ClockSampler(local) as clocks:
         for k in range(2):
-            t0 = time.perf_counter()
-            pix, cnt, var = gs.render(cam, args.render_depth, args.render_spp, seed=1 + k, denoise=True,
-                                      estimator=estimator)
-            runs.append((time.perf_counter() - t0, ctx.render_stats()))
+            secs = img.render(gs, cam, args.render_depth, args.render_spp, 1 + k, denoise=True, estimator=estimator)
+            runs.append((secs, ctx.render_stats()))
     secs = float(np.mean([r[0] for r in runs]))
     st = runs[-1][1]
     rays = st["camera_paths"] + st["bounce_rays"] + st["shadow_rays"] + st["gbuffer_rays"]
@@ -243,9 +263,9 @@ def bench_render(ctx, args, torch, local, estimator=0, with_cpu=True):
            "Msamples_per_s": st["samples"] / secs / 1e6, "Mrays_per_s": rays / secs / 1e6,
            "ms_per_render": secs * 1e3, "samples": st["samples"], "camera_paths": st["camera_paths"],
            "rays": {k: st[k] for k in ("camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
-           "timing": "wall clock around pico_gpu_render, host buffers in and out",
+           "timing": "wall clock around pico_gpu_render, pinned host buffers in and out",
            "clocks": clocks.summary()}
-    conv = convergence(ctx, gs, scene, cam, args, pix, estimator)
+    conv = convergence(ctx, gs, scene, cam, args, img, estimator)
     if conv:
         out["relmse"] = conv
     if with_cpu and not args.no_cpu and args.render_cpu_pixels > 0 and estimator == 0:
@@ -254,11 +274,12 @@ def bench_render(ctx, args, torch, local, estimator=0, with_cpu=True):
     return out
 
 
-def convergence(ctx, gs, scene, cam, args, timed_image, estimator=0):
+def convergence(ctx, gs, scene, cam, args, img, estimator=0):
     """relMSE against the converged judge of the lit field (FP64 mean of 4096 samples on 1024
     seeded pixels, of the reference's integrator or, for the physical estimator, of its FP64
     oracle): of the timed render, and of plain renders at 64 and 256 spp (the reference
-    estimator without its early exit), noisy and after the a-trous pass, with their wall time."""
+    estimator without its early exit), noisy and after the a-trous pass, with their wall time.
+    `img` holds the timed render (PinnedImage) and renders the plain ones."""
     sys.path.insert(0, str(ROOT / "tests" / "golden"))
     from judge import Judge
     try:
@@ -269,16 +290,15 @@ def convergence(ctx, gs, scene, cam, args, timed_image, estimator=0):
     if (j.width, j.height) != tuple(cam.resolution) or j.depth != args.render_depth:
         return None
     W, H = cam.resolution
+    timed = j.relmse_finite(img.pix)
     nrm, pos, dif = gs.denoiser_inputs(cam)
     series = []
     for spp in (64, 256):
-        t0 = time.perf_counter()
-        pix, _, _ = gs.render(cam, args.render_depth, spp, seed=500 + spp, max_variance=-1.0, estimator=estimator)
-        secs = time.perf_counter() - t0
+        secs = img.render(gs, cam, args.render_depth, spp, 500 + spp, max_variance=-1.0, estimator=estimator)
+        pix = img.pix
         den, bad = j.relmse_finite(ctx.atrous(pix, nrm, pos, dif, W, H))
         series.append({"spp": spp, "seconds": secs, "relmse": j.relmse(pix), "relmse_denoised": den,
                        "denoised_nan_pixels": bad})
-    timed = j.relmse_finite(timed_image)
     source = "samples of the FP64 oracle of the physical estimator" if estimator else \
         "reference samples (Integrators.cpp:130-154)"
     return {"judge": f"FP64 mean of {j.spp} {source} on {len(j.pixels)} seeded pixels", "eps": 0.01,
@@ -307,19 +327,19 @@ def bench_radiance_cache(ctx, args, torch, local, plain_series):
         j.check_scene(scene)
     except (OSError, KeyError, ValueError):
         j = None
+    img = PinnedImage(torch, cam)
     cfg = dict(seed=3)
     warm = RadianceCache(ctx, **cfg)
     warm.attach()
-    gs.render(cam, args.render_depth, 2, seed=98, estimator=2)
+    img.render(gs, cam, args.render_depth, 2, 98, estimator=2)
     warm.free()
     series = []
     with ClockSampler(local) as clocks:
         for n in args.nrc_passes:
             c = RadianceCache(ctx, **cfg)
             c.attach()
-            t0 = time.perf_counter()
-            pix, cnt, _ = gs.render(cam, args.render_depth, n, seed=700 + n, estimator=2)
-            secs = time.perf_counter() - t0
+            secs = img.render(gs, cam, args.render_depth, n, 700 + n, estimator=2)
+            pix = img.pix
             st, rs = c.stats(), ctx.render_stats()
             rays = rs["camera_paths"] + rs["bounce_rays"] + rs["shadow_rays"]
             series.append({"passes": n, "seconds": secs, "relmse": j.relmse(pix) if j else None,
@@ -334,23 +354,21 @@ def bench_radiance_cache(ctx, args, torch, local, plain_series):
     if j is not None:
         trained = RadianceCache(ctx, **cfg)
         trained.attach()
-        gs.render(cam, args.render_depth, 256, seed=880, estimator=2)
+        img.render(gs, cam, args.render_depth, 256, 880, estimator=2)
         mlp, grid = trained.params()
         trained.free()
         fz = RadianceCache(ctx, **cfg, train_paths=0, max_train_steps=0)
         fz.set_params(mlp, grid)
         fz.attach()
-        gs.render(cam, args.render_depth, 2, seed=881, estimator=2)   # warm-up
+        img.render(gs, cam, args.render_depth, 2, 881, estimator=2)   # warm-up
         for n in (16, 32, 64, 128):
-            t0 = time.perf_counter()
-            pix, _, _ = gs.render(cam, args.render_depth, n, seed=900 + n, estimator=2)
-            secs = time.perf_counter() - t0
-            frozen.append({"passes": n, "seconds": secs, "relmse": j.relmse(pix)})
+            secs = img.render(gs, cam, args.render_depth, n, 900 + n, estimator=2)
+            frozen.append({"passes": n, "seconds": secs, "relmse": j.relmse(img.pix)})
         fz.free()
     out = {"workload": f"lit field 1920x1080, depth {args.render_depth}, radiance cache (16-level hash grid 2^19, "
                        f"SH4, 5 x 64 ReLU, bf16 tcgen05), 65536 training paths and up to 4 Adam steps of 65536 "
                        f"records per pass, paths end after 1 bounce (2 behind roughness < 0.1)",
-           "timing": "wall clock around pico_gpu_render (host buffers in and out), fresh cache per render",
+           "timing": "wall clock around pico_gpu_render (pinned host buffers in and out), fresh cache per render",
            "series": series, "clocks": clocks.summary(),
            "pretrained_frozen": {"series": frozen,
                                  "note": "a cache trained over a 256-pass render, copied into a cache that does not "
@@ -488,27 +506,26 @@ def measured_bf16_peak():
     return 1900.0, "fallback"
 
 
-def bench_cornell(ctx, args, local):
+def bench_cornell(ctx, args, torch, local):
     """The reference's CPU-runnable case: the Cornell box at 256x256, 16 spp, depth 5, reference
-    estimator, a-trous denoise, through pico_gpu_render (host buffers), next to the reference's
+    estimator, a-trous denoise, through pico_gpu_render (pinned host buffers), next to the reference's
     render loop over the whole image on the host cores (its own code where its harness is built,
     else the port; no denoise on the CPU side)."""
     scene = scenes.cornell_box()
     cam = scenes.cornell_camera(256, 256)
     gs = ctx.upload(scene)
-    gs.render(cam, 5, 16, seed=7, denoise=True)   # warm-up
+    img = PinnedImage(torch, cam)
+    img.render(gs, cam, 5, 16, 7, denoise=True)   # warm-up
     times, samples = [], 0
     with ClockSampler(local) as clocks:   # ~0.5 s of renders, long enough for the clock samples
         for k in range(300):
-            t0 = time.perf_counter()
-            gs.render(cam, 5, 16, seed=11 + k, denoise=True)
-            times.append(time.perf_counter() - t0)
+            times.append(img.render(gs, cam, 5, 16, 11 + k, denoise=True))
             samples = ctx.render_stats()["samples"]
     gs.free()
     secs = float(np.median(times))
     out = {"workload": "Cornell box 256x256, 16 spp, depth 5, reference estimator (early exit at zero variance), "
                        "a-trous 5 levels", "ms_per_render": secs * 1e3, "Msamples_per_s": samples / secs / 1e6,
-           "samples": samples, "timing": "median wall clock of 300 pico_gpu_render calls, host buffers in and out",
+           "samples": samples, "timing": "median wall clock of 300 pico_gpu_render calls, pinned host buffers in and out",
            "clocks": clocks.summary()}
     if not args.no_cpu:
         sys.path.insert(0, str(ROOT / "oracle"))
@@ -957,7 +974,7 @@ def main():
             r = cpu_render(scene, cam, args)
             r.pop("seconds")
             cpu_render_line = r
-        extras["cornell_256"] = bench_cornell(ctx, args, local)
+        extras["cornell_256"] = bench_cornell(ctx, args, torch, local)
         extras["render_1080p_physical"] = bench_render(ctx, args, torch, local, estimator=1)
         extras["render_1080p_relmse"] = bench_render(ctx, args, torch, local, estimator=0, with_cpu=False)
         if args.nrc_passes:

@@ -258,10 +258,13 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
 /* The render runs in batches of up to 2^24 paths (pixels x samples; 208 bytes of
- * path state each, 3.5 GB at the limit).  With a cancel flag (should_quit not
- * NULL) it polls *should_quit before every batch and a batch takes at most 16
- * samples per pixel: a 1080p render at 64 spp is eight batches of 8 samples per
- * pixel, about 30 ms each on a GB300, which bounds how soon a cancel is seen. */
+ * path state each, 3.5 GB at the limit).  Where the reference's early exit can
+ * stop pixels (reference estimator, max_variance >= 0) the first batch takes 6
+ * samples per pixel and later batches only the pixels still sampling, as many
+ * samples each as fill the path state; otherwise every batch covers all pixels.
+ * With a cancel flag (should_quit not NULL) it polls *should_quit before every
+ * batch and a batch takes at most 16 samples per pixel: about 30-40 ms each for a
+ * 1080p render on a GB300, which bounds how soon a cancel is seen. */
 int pico_gpu_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_camera* camera,
                     const pico_render_config* config, float* pixels_rgb, uint32_t* sample_count,
                     float* variance_rgb, const volatile int32_t* should_quit);

@@ -8,7 +8,7 @@
 //            light hit adds its radiance)
 //   shade    BSRDF sample, emission, NEE setup, Russian roulette, next ray;
 //            survivors and shadow rays are appended to queues with one
-//            atomic per warp (ballot + popc + shuffle)
+//            atomic per block and queue (block_append)
 // then `accumulate` takes each payload as a sample value (NaN/Inf -> pink, as
 // Integrators.cpp:145-146) and applies the reference's running mean / variance
 // and early-exit rule per pixel, samples in order.
@@ -89,15 +89,16 @@ __global__ void __launch_bounds__(kRenderThreads) raygen_kernel(PathBatch b, Cam
 {
     __shared__ AppendScratch app;
     // whole blocks iterate together so the queue append can use block collectives
+    const uint32_t n = b.plan ? b.plan->n : b.n, npix = b.plan ? b.plan->npix : b.npix;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t rounds = (b.n + stride - 1) / stride;
+    const uint32_t rounds = (n + stride - 1) / stride;
     for (uint32_t r = 0; r < rounds; ++r) {
         const uint32_t i = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
         bool live = false;
         uint32_t pixel = 0, s = 0;
-        if (i < b.n) {
-            const uint32_t slot = i % b.npix;
-            s = i / b.npix;
+        if (i < n) {
+            const uint32_t slot = i % npix;
+            s = i / npix;
             pixel = b.pix_list[slot];
             live = b.done[pixel] == 0;
         }
@@ -657,8 +658,11 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
                                                                    float max_variance, bool physical)
 {
     using namespace ex;
+    const uint32_t npix = b.plan ? b.plan->npix : b.npix;
+    if (b.plan) spb = b.plan->spb;
+    if (spb == 0) return;   // an empty round (the whole grid leaves)
     uint32_t added = 0;   // samples this thread added to its pixels
-    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < b.npix; slot += gridDim.x * blockDim.x) {
+    for (uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x; slot < npix; slot += gridDim.x * blockDim.x) {
         const uint32_t pixel = b.pix_list[slot];
         if (b.done[pixel]) continue;
         float* px = b.pixels + 3 * (size_t)pixel;
@@ -668,7 +672,7 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         const uint32_t taken0 = taken;
         for (uint32_t s = 0; s < spb && taken < max_samples; ++s) {
             // the path's payload is the sample; NaN / Inf becomes pink (Integrators.cpp:145-146)
-            const float4 x4 = b.pay[(size_t)s * b.npix + slot];
+            const float4 x4 = b.pay[(size_t)s * npix + slot];
             const bool finite = isfinite(x4.x) && isfinite(x4.y) && isfinite(x4.z);
             float x[3] = {finite ? x4.x : 1.0f, finite ? x4.y : 0.4f, finite ? x4.z : 0.7f};
             const uint32_t prev = cnt;
@@ -703,6 +707,51 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         // one atomic per warp: every thread of the block gets here
         const uint32_t warp_total = __reduce_add_sync(0xffffffffu, added);
         if ((threadIdx.x & 31u) == 0 && warp_total) atomicAdd(b.sample_tally, (unsigned long long)warp_total);
+    }
+}
+
+// Exit-aware rounds (RoundPlan).  One thread sets the round from the pixels the
+// previous compaction kept.
+__global__ void plan_init_kernel(RoundPlan* p, uint32_t npix)
+{
+    *p = RoundPlan{0u, 0u, 0u, 0u, npix, {0u, 0u, 0u}};
+}
+
+__global__ void plan_round_kernel(RoundPlan* p, uint32_t max_samples, uint32_t first_cap, uint32_t cap,
+                                  uint32_t max_paths)
+{
+    const uint32_t npix = p->next_npix;
+    uint32_t spb = max_samples > p->scheduled ? max_samples - p->scheduled : 0u;
+    spb = min(spb, npix ? max_paths / npix : 0u);
+    if (p->scheduled == 0) spb = min(spb, first_cap);
+    spb = min(spb, cap);
+    p->npix = npix;
+    p->spb = spb;
+    p->n = npix * spb;
+    p->scheduled += spb;
+    p->next_npix = 0;
+}
+
+// The round's pixels that are still sampling, appended to `out` (block order is
+// the atomics', order within a block is kept, so warps keep neighbouring pixels).
+__global__ void __launch_bounds__(kRenderThreads) compact_pixels_kernel(RoundPlan* p, const uint32_t* in,
+                                                                       const uint32_t* done, uint32_t* out)
+{
+    __shared__ AppendScratch app;
+    const uint32_t npix = p->npix;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (npix + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t k = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        uint32_t pixel = 0;
+        bool keep = false;
+        if (k < npix) {
+            pixel = in[k];
+            keep = done[pixel] == 0;
+        }
+        uint32_t at, unused;
+        block_append(r, keep, &p->next_npix, false, nullptr, app, at, unused);
+        if (keep) out[at] = pixel;
     }
 }
 
@@ -937,6 +986,27 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     }
     accumulate_kernel<<<grid_for(accumulate_kernel, b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,
                                                                                     physical);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plan_init(RoundPlan* plan, uint32_t npix, cudaStream_t st)
+{
+    plan_init_kernel<<<1, 1, 0, st>>>(plan, npix);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_plan_round(RoundPlan* plan, uint32_t max_samples, uint32_t first_cap, uint32_t cap,
+                              uint32_t max_paths, cudaStream_t st)
+{
+    plan_round_kernel<<<1, 1, 0, st>>>(plan, max_samples, first_cap, cap, max_paths);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact_pixels(RoundPlan* plan, const uint32_t* in, const uint32_t* done, uint32_t* out,
+                                  uint32_t npix_bound, cudaStream_t st)
+{
+    compact_pixels_kernel<<<grid_for(compact_pixels_kernel, npix_bound, kRenderThreads), kRenderThreads, 0, st>>>(
+        plan, in, done, out);
     return cudaGetLastError();
 }
 

@@ -21,6 +21,20 @@ struct CameraView {
     float view[16];                    // glm::lookAt(pos, pos + dir, up), column-major
 };
 
+// The device-side plan of one sample round of a render with the early exit on
+// (launch_plan_round, launch_compact_pixels): a batch with a plan reads the round's
+// pixel count and samples per pixel from it instead of PathBatch::n / npix and the
+// spb argument, so that the host enqueues rounds without knowing how many pixels
+// are still sampling.
+struct RoundPlan {
+    uint32_t npix;        // pixels listed for this round (all still sampling)
+    uint32_t spb;         // samples per pixel this round (0: the round does nothing)
+    uint32_t n;           // paths of the round: npix * spb
+    uint32_t scheduled;   // samples per pixel the rounds so far took
+    uint32_t next_npix;   // pixels the compaction kept for the next round
+    uint32_t pad[3];
+};
+
 // Structure-of-arrays path state of one batch (capacity >= n) and the
 // per-pixel accumulation buffers of the whole image.
 struct PathBatch {
@@ -41,6 +55,7 @@ struct PathBatch {
     // image state (W*H entries)
     float* pixels; float* variance; uint32_t* count; uint32_t* taken; uint32_t* done;
     unsigned long long* sample_tally;  // samples added to the image (set by launch_render_batch)
+    const RoundPlan* plan;             // null, or the round's n / npix / spb (n and npix above are then bounds)
 };
 
 // Measurement hooks of a render's closest-hit launches: CUDA events recorded on
@@ -93,6 +108,16 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
                                 uint32_t spb, uint32_t max_depth, uint32_t max_samples, float max_variance,
                                 int estimator, DeviceStatus* status, int order, cudaStream_t st,
                                 const NrcShadeArgs* nrc = nullptr, const RenderProbe* probe = nullptr);
+// Exit-aware rounds: plan_init lists npix pixels for the first round; plan_round
+// sets the next round from the pixels the compaction kept: samples per pixel
+// min(max_samples - scheduled, max_paths / pixels, cap), at most first_cap in the
+// first round; compact_pixels keeps the pixels of `in` (plan->npix of them) that
+// are not done, in `out`, counting them in plan->next_npix.
+cudaError_t launch_plan_init(RoundPlan* plan, uint32_t npix, cudaStream_t st);
+cudaError_t launch_plan_round(RoundPlan* plan, uint32_t max_samples, uint32_t first_cap, uint32_t cap,
+                              uint32_t max_paths, cudaStream_t st);
+cudaError_t launch_compact_pixels(RoundPlan* plan, const uint32_t* in, const uint32_t* done, uint32_t* out,
+                                  uint32_t npix_bound, cudaStream_t st);
 // The image state of a render into caller device buffers: every pixel listed in
 // order, done where count >= max_samples, nothing taken yet.
 cudaError_t launch_prepare_image(const uint32_t* count, uint32_t npx, uint32_t max_samples, uint32_t* pix_list,

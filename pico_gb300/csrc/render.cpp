@@ -246,6 +246,67 @@ int validate_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
 // so that a cancel is seen after at most one such batch (on small images a batch
 // could otherwise hold hundreds of samples per pixel).
 constexpr uint32_t kCancelSamplesPerBatch = 16;
+// The reference's early exit can first stop a fresh pixel at its sixth sample
+// (Scene.cpp:193-197: after a sample taken with more than 4 before it), so the
+// first round of an exit-aware render takes six.
+constexpr uint32_t kFirstExitSamples = 6;
+
+// Whether the reference's early exit can stop pixels of this render: the reference
+// estimator with a variance bound that a variance can meet.
+static bool early_exit_on(const pico_render_config* cfg)
+{
+    return cfg->estimator == PICO_ESTIMATOR_REFERENCE && cfg->max_variance >= 0.0f;
+}
+
+// Exit-aware rounds over the first `nactive` pixels of r.pix_list (at most
+// kMaxPaths of them): the first round takes kFirstExitSamples samples per pixel;
+// after every round a compaction keeps the pixels still sampling and the next round
+// takes as many samples per pixel as fill the path state (2^24 paths), so that
+// rounds after the exits are dense.  Both are decided on the device (RoundPlan), so
+// nothing here waits for it: the host enqueues as many rounds as a render with no
+// exit needs, and rounds with nothing left to do launch empty kernels.  Images are
+// the same as with fixed batches: a path's random stream depends on its pixel and
+// sample index only, and every pixel takes its samples in order.
+static int run_exit_aware_rounds(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_render_config* cfg,
+                                 const CameraView& cam, RenderBuffers& r, uint32_t nactive, float* pixels,
+                                 float* variance, uint32_t* count, const volatile int32_t* should_quit,
+                                 cudaStream_t st, bool& cancelled)
+{
+    const uint32_t cap = should_quit ? kCancelSamplesPerBatch : cfg->max_samples;
+    const uint32_t paths = (uint32_t)std::min<uint64_t>(kMaxPaths, (uint64_t)nactive * cfg->max_samples);
+    cudaError_t e = reserve_paths(r, paths);
+    if (e == cudaSuccess) e = r.pix_list2.reserve((size_t)nactive * sizeof(uint32_t));
+    if (e == cudaSuccess) e = r.plan.reserve(sizeof(RoundPlan));
+    if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
+    // rounds a render with no exit needs: the first, then rounds of the smallest
+    // later size (every pixel still sampling)
+    const uint32_t first = std::min({kFirstExitSamples, cfg->max_samples, cap});
+    const uint32_t later = std::max(1u, std::min(paths / nactive, cap));
+    const uint32_t rounds = 1 + (cfg->max_samples - first + later - 1) / later;
+    RoundPlan* plan = as<RoundPlan>(r.plan);
+    uint32_t* lists[2] = {as<uint32_t>(r.pix_list), as<uint32_t>(r.pix_list2)};
+    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr};
+    const RenderProbe* pp = (probe.timer || probe.counters) ? &probe : nullptr;
+    e = launch_plan_init(plan, nactive, st);
+    for (uint32_t k = 0; k < rounds && e == cudaSuccess; ++k) {
+        if (should_quit && *should_quit) { cancelled = true; break; }
+        e = launch_plan_round(plan, cfg->max_samples, first, cap, paths, st);
+        if (e != cudaSuccess) break;
+        PathBatch b = make_batch(r, paths, nactive, cfg->width, lists[k & 1]);
+        b.plan = plan;
+        b.pixels = pixels;
+        b.variance = variance;
+        b.count = count;
+        e = launch_render_batch(traversal_view(ctx, scene), b, cam, cfg->seed, 0, cfg->max_ray_depth, cfg->max_samples,
+                                cfg->max_variance, (int)cfg->estimator, ctx->status, scene_order(ctx, scene), st,
+                                nullptr, pp);
+        if (e == cudaSuccess && k + 1 < rounds)
+            e = launch_compact_pixels(plan, lists[k & 1], as<uint32_t>(r.done), lists[(k + 1) & 1], nactive, st);
+        if (e == cudaSuccess && should_quit) e = cudaStreamSynchronize(st);
+    }
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render round");
+    return PICO_OK;
+}
 
 // The sample batches of a reference or physical render over the first `nactive`
 // pixels of r.pix_list, advancing the image buffers (pixels, variance, count) and
@@ -255,6 +316,9 @@ int run_sample_batches(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pic
                        const CameraView& cam, RenderBuffers& r, size_t nactive, float* pixels, float* variance,
                        uint32_t* count, const volatile int32_t* should_quit, cudaStream_t st, bool& cancelled)
 {
+    if (early_exit_on(cfg) && nactive <= kMaxPaths)
+        return run_exit_aware_rounds(ctx, scene, cfg, cam, r, (uint32_t)nactive, pixels, variance, count, should_quit,
+                                     st, cancelled);
     const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, kMaxPaths);
     uint32_t spb_cap = kMaxPaths / chunk_pix;
     if (should_quit) spb_cap = std::min(spb_cap, kCancelSamplesPerBatch);

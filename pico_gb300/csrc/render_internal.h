@@ -9,6 +9,7 @@ struct RenderBuffers {
     pico::DeviceBuffer org, dir, thr, pay, hit, hit_tri, rng, depth, ior_n, ior_lo, ior_hi, sorg, sdir, scontrib,
         senergy, q0, q1, sq, counters;
     pico::DeviceBuffer pixels, variance, count, taken, done, pix_list;
+    pico::DeviceBuffer pix_list2, plan;   // exit-aware rounds: the compacted pixel list, the round plan
     pico::DeviceBuffer gn, gp, gd, ga, gb, stats, out, tonemap;
     // radiance cache: terminal queries / training records, record throughput and
     // payload, targets, previous roughness per path, entry counters
@@ -17,7 +18,8 @@ struct RenderBuffers {
     {
         for (pico::DeviceBuffer* b : {&org, &dir, &thr, &pay, &hit, &hit_tri, &rng, &depth, &ior_n, &ior_lo, &ior_hi,
                                       &sorg, &sdir, &scontrib, &senergy, &q0, &q1, &sq, &counters, &pixels,
-                                      &variance, &count, &taken, &done, &pix_list, &gn, &gp, &gd, &ga, &gb, &stats,
+                                      &variance, &count, &taken, &done, &pix_list, &pix_list2, &plan, &gn, &gp, &gd,
+                                      &ga, &gb, &stats,
                                       &out, &tonemap, &nrc_q, &nrc_tp, &nrc_tgt, &nrc_prev, &nrc_count})
             b->release();
     }
