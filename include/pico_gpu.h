@@ -508,6 +508,15 @@ int pico_gpu_nrc_train_device(pico_gpu_nrc* cache, const pico_nrc_query* d_queri
                               uint64_t n, int apply, void* stream);
 /* Gradients of the last training call: network (6 x 64 x 64) and grid (levels x entries x 2). */
 int pico_gpu_nrc_gradients(pico_gpu_nrc* cache, float* mlp_grad, float* grid_grad);
+/* The cache's kernels wait on mbarriers for their bulk copies and tensor-core
+ * commits; each wait gives up after limit_ns nanoseconds of the device's global
+ * timer (1e9 by default), the kernel frees its tensor memory and returns, and the
+ * call that launched it (or the render using the cache) returns PICO_ERR_TIMEOUT
+ * with the context still usable.  withheld_bytes > 0 (at most 1024, a multiple of
+ * 16) makes the inference kernel's weight-load barrier expect that many bytes more
+ * than its copy delivers, so that this wait runs out: a test of the timeout path,
+ * nothing else; 0 (the default) for every other use. */
+int pico_gpu_nrc_set_wait_limit(pico_gpu_nrc* cache, uint64_t limit_ns, uint32_t withheld_bytes);
 /* The cache PICO_ESTIMATOR_RADIANCE_CACHE renders of this context use (NULL: none). */
 int pico_gpu_set_radiance_cache(pico_gpu_ctx* ctx, pico_gpu_nrc* cache);
 

@@ -90,6 +90,7 @@ SIGNATURES = {
     "pico_gpu_nrc_encode": (C.c_int, [_vp, _vp, _u64, _vp]),
     "pico_gpu_nrc_infer": (C.c_int, [_vp, _vp, _u64, _vp]),
     "pico_gpu_nrc_infer_device": (C.c_int, [_vp, _vp, _u64, _vp, _vp]),
+    "pico_gpu_nrc_set_wait_limit": (C.c_int, [_vp, _u64, C.c_uint32]),
     "pico_gpu_nrc_train": (C.c_int, [_vp, _vp, _vp, _u64, C.c_int, _fp]),
     "pico_gpu_nrc_train_device": (C.c_int, [_vp, _vp, _vp, _u64, C.c_int, _vp]),
     "pico_gpu_nrc_gradients": (C.c_int, [_vp, _vp, _vp]),
@@ -536,6 +537,12 @@ class RadianceCache:
         out = np.empty((len(q), 3), np.float32)
         self.ctx.check(self.lib.pico_gpu_nrc_infer(self.handle, q.ctypes.data, len(q), out.ctypes.data), "nrc_infer")
         return out
+
+    def set_wait_limit(self, limit_ns: int = 1_000_000_000, withheld_bytes: int = 0):
+        """pico_gpu_nrc_set_wait_limit: how long the kernels' mbarrier waits last before they give up
+        (PICO_ERR_TIMEOUT); withheld_bytes > 0 makes the inference's weight-load wait run out (tests)."""
+        self.ctx.check(self.lib.pico_gpu_nrc_set_wait_limit(self.handle, int(limit_ns), int(withheld_bytes)),
+                       "nrc_set_wait_limit")
 
     def infer_device(self, d_queries: int, n: int, d_rgb: int, stream: int = 0):
         self.ctx.check(self.lib.pico_gpu_nrc_infer_device(self.handle, d_queries, n, d_rgb, stream or None),

@@ -981,7 +981,7 @@ cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraV
     if (e != cudaSuccess) return e;
     if (na.mode == kNrcTerminate) {
         e = nrc::launch_infer(na.geo, na.table, na.weights, na.queries, na.capacity, nullptr, b.thr, b.pay, na.err, st,
-                              na.count, na.infer_groups);
+                              na.count, na.infer_groups, na.wait);
         if (e != cudaSuccess) return e;
     }
     accumulate_kernel<<<grid_for(accumulate_kernel, b.npix, kRenderThreads), kRenderThreads, 0, st>>>(b, spb, max_samples, max_variance,

@@ -102,6 +102,7 @@ struct NrcShadeArgs {
     const uint8_t* weights;
     int* err;
     int infer_groups;
+    nrc::WaitPolicy wait;
 };
 
 cudaError_t launch_render_batch(const SceneView& sc, PathBatch& b, const CameraView& cam, unsigned long long seed,

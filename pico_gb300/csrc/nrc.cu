@@ -93,6 +93,7 @@ struct InferArgs {
     float4* pay;
     int* err;
     const uint32_t* n_dev;
+    WaitPolicy wait;
 };
 
 // G warpgroups per CTA share one copy of the weights; each runs its own 128-row
@@ -149,10 +150,10 @@ __global__ void __launch_bounds__(128 * G) infer_kernel(InferArgs a)
     tc_fence_after();
     const uint32_t tmem = *tslot + 64u * g;
     if (tid == 0) {
-        mbar_expect_tx(bar_w, kWeightBytes);
+        mbar_expect_tx(bar_w, kWeightBytes + a.wait.withheld_bytes);
         bulk_load(smem_addr(W), a.weights, kWeightBytes, bar_w);
     }
-    bool ok = mbar_wait(bar_w, 0);
+    bool ok = mbar_wait(bar_w, 0, a.wait.limit_ns);
     uint32_t phase = 0;
     const uint32_t lane_addr = tmem + (((warp & 3u) * 32u) << 16);
     const uint32_t x_addr = smem_addr(X), w_addr = smem_addr(W);
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(128 * G) infer_kernel(InferArgs a)
                 issue_forward(tmem, x_addr, w_addr + (uint32_t)l * kLayerBytes, l);
                 mma_commit(bar_m);
             }
-            ok = mbar_wait(bar_m, phase);
+            ok = mbar_wait(bar_m, phase, a.wait.limit_ns);
             phase ^= 1u;
             tc_fence_after();
             if (l < kHidden) {
@@ -230,6 +231,7 @@ struct TrainArgs {
     float* partial;        // [gridDim.x][kMlpParams]
     float* loss;
     int* err;
+    WaitPolicy wait;
 };
 
 __global__ void __launch_bounds__(kThreads, 1) train_kernel(TrainArgs a)
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(kThreads, 1) train_kernel(TrainArgs a)
         mbar_expect_tx(bar_w, kWeightBytes);
         bulk_load(smem_addr(W), a.weights, kWeightBytes, bar_w);
     }
-    bool ok = mbar_wait(bar_w, 0);
+    bool ok = mbar_wait(bar_w, 0, a.wait.limit_ns);
     uint32_t phase = 0;
     const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
     const uint32_t w_addr = smem_addr(W), x_addr = smem_addr(X), dy_addr = smem_addr(dY);
@@ -300,7 +302,7 @@ __global__ void __launch_bounds__(kThreads, 1) train_kernel(TrainArgs a)
                 issue_forward(tmem, x_addr + (uint32_t)l * kTileBytes, w_addr + (uint32_t)l * kLayerBytes, l);
                 mma_commit(bar_m);
             }
-            ok = mbar_wait(bar_m, phase);
+            ok = mbar_wait(bar_m, phase, a.wait.limit_ns);
             phase ^= 1u;
             tc_fence_after();
             if (l < kHidden) {
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1) train_kernel(TrainArgs a)
                              (!first || k > 0) ? 1u : 0u);
                 mma_commit(bar_m);
             }
-            ok = mbar_wait(bar_m, phase);
+            ok = mbar_wait(bar_m, phase, a.wait.limit_ns);
             phase ^= 1u;
             tc_fence_after();
             float v[kWidth];
@@ -528,10 +530,10 @@ static cudaError_t launch_infer_groups(const InferArgs& a, cudaStream_t st)
 
 cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint8_t* weights, const float4* queries,
                          uint32_t n, float* out_rgb, const float4* thr, float4* pay, int* err, cudaStream_t st,
-                         const uint32_t* n_dev, int groups)
+                         const uint32_t* n_dev, int groups, const WaitPolicy& wait)
 {
     if (n == 0) return cudaSuccess;
-    const InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev};
+    const InferArgs a{g, table, weights, queries, n, out_rgb, thr, pay, err, n_dev, wait};
     switch (groups) {
     case 1: return launch_infer_groups<1>(a, st);
     case 2: return launch_infer_groups<2>(a, st);
@@ -541,7 +543,7 @@ cudaError_t launch_infer(const GridGeometry& g, const __half2* table, const uint
 
 cudaError_t launch_train(const GridGeometry& g, const __half2* table, const uint8_t* weights, const TrainBatch& b,
                          float2* grid_grad, float* partial, uint32_t max_parts, uint32_t* parts, float* loss,
-                         int* err, cudaStream_t st)
+                         int* err, cudaStream_t st, const WaitPolicy& wait)
 {
     *parts = 0;
     if (b.n == 0) return cudaSuccess;
@@ -553,7 +555,7 @@ cudaError_t launch_train(const GridGeometry& g, const __half2* table, const uint
     }
     uint32_t grid = train_grid_size(b.n);
     if (grid > max_parts) grid = max_parts;
-    TrainArgs a{g, table, weights, b, 1.0f / (3.0f * (float)b.n), grid_grad, partial, loss, err};
+    TrainArgs a{g, table, weights, b, 1.0f / (3.0f * (float)b.n), grid_grad, partial, loss, err, wait};
     train_kernel<<<grid, kThreads, kTrainSmem, st>>>(a);
     *parts = grid;
     return cudaGetLastError();

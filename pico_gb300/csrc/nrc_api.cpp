@@ -98,7 +98,7 @@ int train_step(pico_gpu_nrc* c, const TrainBatch& b, bool apply, cudaStream_t st
     uint32_t parts = 0;
     if (e == cudaSuccess)
         e = launch_train(c->geo, c->table, c->image, b, reinterpret_cast<float2*>(c->grid_grad), c->partial,
-                         c->max_parts, &parts, c->loss, c->err, st);
+                         c->max_parts, &parts, c->loss, c->err, st, c->wait);
     if (e != cudaSuccess) return cuda_error(ctx, e, "radiance cache training");
     const AdamStep s = apply ? next_adam_step(c) : AdamStep{};
     if (parts > 0) e = launch_adam_mlp(c->partial, parts, c->master, c->adam_m, c->adam_v, c->grad, c->image, s, apply, st);
@@ -306,8 +306,19 @@ int pico_gpu_nrc_infer_device(pico_gpu_nrc* c, const pico_nrc_query* d_q, uint64
     const DeviceScope device_scope(c->ctx->device);
     cudaError_t e = launch_infer(c->geo, c->table, c->image, reinterpret_cast<const float4*>(d_q), (uint32_t)n, d_rgb,
                                  nullptr, nullptr, c->err, static_cast<cudaStream_t>(stream), nullptr,
-                                 (int)c->cfg.infer_groups);
+                                 (int)c->cfg.infer_groups, c->wait);
     if (e != cudaSuccess) return cuda_error(c->ctx, e, "radiance cache inference");
+    return PICO_OK;
+}
+
+int pico_gpu_nrc_set_wait_limit(pico_gpu_nrc* c, uint64_t limit_ns, uint32_t withheld_bytes)
+{
+    if (!c) return PICO_ERR_INVALID_ARG;
+    if (limit_ns == 0 || withheld_bytes > 1024 || withheld_bytes % 16)
+        return set_error(c->ctx, PICO_ERR_INVALID_ARG,
+                         "wait limit: a positive time, and at most 1024 withheld bytes in multiples of 16");
+    c->wait.limit_ns = limit_ns;
+    c->wait.withheld_bytes = withheld_bytes;
     return PICO_OK;
 }
 

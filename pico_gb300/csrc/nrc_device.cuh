@@ -228,15 +228,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-// Waits for the phase with the given parity to complete, for at most about a
-// second; false if it did not.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+// Waits for the phase with the given parity to complete, for at most limit_ns
+// nanoseconds of the global timer; false if it did not.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns)
 {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (globaltimer() - t0 > 1000000000ull) return false;
+        if (globaltimer() - t0 > limit_ns) return false;
     }
 }
 

@@ -25,6 +25,7 @@ struct pico_gpu_nrc {
     __half2* table = nullptr;
     float* loss = nullptr;
     int* err = nullptr;
+    pico::nrc::WaitPolicy wait{};      // pico_gpu_nrc_set_wait_limit
     std::vector<void*> allocations;
     // cumulative render work: training paths, training records, optimiser steps, cache queries
     uint64_t render_stats[4] = {0, 0, 0, 0};

@@ -167,6 +167,7 @@ int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_n
     na.err = c->err;
     na.bounces = c->cfg.bounces;
     na.infer_groups = (int)c->cfg.infer_groups;
+    na.wait = c->wait;
     const unsigned long long train_seed = c->cfg.seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
     const int order = scene_order(ctx, scene);
     const bool training = ntrain > 0 && c->cfg.max_train_steps > 0;

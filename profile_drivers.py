@@ -91,7 +91,7 @@ def cache_render(passes: int) -> None:
 def render(estimator: int, passes: int, width: int, height: int) -> None:
     ctx = pico_gb300.Context(0)
     gs = ctx.upload(scenes.lit_field())
-    gs.render(scenes.lit_field_camera(width, height), 8, passes, seed=99, estimator=estimator)
+    gs.render(scenes.lit_field_camera(width, height), 8, passes, seed=99, estimator=estimator, cancellable=False)
     print("render driver:", ctx.render_stats())
     gs.free()
     ctx.close()

@@ -177,3 +177,27 @@ def test_training_fits_a_smooth_target(ctx):
         assert c.info()["steps"] == 300
     finally:
         c.free()
+
+
+def test_a_wait_that_runs_out_reports_a_timeout_and_the_context_stays_usable(ctx):
+    """The kernels' mbarrier waits are bounded: with the inference's weight-load barrier expecting
+    bytes that never arrive (the copy itself completes), the wait gives up after its limit, the
+    call returns PICO_ERR_TIMEOUT, and the same cache then infers as before."""
+    import pico_gb300
+    c = RadianceCache(ctx, log2_table_size=14, aabb_min=LO, aabb_max=HI, seed=3)
+    try:
+        lively_params(c, 2)
+        q = po_nrc.make_queries(300, 8, LO, HI)
+        want = c.infer(q)
+        c.set_wait_limit(limit_ns=2_000_000, withheld_bytes=16)
+        with pytest.raises(pico_gb300.PicoError) as err:
+            c.infer(q)
+        assert err.value.status == -5          # PICO_ERR_TIMEOUT
+        c.set_wait_limit()                     # defaults: 1 s, nothing withheld
+        np.testing.assert_array_equal(c.infer(q), want)
+        with pytest.raises(pico_gb300.PicoError):
+            c.set_wait_limit(limit_ns=0)
+        with pytest.raises(pico_gb300.PicoError):
+            c.set_wait_limit(withheld_bytes=8)
+    finally:
+        c.free()
