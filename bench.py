@@ -674,7 +674,7 @@ def render_config(args, n_gpus):
             "resolution": [1920, 1080], "spp": args.render_spp, "max_depth": args.render_depth,
             "instances": 4096, "triangles_per_mesh": 5120, "lights": 8, "denoise": "a-trous 5 levels",
             "seed": "fixed: every step renders the same seed from cleared buffers (identical work per step)",
-            "l2": "path state (2^24 paths x 208 B = 3.5 GB per batch) and image buffers (57 MB) exceed L2; "
+            "l2": "path state (up to 2^26 paths x 208 B = 14 GB per round) and image buffers (57 MB) exceed L2; "
                   "the scene (1.5 MB) stays in L2 by design",
             "parallelism": f"replicas x{n_gpus}"}
 

@@ -257,8 +257,8 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                          const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
-/* The render runs in batches of up to 2^24 paths (pixels x samples; 208 bytes of
- * path state each, 3.5 GB at the limit).  Where the reference's early exit can
+/* The render runs in batches of up to 2^26 paths (pixels x samples; 208 bytes of
+ * path state each, 14 GB at the limit).  Where the reference's early exit can
  * stop pixels (reference estimator, max_variance >= 0) the first batch takes 6
  * samples per pixel and later batches only the pixels still sampling, as many
  * samples each as fill the path state; otherwise every batch covers all pixels.

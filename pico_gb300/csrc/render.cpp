@@ -262,7 +262,7 @@ static bool early_exit_on(const pico_render_config* cfg)
 // Exit-aware rounds over the first `nactive` pixels of r.pix_list (at most
 // kMaxPaths of them): the first round takes kFirstExitSamples samples per pixel;
 // after every round a compaction keeps the pixels still sampling and the next round
-// takes as many samples per pixel as fill the path state (2^24 paths), so that
+// takes as many samples per pixel as fill the path state (kMaxPaths), so that
 // rounds after the exits are dense.  Both are decided on the device (RoundPlan), so
 // nothing here waits for it: the host enqueues as many rounds as a render with no
 // exit needs, and rounds with nothing left to do launch empty kernels.  Images are

@@ -28,10 +28,12 @@ struct RenderBuffers {
 namespace pico {
 
 // Paths of one batch of a single render (pixels x samples; 208 B of path state
-// each, 3.5 GB at the limit).  Larger batches amortise each launch and its
+// each, 14 GB at the limit).  Larger batches amortise each launch and its
 // tail: a 1080p render at 64 spp measured 159 / 206 / 267 / 279 / 286 Msamples/s
-// with batches of 2^19 / 2^20 / 2^22 / 2^23 / 2^24 paths (physical estimator).
-constexpr uint32_t kMaxPaths = 1u << 24;
+// with batches of 2^19 / 2^20 / 2^22 / 2^23 / 2^24 paths (physical estimator),
+// and 2^25 / 2^26 took the 1080p renders 1.4 / 2.5 % (reference estimator) and
+// 1.4 / 2.0 % (physical) below 2^24's time.
+constexpr uint32_t kMaxPaths = 1u << 26;
 // Device bytes of path state per path that reserve_paths allocates: eleven float4
 // arrays, six uint32 arrays and the 64-bit random state.
 constexpr size_t kPathStateBytes = 11 * 16 + 6 * 4 + 8;

@@ -141,3 +141,22 @@ def test_physical_rejects_btdf_scenes_and_unknown_estimators(ctx):
         gs.render(cam, 5, 1, estimator=2)
     assert e.value.status == PICO_ERR_INVALID_ARG
     gs.free()
+
+
+def test_direct_light_matches_lamberts_closed_form(ctx):
+    """The device's physical estimator against a closed form (tests/analytic.py): direct light
+    from one quad emitter onto a Lambertian plane, every pixel within 4 standard errors of
+    Lambert's contour integral (all but 1 %), and no bias over the image."""
+    import analytic
+    gs = ctx.upload(analytic.lit_plane_scene())
+    try:
+        spp = 2048
+        pix, cnt, var = gs.render(analytic.lit_plane_camera(32), 2, spp, seed=5, estimator=ESTIMATOR_PHYSICAL)
+    finally:
+        gs.free()
+    assert (cnt == spp).all()
+    want = analytic.expected_pixels(32).reshape(32, 32, 3)
+    se = np.sqrt(var.astype(np.float64) / spp)
+    z = np.abs(pix - want) / se
+    assert np.mean(z < 4) >= 0.99, np.sort(z.ravel())[-5:]
+    assert abs(np.sum(pix - want)) < 4 * np.sqrt(np.sum(se ** 2))

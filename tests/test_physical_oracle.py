@@ -163,3 +163,27 @@ def test_white_furnace(oracle):
     centre = mean.reshape(16, 16, 3)[5:11, 5:11]
     np.testing.assert_allclose(centre, 0.5, atol=1e-9)
     assert np.isclose(mean, 1.0).any()   # sky pixels see the sky itself
+
+
+def test_direct_light_matches_lamberts_closed_form(oracle):
+    """The oracle against a closed form (tests/analytic.py): direct light from one quad emitter
+    onto a Lambertian plane, next-event estimation and BSDF sampling under MIS, per pixel within
+    4 standard errors of Lambert's contour integral, and without bias over the pixels."""
+    import sys
+    from pathlib import Path
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    import analytic
+    # the formula itself: an emitter filling the hemisphere gives E / L = pi
+    big = [[-1e6, 1.0, -1e6], [1e6, 1.0, -1e6], [1e6, 1.0, 1e6], [-1e6, 1.0, 1e6]]
+    assert abs(analytic.polygon_irradiance([0.0, 0.0, 0.0], (0.0, 1.0, 0.0), big)[0] - np.pi) < 1e-4
+    want = analytic.expected_pixels(32)
+    rng = np.random.default_rng(12)
+    idx = np.sort(rng.choice(32 * 32, 96, replace=False)).astype(np.uint32)
+    spp = 4096
+    seeds = rng.integers(1, 2**63, len(idx), dtype=np.uint64)
+    mean, var = oracle.scene(analytic.lit_plane_scene()).phys_render_mean(analytic.lit_plane_camera(32), 2, spp,
+                                                                         idx, seeds)
+    se = np.sqrt(var / spp)
+    z = np.abs(mean - want[idx]) / se
+    assert np.mean(z < 4) >= 0.98, np.sort(z.ravel())[-5:]
+    assert abs(np.sum(mean - want[idx])) < 4 * np.sqrt(np.sum(se ** 2))
