@@ -149,9 +149,15 @@ typedef struct {
  * from the fourth vertex, a jitter over the whole pixel and a plain running mean
  * (every sample counts; max_variance is ignored and no pixel stops early).
  * Diffuse, Specular, Dielectric, Light and Specular_Delta (a mirror with Schlick
- * reflectance) instances are supported; a scene with Transparent or Fresnel
- * instances returns PICO_ERR_UNSUPPORTED.  Emitters are two-sided; the sun is a
- * directional light whose colour is its irradiance. */
+ * reflectance) instances are supported, and Transparent and Fresnel ones as a
+ * rough dielectric interface between air and the material's
+ * index_of_refraction (GGX with alpha = roughness^2, Walter et al. 2007): the
+ * Fresnel kind reflects with the exact dielectric Fresnel probability and
+ * refracts otherwise, the Transparent kind only refracts (it reflects under
+ * total internal reflection), refraction tinted by the diffuse colour; these
+ * vertices take no next-event estimation.  The radiance cache estimator returns
+ * PICO_ERR_UNSUPPORTED for Transparent and Fresnel instances.  Emitters are
+ * two-sided; the sun is a directional light whose colour is its irradiance. */
 enum pico_estimator {
     PICO_ESTIMATOR_REFERENCE = 0,
     PICO_ESTIMATOR_PHYSICAL = 1,

@@ -127,6 +127,52 @@ static d3 sample_vndf(d3 v, double alpha, double u1, double u2)
     return d3_norm(d3v(alpha * nh.x, alpha * nh.y, fmax(nh.z, 0.0)));
 }
 
+/* Exact dielectric Fresnel reflectance, eta = eta_i / eta_t, cos_i > 0; 1 under total
+ * internal reflection. */
+static double fresnel_dielectric(double cos_i, double eta)
+{
+    const double sin2_t = eta * eta * fmax(1.0 - cos_i * cos_i, 0.0);
+    if (sin2_t >= 1.0) return 1.0;
+    const double cos_t = sqrt(1.0 - sin2_t);
+    const double rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    const double rp = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    return 0.5 * (rs * rs + rp * rp);
+}
+
+/* Transparent / Fresnel kinds: a rough dielectric interface (Walter et al. 2007; GGX,
+ * visible-normal sampling).  The Fresnel kind reflects about the sampled microfacet
+ * normal with probability F(v.h), else refracts; the Transparent kind refracts unless
+ * total internal reflection forces a reflection.  Weights: G2 / G1(v) for a
+ * reflection, tint G2 / G1 eta^2 for a refraction.  Returns 0 when the direction
+ * leaves on the wrong side; *refracted tells which. */
+static int sample_dielectric(d3 v, double alpha, double eta, d3 tint, int reflect_lobe, const double* u, d3* l,
+                             d3* weight, int* refracted)
+{
+    *refracted = 0;
+    *weight = d3v(0, 0, 0);
+    *l = d3v(0, 0, 1);
+    if (v.z <= 0.0) return 0;
+    const d3 h = sample_vndf(v, alpha, u[1], u[2]);
+    const double vh = d3_dot(v, h);
+    if (vh <= 0.0) return 0;
+    const double F = fresnel_dielectric(vh, eta);
+    const double a2 = alpha * alpha, lv = ggx_lambda(v, a2);
+    if (F >= 1.0 || (reflect_lobe && u[0] < F)) {
+        *l = d3_sub(d3_scale(h, 2.0 * vh), v);
+        if (l->z <= 0.0) return 0;
+        const double g = (1.0 + lv) / (1.0 + lv + ggx_lambda(*l, a2));
+        *weight = d3v(g, g, g);
+    } else {
+        const double cos_t = sqrt(fmax(1.0 - eta * eta * (1.0 - vh * vh), 0.0));
+        *l = d3_norm(d3_sub(d3_scale(h, eta * vh - cos_t), d3_scale(v, eta)));
+        if (l->z >= 0.0) return 0;
+        const double g = (1.0 + lv) / (1.0 + lv + ggx_lambda(*l, a2)) * eta * eta;
+        *weight = d3_scale(tint, g);
+        *refracted = 1;
+    }
+    return 1;
+}
+
 /* One sample from three uniforms; returns 0 when it leaves below the surface. */
 static int sample_local(const lobes* lb, d3 v, const double* u, d3* l, double* pdf, d3* weight)
 {
@@ -381,10 +427,11 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
         prev_rough = in->bsdf == PO_DELTA ? 0.0 : m->roughness;   /* a mirror is glossy */
         d3 n = d3_norm(d3_of(f.normal));
         const d3 v = d3_scale(d, -1.0);
-        if (d3_dot(n, v) < 0.0) n = d3_scale(n, -1.0);
+        const int front = !(d3_dot(n, v) < 0.0);   /* the viewer on the side the normal points to */
+        if (!front) n = d3_scale(n, -1.0);
         const d3 P = d3v(f.position[0], f.position[1], f.position[2]);
         const double eps = 1e-4 * (1.0 + fmax(fmax(fabs(P.x), fabs(P.y)), fabs(P.z)));
-        const d3 org = d3_add(P, d3_scale(n, eps));
+        d3 org = d3_add(P, d3_scale(n, eps));
         d3 L, weight;
         double pdf_next = 0.0;
         int ok;
@@ -393,6 +440,18 @@ static d3 phys_path(const phys_scene* ps, const po_camera* cam, uint32_t px, uin
             L = d3_sub(d3_scale(n, 2.0 * c), v);
             weight = d3v(schlick(m->specular[0], c), schlick(m->specular[1], c), schlick(m->specular[2], c));
             ok = c > 0.0;
+        } else if (in->bsdf == PO_BTDF || in->bsdf == PO_FRESNEL) {
+            /* air outside, the material's index inside; no next-event estimation here */
+            const frame fr = frame_of(n);
+            const double ior = m->index_of_refraction > 0.0f ? m->index_of_refraction : 1.0;
+            double u[3] = {rnd(rng), rnd(rng), rnd(rng)};
+            d3 l;
+            int refracted;
+            ok = sample_dielectric(to_local(&fr, v), fmax((double)m->roughness * m->roughness, PHYS_MIN_ALPHA),
+                                   front ? 1.0 / ior : ior, d3_of(m->diffuse), in->bsdf == PO_FRESNEL, u, &l, &weight,
+                                   &refracted);
+            L = to_world(&fr, l);
+            if (refracted) org = d3_sub(P, d3_scale(n, eps));
         } else {
             const frame fr = frame_of(n);
             const d3 vl = to_local(&fr, v);

@@ -120,8 +120,6 @@ int validate(pico_gpu_ctx* ctx, uint32_t n, const pico_render_item* items)
             return set_error(ctx, PICO_ERR_INVALID_ARG, who + "bad image size");
         if (c.estimator != PICO_ESTIMATOR_REFERENCE && c.estimator != PICO_ESTIMATOR_PHYSICAL)
             return set_error(ctx, PICO_ERR_INVALID_ARG, who + "batches take the reference or physical estimator");
-        if (c.estimator == PICO_ESTIMATOR_PHYSICAL && it.scene->has_btdf)
-            return set_error(ctx, PICO_ERR_UNSUPPORTED, who + "the physical estimator has no Transparent or Fresnel lobes");
         if (c.denoise || c.tonemap) return set_error(ctx, PICO_ERR_INVALID_ARG, who + "batches do not denoise or tone map");
         if (it.scene->ctx != ctx) return set_error(ctx, PICO_ERR_INVALID_ARG, who + "scene of another context");
     }

@@ -114,7 +114,7 @@ struct pico_gpu_scene {
     // Which of those the reference returns depends on its own visit order and pruning,
     // so scenes with sphere instances are always traversed in the reference's order.
     bool needs_reference_order = false;
-    bool has_btdf = false;   // Transparent or Fresnel instances: the physical estimator has no such lobes
+    bool has_btdf = false;   // Transparent or Fresnel instances: the radiance cache has no such lobes
     uint64_t info[6] = {0, 0, 0, 0, 0, 0};
 };
 

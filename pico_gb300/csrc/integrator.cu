@@ -450,7 +450,8 @@ __global__ void __launch_bounds__(kRenderThreads, kShadeBlocksPerSm) shade_physi
                     const Fragment f = make_fragment(sc, rank, b.hit_tri[i], hit.y, hit.z, b.org[i], dir);
                     float3 nrm = normalize3(make_float3(f.n.x, f.n.y, f.n.z));
                     const float3 v = make_float3(-dir.x, -dir.y, -dir.z);
-                    if (dot3(nrm, v) < 0.0f) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
+                    const bool front = !(dot3(nrm, v) < 0.0f);   // the viewer on the side the normal points to
+                    if (!front) nrm = make_float3(-nrm.x, -nrm.y, -nrm.z);
                     if (nrc.mode == kNrcRecord) {
                         nrc_query(f, nrm, v, m, is.bsdf, i, eq);
                         et = thr;
@@ -460,7 +461,7 @@ __global__ void __launch_bounds__(kRenderThreads, kShadeBlocksPerSm) shade_physi
                         nrc.prev_rough[i] = is.bsdf == PICO_BSDF_DELTA ? 0.0f : m.roughness;   // a mirror is glossy
                     }
                     const float eps = ray_offset(f.px, f.py, f.pz);
-                    const float4 org = make_float4(f.px + eps * nrm.x, f.py + eps * nrm.y, f.pz + eps * nrm.z, f.pw);
+                    float4 org = make_float4(f.px + eps * nrm.x, f.py + eps * nrm.y, f.pz + eps * nrm.z, f.pw);
                     float3 L, weight;
                     float pdf_next = 0.0f;
                     bool ok;
@@ -471,6 +472,22 @@ __global__ void __launch_bounds__(kRenderThreads, kShadeBlocksPerSm) shade_physi
                         weight = make_float3(schlick(m.specular[0], c), schlick(m.specular[1], c),
                                              schlick(m.specular[2], c));
                         ok = c > 0.0f;
+                    } else if (is.bsdf == PICO_BSDF_BTDF || is.bsdf == PICO_BSDF_FRESNEL) {
+                        // a rough dielectric interface between air and the material (entered where
+                        // the viewer is on the normal's side); no next-event estimation, so the
+                        // emission the continuation meets is not weighted
+                        const Frame fr = frame_of(nrm);
+                        const float ior = m.ior > 0.0f ? m.ior : 1.0f;
+                        const float u0 = rng.uniform(), u1 = rng.uniform(), u2 = rng.uniform();
+                        const DielectricSample ds =
+                            sample_dielectric(to_local(fr, v), fmaxf(m.roughness * m.roughness, kMinAlpha),
+                                              front ? 1.0f / ior : ior,
+                                              make_float3(m.diffuse[0], m.diffuse[1], m.diffuse[2]),
+                                              is.bsdf == PICO_BSDF_FRESNEL, u0, u1, u2);
+                        ok = ds.ok;
+                        L = to_world(fr, ds.l);
+                        weight = ds.weight;
+                        if (ds.refracted) org = make_float4(f.px - eps * nrm.x, f.py - eps * nrm.y, f.pz - eps * nrm.z, f.pw);
                     } else {
                         const Frame fr = frame_of(nrm);
                         const float3 vl = to_local(fr, v);

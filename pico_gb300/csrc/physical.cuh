@@ -7,7 +7,8 @@
 // Schlick's Fresnel F = F0 + (1 - F0)(1 - v.h)^5 (Walter et al. 2007, "Microfacet
 // models for refraction through rough surfaces"; Heitz 2014, "Understanding the
 // masking-shadowing function in microfacet-based BRDFs").  Diffuse kinds have
-// F0 = 0, Specular kinds no diffuse term, Dielectric kinds both.
+// F0 = 0, Specular kinds no diffuse term, Dielectric kinds both; Transparent and
+// Fresnel kinds are a rough dielectric interface (sample_dielectric).
 //
 // Sampling picks the GGX lobe with probability p = sum(F0) / (sum(F0) + sum(diffuse)),
 // else the cosine lobe.  The GGX lobe samples a visible normal (Heitz 2018,
@@ -182,6 +183,68 @@ __device__ __forceinline__ Sample sample(const Lobes& lb, float3 v, float u0, fl
     if (!(s.pdf > 0.0f)) return s;
     const float k = s.l.z / s.pdf;
     s.weight = make_float3(f.x * k, f.y * k, f.z * k);
+    s.ok = true;
+    return s;
+}
+
+// Exact dielectric Fresnel reflectance of unpolarised light at an interface with
+// relative index eta = eta_i / eta_t, for cos_i > 0 the cosine on the incident side;
+// 1 under total internal reflection.
+__device__ __forceinline__ float fresnel_dielectric(float cos_i, float eta)
+{
+    const float sin2_t = eta * eta * fmaxf(1.0f - cos_i * cos_i, 0.0f);
+    if (sin2_t >= 1.0f) return 1.0f;
+    const float cos_t = sqrtf(1.0f - sin2_t);
+    const float rs = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    const float rp = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    return 0.5f * (rs * rs + rp * rp);
+}
+
+// The reference's Transparent and Fresnel kinds as a rough dielectric interface
+// (Walter et al. 2007; GGX, visible-normal sampling).  v: local direction towards
+// the viewer (v.z > 0); eta = eta_i / eta_t for the side v lies on.  A visible
+// microfacet normal h is sampled; the Fresnel kind reflects about it with
+// probability F(v.h) and refracts otherwise, the Transparent kind always refracts
+// (it has no reflection lobe) but under total internal reflection, where both
+// reflect.  With the sampling probabilities equal to the lobes' weights the
+// throughput factor is G2(v, l) / G1(v) for a reflection and tint G2 / G1 eta^2
+// for a refraction (eta^2: radiance transport across the interface).  The lobe
+// is never evaluated: vertices on it take no next-event estimation, like mirrors.
+struct DielectricSample {
+    float3 l;        // local direction, l.z < 0 when refracted
+    float3 weight;
+    bool ok, refracted;
+};
+
+__device__ __forceinline__ DielectricSample sample_dielectric(float3 v, float alpha, float eta, float3 tint,
+                                                              bool reflect_lobe, float u0, float u1, float u2)
+{
+    DielectricSample s;
+    s.ok = false;
+    s.refracted = false;
+    s.weight = make_float3(0.0f, 0.0f, 0.0f);
+    s.l = make_float3(0.0f, 0.0f, 1.0f);
+    if (v.z <= 0.0f) return s;
+    const float3 h = sample_vndf(v, alpha, u1, u2);
+    const float vh = dot3(v, h);
+    if (vh <= 0.0f) return s;
+    const float F = fresnel_dielectric(vh, eta);
+    const float a2 = alpha * alpha;
+    const float lv = ggx_lambda(v, a2);
+    if (F >= 1.0f || (reflect_lobe && u0 < F)) {
+        s.l = make_float3(2.0f * vh * h.x - v.x, 2.0f * vh * h.y - v.y, 2.0f * vh * h.z - v.z);
+        if (s.l.z <= 0.0f) return s;
+        const float g = (1.0f + lv) / (1.0f + lv + ggx_lambda(s.l, a2));
+        s.weight = make_float3(g, g, g);
+    } else {
+        const float cos_t = sqrtf(fmaxf(1.0f - eta * eta * (1.0f - vh * vh), 0.0f));
+        const float k = eta * vh - cos_t;
+        s.l = normalize3(make_float3(k * h.x - eta * v.x, k * h.y - eta * v.y, k * h.z - eta * v.z));
+        if (s.l.z >= 0.0f) return s;
+        const float g = (1.0f + lv) / (1.0f + lv + ggx_lambda(s.l, a2)) * eta * eta;
+        s.weight = make_float3(tint.x * g, tint.y * g, tint.z * g);
+        s.refracted = true;
+    }
     s.ok = true;
     return s;
 }

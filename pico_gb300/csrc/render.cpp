@@ -236,8 +236,8 @@ int validate_render(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pico_c
     if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && cfg->estimator != PICO_ESTIMATOR_PHYSICAL &&
         cfg->estimator != PICO_ESTIMATOR_RADIANCE_CACHE)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "unknown estimator");
-    if (cfg->estimator != PICO_ESTIMATOR_REFERENCE && scene->has_btdf)
-        return set_error(ctx, PICO_ERR_UNSUPPORTED, "the physical estimator has no Transparent or Fresnel lobes");
+    if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE && scene->has_btdf)
+        return set_error(ctx, PICO_ERR_UNSUPPORTED, "the radiance cache has no Transparent or Fresnel lobes");
     if (cfg->estimator == PICO_ESTIMATOR_RADIANCE_CACHE && !ctx->cache)
         return set_error(ctx, PICO_ERR_INVALID_ARG, "no radiance cache attached (pico_gpu_set_radiance_cache)");
     return PICO_OK;

@@ -70,3 +70,22 @@ def expected_pixels(size: int = 32, sub: int = 16) -> np.ndarray:
     pts = np.stack([-CAMERA_HEIGHT * dx, np.zeros_like(dx), CAMERA_HEIGHT * dy], axis=-1).reshape(-1, 3)
     e = polygon_irradiance(pts, (0.0, 1.0, 0.0), LIGHT_QUAD).reshape(size * size, sub * sub).mean(axis=1)
     return (ALBEDO / np.pi) * e[:, None] * np.asarray(RADIANCE)[None, :]
+
+
+def glass_slab_scene(kind: int, roughness: float = 0.0, ior: float = 1.5, tint=(1.0, 1.0, 1.0)) -> SceneData:
+    """A slab of glass (Transparent or Fresnel kind) between y = -1 and y = 0, 2000 wide, under a
+    uniform sky of radiance 1: a smooth dielectric neither creates nor absorbs light and the
+    eta^2 factors of entering and leaving cancel, so with a white tint every pixel's expectation
+    is 1 (a furnace test of the interface)."""
+    s = SceneData(materials=[Material(diffuse=tint, roughness=roughness, ior=ior)], sky=(1.0, 1.0, 1.0))
+    w = 1000.0
+    s.meshes.append(scenes.quad_mesh([[-w, 0, -w], [-w, 0, w], [w, 0, w], [w, 0, -w]], [0, 1, 0]))
+    s.meshes.append(scenes.quad_mesh([[-w, -1, -w], [w, -1, -w], [w, -1, w], [-w, -1, w]], [0, -1, 0]))
+    s.instances.append(Instance(0, scenes.glm_storage(np.eye(4)), kind, 0))
+    s.instances.append(Instance(1, scenes.glm_storage(np.eye(4)), kind, 0))
+    return s
+
+
+def glass_slab_camera(size: int = 16) -> Camera:
+    return Camera(position=(0.0, 5.0, 0.0), direction=(0.0, -1.0, 0.0), resolution=(size, size), aspect=1.0,
+                  up=(0.0, 0.0, 1.0))

@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from pico_gb300 import PicoError, scenes
-from pico_gb300.types import BTDF, DIELECTRIC, DIFFUSE, ESTIMATOR_PHYSICAL, SPECULAR, Material
+from pico_gb300.types import BTDF, DIELECTRIC, DIFFUSE, ESTIMATOR_PHYSICAL, FRESNEL, LIGHT, SPECULAR, Material
 
 sys.path.insert(0, str(Path(__file__).resolve().parent))
 from calibration import assert_like_oracle, stats  # noqa: E402
@@ -127,13 +127,18 @@ def test_physical_counts_every_sample(ctx):
     gs.free()
 
 
-def test_physical_rejects_btdf_scenes_and_unknown_estimators(ctx):
+def test_btdf_scenes_render_and_the_cache_estimator_rejects_them(ctx):
+    """Transparent and Fresnel instances render through the physical estimator; the radiance
+    cache estimator returns PICO_ERR_UNSUPPORTED for them, and without a cache attached it
+    rejects the arguments."""
     scene = scenes.cornell_box()
-    scene.instances[-1].bsdf = BTDF
+    scene.instances[0].bsdf = BTDF
     gs = ctx.upload(scene)
     cam = scenes.cornell_camera(8, 8)
+    pix, cnt, _ = gs.render(cam, 5, 4, estimator=ESTIMATOR_PHYSICAL)
+    assert (cnt == 4).all() and np.isfinite(pix).all()
     with pytest.raises(PicoError) as e:
-        gs.render(cam, 5, 1, estimator=ESTIMATOR_PHYSICAL)
+        gs.render(cam, 5, 1, estimator=2)
     assert e.value.status == PICO_ERR_UNSUPPORTED
     gs.free()
     gs = ctx.upload(scenes.cornell_box())
@@ -141,6 +146,42 @@ def test_physical_rejects_btdf_scenes_and_unknown_estimators(ctx):
         gs.render(cam, 5, 1, estimator=2)
     assert e.value.status == PICO_ERR_INVALID_ARG
     gs.free()
+
+
+def glass_field():
+    """The glossy field with every third instance made of rough tinted glass (Transparent and
+    Fresnel kinds alternating, roughness 0.05-0.5, index 1.3-1.8)."""
+    s = scenes.glossy_field()
+    rng = np.random.default_rng(3)
+    for k, inst in enumerate(s.instances):
+        if inst.bsdf != LIGHT and k % 3 == 0:
+            s.materials.append(Material(diffuse=tuple(rng.uniform(0.5, 1.0, 3)), roughness=float(rng.uniform(0.05, 0.5)),
+                                        ior=float(rng.uniform(1.3, 1.8))))
+            inst.material = len(s.materials) - 1
+            inst.bsdf = FRESNEL if (k // 3) % 2 else BTDF
+    return s
+
+
+def test_glass_field_physical_render_matches_oracle(ctx, oracle):
+    """Rough dielectric interfaces (refraction, Fresnel reflection, total internal reflection,
+    paths through glass) next to GGX metals, a mirror, three quad lights and the sun."""
+    check_against_oracle(ctx, oracle, glass_field(), scenes.glossy_field_camera(64, 48), 8, 1024, 4096, 512, 14)
+
+
+@pytest.mark.parametrize("kind_name", ["BTDF", "FRESNEL"])
+def test_smooth_glass_slab_furnace(ctx, kind_name):
+    """A smooth glass slab under a uniform sky of radiance 1 renders 1 (tests/analytic.py)."""
+    import analytic
+    from pico_gb300 import types
+    gs = ctx.upload(analytic.glass_slab_scene(getattr(types, kind_name)))
+    try:
+        spp = 1024
+        pix, cnt, var = gs.render(analytic.glass_slab_camera(16), 32, spp, seed=3, estimator=ESTIMATOR_PHYSICAL)
+    finally:
+        gs.free()
+    se = np.sqrt(np.maximum(var.astype(np.float64), 0.0) / spp)
+    assert np.mean(np.abs(pix - 1.0) < 4 * se + 1e-4) >= 0.98
+    assert abs(np.mean(pix) - 1.0) < 4 * np.sqrt(np.sum(se ** 2)) / pix.size + 1e-5
 
 
 def test_direct_light_matches_lamberts_closed_form(ctx):
