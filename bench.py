@@ -666,7 +666,7 @@ def atrous_traffic_per_call():
 
 RENDER_WORKLOAD = ("lit field: 4096 x level-4 icosphere (5120 tris each) with metalness-roughness materials, "
                    "ground quad, 8 quad lights; 1920x1080, {spp} spp, depth {depth}, a-trous 5 levels; reference "
-                   "estimator (Integrators.cpp:46-209, Scene.cpp:143-235: zero-variance pixels stop after 5 samples)")
+                   "estimator (Integrators.cpp:46-209, Scene.cpp:143-235: zero-variance pixels stop at their sixth sample)")
 
 
 def render_config(args, n_gpus):
