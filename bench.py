@@ -53,6 +53,7 @@ from pico_gb300.types import HIT_DTYPE, RAY_DTYPE  # noqa: E402
 
 RAY_BYTES, HIT_BYTES = RAY_DTYPE.itemsize, HIT_DTYPE.itemsize
 NODE_BYTES, TRI_BYTES, INST_BYTES = 64, 48, 144
+SHADE_VERTEX_BYTES = 32 + 2 * 64 + 8   # material, path state read + written, queue entries (per shaded vertex)
 
 
 def parse():
@@ -843,12 +844,27 @@ def bench_render_headline(ctx, args, torch, local, dist, world, l2_gbs):
                                     "instance_entries": work["instances"], "rays": traced},
                 "bytes_model": "64 B per node visited, 48 B per triangle tested, 144 B per instance entry, "
                                "52 B of ray in / hit out per ray"}
-    batches = launches // (depth + 1) if launches else 0
-    kernels_per_render = 2 * launches + 3 * batches + 1 + (1 + 10)   # + prepare, G-buffer, a-trous
+    # the shade kernel against HBM: the per-vertex byte model over its timed launches
+    shade_ms = timing["shade_ms"] / args.steps
+    shaded = st["camera_paths"] + st["bounce_rays"]   # the path segments the shade launches take
+    shade_bytes = shaded * SHADE_VERTEX_BYTES
+    shade_rate = shade_bytes / (shade_ms / 1e3) / 1e9 if shade_ms > 0 else 0.0
+    shade_roofline = {"bound": "hbm", "achieved": shade_rate, "peak": hbm, "unit": "GB/s",
+                      "frac": shade_rate / hbm, "peak_source": hbm_src,
+                      "kernel": "shade_kernel (reference estimator)",
+                      "launches_per_render": timing["shade_launches"] // args.steps, "ms_per_render": shade_ms,
+                      "share_of_step": shade_ms / ms, "vertices_per_render": shaded,
+                      "algorithmic_bytes_per_render": shade_bytes,
+                      "bytes_model": f"{SHADE_VERTEX_BYTES} B per shaded path vertex: 32 B of material, 2 x 64 B of "
+                                     "path state read and written, 8 B of queue entries"}
+    # kernels per render: extend and shade per depth; per round plan, raygen, accumulate and the
+    # compaction (none after the last round); plan set-up, image preparation, G-buffer, a-trous
+    rounds = launches // (depth + 1) if launches else 0
+    kernels_per_render = 2 * launches + 4 * rounds - 1 + 2 + 1 + 12
     out = {"value": value, "ms_per_step": ms, "Mrays_per_s": replica_throughput(rays, world, ms / 1e3),
            "samples_per_render": st["samples"], "rays_per_render": {k: st[k] for k in (
                "camera_paths", "bounce_rays", "shadow_rays", "gbuffer_rays")},
-           "e2e": e2e, "roofline": roofline, "clocks": clocks.summary(),
+           "e2e": e2e, "roofline": roofline, "shade_roofline": shade_roofline, "clocks": clocks.summary(),
            "gpu_launches": kernels_per_render * args.steps}
     gs.free()
     return out
@@ -992,6 +1008,7 @@ def main():
                 "ms_per_step": render["ms_per_step"], "Mrays_per_s": render["Mrays_per_s"],
                 "config": render_config(args, world), "e2e": render["e2e"],
                 "gpu_launches": render["gpu_launches"], "roofline": render["roofline"],
+                "shade_roofline": render["shade_roofline"],
                 "cpu_baseline": cpu_render_line, "clocks": render["clocks"],
                 "samples_per_render": render["samples_per_render"], "rays_per_render": render["rays_per_render"],
                 "l2_read_gbs": l2_gbs, "traversal_microbench": trace, **extras}

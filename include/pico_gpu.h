@@ -306,6 +306,9 @@ int pico_gpu_render_device(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const
  * timed launches' summed duration. */
 int pico_gpu_set_render_probe(pico_gpu_ctx* ctx, int32_t time_extend, int32_t count_work);
 int pico_gpu_render_probe_read(pico_gpu_ctx* ctx, uint64_t* out4, double* extend_ms);
+/* With time_extend on, the shade launches (one per bounce depth) are bracketed too:
+ * their count and summed duration since the probe was set. */
+int pico_gpu_render_probe_read_shade(pico_gpu_ctx* ctx, uint64_t* launches, double* shade_ms);
 /* The read bandwidth of the L2 cache (GB/s), the roof of the closest-hit kernels
  * whose scene data stays in L2: one launch reads a device buffer of `bytes` bytes
  * (0: 32 MiB, which the GB300's L2 holds) `passes` times (0: 100) with 16-byte

@@ -65,6 +65,7 @@ SIGNATURES = {
                                          _vp]),
     "pico_gpu_set_render_probe": (C.c_int, [_vp, _i32, _i32]),
     "pico_gpu_render_probe_read": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(C.c_double)]),
+    "pico_gpu_render_probe_read_shade": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(C.c_double)]),
     "pico_gpu_l2_read_bandwidth": (C.c_int, [_vp, _u64, _u32, C.POINTER(C.c_double)]),
     "pico_gpu_denoiser_inputs": (C.c_int, [_vp, _vp, C.POINTER(CCamera), _fp, _fp, _fp]),
     "pico_gpu_atrous": (C.c_int, [_vp, _fp, _fp, _fp, _fp, _u32, _u32, _fp]),
@@ -208,8 +209,12 @@ class Context:
         out = (C.c_uint64 * 4)()
         ms = C.c_double(0.0)
         self.check(self.lib.pico_gpu_render_probe_read(self.handle, out, C.byref(ms)), "render_probe_read")
+        n_shade = C.c_uint64(0)
+        shade_ms = C.c_double(0.0)
+        self.check(self.lib.pico_gpu_render_probe_read_shade(self.handle, C.byref(n_shade), C.byref(shade_ms)),
+                   "render_probe_read_shade")
         return {"launches": int(out[0]), "nodes": int(out[1]), "tris": int(out[2]), "instances": int(out[3]),
-                "extend_ms": ms.value}
+                "extend_ms": ms.value, "shade_launches": int(n_shade.value), "shade_ms": shade_ms.value}
 
     def l2_read_bandwidth(self, nbytes: int = 0, passes: int = 0) -> float:
         """Measured L2 read bandwidth in GB/s (pico_gpu_l2_read_bandwidth)."""

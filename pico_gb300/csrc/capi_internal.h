@@ -76,6 +76,10 @@ struct pico_gpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;
+    // a low-priority stream that a render forks its G-buffer onto (it needs none of the
+    // samples), joined before the denoiser; created at the first denoised render
+    cudaStream_t side = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     pico::DeviceStatus* status = nullptr;   // two status blocks, one per stream
     std::string last_error;
     pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
@@ -97,6 +101,7 @@ struct pico_gpu_ctx {
     pico_gpu_nrc* cache = nullptr;              // radiance cache of PICO_ESTIMATOR_RADIANCE_CACHE renders
     BatchState* batch = nullptr;                // per-render state and streams of pico_gpu_render_many
     pico::LaunchTimer* extend_timer = nullptr;  // pico_gpu_set_render_probe: events around closest-hit launches
+    pico::LaunchTimer* shade_timer = nullptr;   // ... and around the shade launches
     bool count_work = false;                    // pico_gpu_set_render_probe: counting closest-hit variant
     pico::DeviceStatus* status2() { return status + 1; }
 };

@@ -931,6 +931,7 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
                                   const RenderProbe* probe = nullptr)
 {
     LaunchTimer* timer = probe ? probe->timer : nullptr;
+    LaunchTimer* shade_timer = probe ? probe->shade_timer : nullptr;
     unsigned long long* counters = probe ? probe->counters : nullptr;
     cudaError_t e = cudaSuccess;
     const bool trace_last =
@@ -951,12 +952,14 @@ static cudaError_t run_depth_loop(const SceneView& sc, PathBatch& b, uint32_t ma
         e = cudaMemsetAsync(&b.counters[cur ^ 1], 0, sizeof(uint32_t), st);
         if (e == cudaSuccess) e = cudaMemsetAsync(&b.counters[2], 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
+        if (shade_timer && (e = shade_timer->record(st)) != cudaSuccess) return e;
         if (physical)
             shade_physical_kernel<<<grid_for(shade_physical_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth,
                                                                                          max_depth, nrc);
         else
             shade_kernel<<<grid_for(shade_kernel, b.n, kRenderThreads), kRenderThreads, 0, st>>>(sc, b, cur, depth, max_depth,
                                                                                     trace_last);
+        if (shade_timer && (e = shade_timer->record(st)) != cudaSuccess) return e;
         cur ^= 1;
     }
     return cudaGetLastError();

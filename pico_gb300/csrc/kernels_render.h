@@ -75,6 +75,7 @@ struct LaunchTimer {
 struct RenderProbe {
     LaunchTimer* timer;
     unsigned long long* counters;      // 4 counters, or null
+    LaunchTimer* shade_timer;          // events around the shade launches, or null
 };
 
 // What the physical shade step does for the radiance cache.
