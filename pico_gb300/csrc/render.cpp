@@ -78,6 +78,8 @@ void free_render_buffers(pico_gpu_ctx* ctx)
     ctx->render = nullptr;
     delete ctx->extend_timer;
     ctx->extend_timer = nullptr;
+    delete ctx->shade_timer;
+    ctx->shade_timer = nullptr;
 }
 
 cudaError_t reserve_paths(RenderBuffers& r, size_t n)
@@ -286,7 +288,7 @@ static int run_exit_aware_rounds(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
     const uint32_t rounds = 1 + (cfg->max_samples - first + later - 1) / later;
     RoundPlan* plan = as<RoundPlan>(r.plan);
     uint32_t* lists[2] = {as<uint32_t>(r.pix_list), as<uint32_t>(r.pix_list2)};
-    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr};
+    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr, ctx->shade_timer};
     const RenderProbe* pp = (probe.timer || probe.counters) ? &probe : nullptr;
     e = launch_plan_init(plan, nactive, st);
     for (uint32_t k = 0; k < rounds && e == cudaSuccess; ++k) {
@@ -326,7 +328,7 @@ int run_sample_batches(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pic
     const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, spb_cap));
     cudaError_t e = reserve_paths(r, (size_t)chunk_pix * spb_max);
     if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
-    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr};
+    const RenderProbe probe{ctx->extend_timer, ctx->count_work ? ctx->status->counters : nullptr, ctx->shade_timer};
     const RenderProbe* pp = (probe.timer || probe.counters) ? &probe : nullptr;
     for (size_t p0 = 0; p0 < nactive && !cancelled; p0 += chunk_pix) {
         const uint32_t npix = (uint32_t)std::min<size_t>(chunk_pix, nactive - p0);
@@ -541,10 +543,14 @@ int pico_gpu_set_render_probe(pico_gpu_ctx* ctx, int32_t time_extend, int32_t co
     if (e != cudaSuccess) return cuda_error(ctx, e, "render probe");
     if (time_extend) {
         if (!ctx->extend_timer) ctx->extend_timer = new LaunchTimer();
+        if (!ctx->shade_timer) ctx->shade_timer = new LaunchTimer();
         ctx->extend_timer->reset();
+        ctx->shade_timer->reset();
     } else {
         delete ctx->extend_timer;
         ctx->extend_timer = nullptr;
+        delete ctx->shade_timer;
+        ctx->shade_timer = nullptr;
     }
     ctx->count_work = count_work != 0;
     e = cudaMemset(ctx->status->counters, 0, sizeof(ctx->status->counters));
@@ -568,6 +574,20 @@ int pico_gpu_render_probe_read(pico_gpu_ctx* ctx, uint64_t* out4, double* extend
     out4[2] = c[1];
     out4[3] = c[2];
     *extend_ms = ms;
+    return PICO_OK;
+}
+
+int pico_gpu_render_probe_read_shade(pico_gpu_ctx* ctx, uint64_t* launches, double* shade_ms)
+{
+    if (!ctx || !launches || !shade_ms) return PICO_ERR_INVALID_ARG;
+    const DeviceScope device_scope(ctx->device);
+    cudaError_t e = cudaDeviceSynchronize();
+    double ms = 0.0;
+    uint64_t n = 0;
+    if (e == cudaSuccess && ctx->shade_timer) e = ctx->shade_timer->total(ms, n);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "render probe");
+    *launches = n;
+    *shade_ms = ms;
     return PICO_OK;
 }
 
