@@ -76,10 +76,6 @@ struct pico_gpu_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;
-    // a low-priority stream that a render forks its G-buffer onto (it needs none of the
-    // samples), joined before the denoiser; created at the first denoised render
-    cudaStream_t side = nullptr;
-    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     pico::DeviceStatus* status = nullptr;   // two status blocks, one per stream
     std::string last_error;
     pico::DeviceBuffer buf_a, buf_b, buf_c, buf_d, buf_e;
