@@ -684,36 +684,48 @@ __global__ void __launch_bounds__(kRenderThreads) accumulate_kernel(PathBatch b,
         if (b.done[pixel]) continue;
         float* px = b.pixels + 3 * (size_t)pixel;
         float* var = b.variance + 3 * (size_t)pixel;
+        // the pixel's mean and variance stay in registers for the batch; the payloads are
+        // loaded two samples ahead of their use (the running mean is serial per pixel)
+        float mean[3] = {px[0], px[1], px[2]}, vr[3] = {var[0], var[1], var[2]};
         uint32_t cnt = b.count[pixel];
         uint32_t taken = b.taken[pixel];
         const uint32_t taken0 = taken;
+        const float4* pay = b.pay + slot;
+        const float4 none = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float4 ahead0 = pay[0], ahead1 = spb > 1 ? pay[npix] : none;
         for (uint32_t s = 0; s < spb && taken < max_samples; ++s) {
             // the path's payload is the sample; NaN / Inf becomes pink (Integrators.cpp:145-146)
-            const float4 x4 = b.pay[(size_t)s * npix + slot];
+            const float4 x4 = ahead0;
+            ahead0 = ahead1;
+            if (s + 2 < spb) ahead1 = pay[(size_t)(s + 2) * npix];
             const bool finite = isfinite(x4.x) && isfinite(x4.y) && isfinite(x4.z);
             float x[3] = {finite ? x4.x : 1.0f, finite ? x4.y : 0.4f, finite ? x4.z : 0.7f};
             const uint32_t prev = cnt;
             ++taken;
             if (prev < 1) {
                 cnt = 1;
-                var[0] = var[1] = var[2] = 0.0f;
+                vr[0] = vr[1] = vr[2] = 0.0f;
             } else {
                 const float g = div(1.0f, (float)(prev + 1));
                 const float f = physical ? g : div(1.0f, (float)prev);
                 for (int c = 0; c < 3; ++c) {
-                    const float pp = px[c];
+                    const float pp = mean[c];
                     const float np = add(pp, mul(sub(x[c], pp), f));
-                    var[c] = mul(add(mul(var[c], (float)prev), mul(sub(x[c], pp), sub(x[c], np))), g);
+                    vr[c] = mul(add(mul(vr[c], (float)prev), mul(sub(x[c], pp), sub(x[c], np))), g);
                     x[c] = np;
                 }
                 cnt = prev + 1;
             }
-            px[0] = x[0]; px[1] = x[1]; px[2] = x[2];
-            if (!physical && prev > 4 && var[0] <= max_variance && var[1] <= max_variance &&
-                var[2] <= max_variance) {
+            mean[0] = x[0]; mean[1] = x[1]; mean[2] = x[2];
+            if (!physical && prev > 4 && vr[0] <= max_variance && vr[1] <= max_variance &&
+                vr[2] <= max_variance) {
                 b.done[pixel] = 1;
                 break;
             }
+        }
+        if (taken != taken0) {
+            px[0] = mean[0]; px[1] = mean[1]; px[2] = mean[2];
+            var[0] = vr[0]; var[1] = vr[1]; var[2] = vr[2];
         }
         if (taken >= max_samples) b.done[pixel] = 1;
         b.count[pixel] = cnt;
