@@ -401,6 +401,11 @@ def bench_radiance_cache(ctx, args, torch, local, plain_series):
     return out
 
 
+class MeasuredL2:
+    """The L2 read bandwidth measured at the start of the run (GB/s), for the secondary rooflines."""
+    gbs = None
+
+
 def bench_cache_kernels(ctx, torch, local):
     """Inference over 2^21 queries and one training step over 2^16 records, device buffers."""
     from pico_gb300 import RadianceCache
@@ -444,6 +449,17 @@ def bench_cache_kernels(ctx, torch, local):
     c.free()
     peak = measured_bf16_peak()
     ach = NRC_FLOPS_PER_QUERY * n / (ms_inf / 1e3) / 1e12
+    # the hash-grid encoding against the L2 (the 32 MiB table stays in L2): 16 levels x 8 corners
+    # of 4-byte features per query, each gather a 32-byte sector
+    gather_bytes = n * 16 * 8 * 32 / (ms_inf / 1e3) / 1e9
+    l2 = MeasuredL2.gbs
+    gather = {"bound": "l2", "achieved": gather_bytes, "unit": "GB/s",
+              "sector_bytes_per_query": 16 * 8 * 32, "algorithmic_bytes_per_query": 16 * 8 * 4,
+              "note": "sector traffic of the corner gathers (an upper bound: neighbouring corners of the dense "
+                      "levels can share a sector)"}
+    if l2:
+        gather.update({"peak": l2, "frac": gather_bytes / l2,
+                       "peak_source": "measured in this run: L2 read bandwidth (pico_gpu_l2_read_bandwidth)"})
     return {"inference": {"queries": n, "ms": ms_inf, "Mqueries_per_s": n / ms_inf / 1e3,
                           "ms_by_warpgroups_per_cta": per_groups,
                           "queries_note": "uniformly random positions over the lit field's box: incoherent "
@@ -451,6 +467,7 @@ def bench_cache_kernels(ctx, torch, local):
                           "roofline": {"bound": "tensor", "achieved": ach, "peak": peak[0], "unit": "TFLOP/s",
                                        "frac": ach / peak[0], "peak_source": peak[1],
                                        "algorithmic_flops_per_query": NRC_FLOPS_PER_QUERY},
+                          "gather_roofline": gather,
                           "encoding_bytes_per_query": 16 * 8 * 4},
             "training_step": {"records": nt, "ms": ms_train,
                               "note": "grid-gradient clear, fused forward+backward, weight-gradient reduction and "
@@ -972,6 +989,7 @@ def main():
 
     ctx = pico_gb300.Context(local)
     l2_gbs = l2_peak(ctx)
+    MeasuredL2.gbs = l2_gbs
     trace = bench_trace(ctx, args, torch, local, dist, world, l2_gbs)
     render = None
     if args.headline == "render":
