@@ -263,6 +263,13 @@ int pico_gpu_trace_stats(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                          const pico_ray* d_rays, uint64_t n, uint64_t* out3, void* stream);
 
 /* ---- rendering (Scene::render_scene_to_memory) --------------------------- */
+/* No counterpart in the reference.  The most paths (pixels x samples) a batch of
+ * this context's renders holds: 0 for the default, 2^26, else 64 .. 2^26.  A
+ * smaller limit holds less path state on the device (208 bytes per path) for more
+ * launches; an image of more pixels than the limit is rendered in pixel chunks.
+ * The images are the same whatever the limit: a path depends only on its pixel and
+ * sample index, and each pixel takes its samples in order. */
+int pico_gpu_set_path_limit(pico_gpu_ctx* ctx, uint32_t max_paths);
 /* The render runs in batches of up to 2^26 paths (pixels x samples; 208 bytes of
  * path state each, 14 GB at the limit).  Where the reference's early exit can
  * stop pixels (reference estimator, max_variance >= 0) the first batch takes 6

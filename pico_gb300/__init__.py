@@ -64,6 +64,7 @@ SIGNATURES = {
     "pico_gpu_render_device": (C.c_int, [_vp, _vp, C.POINTER(CCamera), C.POINTER(CRenderConfig), _vp, _vp, _vp,
                                          _vp]),
     "pico_gpu_set_render_probe": (C.c_int, [_vp, _i32, _i32]),
+    "pico_gpu_set_path_limit": (C.c_int, [_vp, C.c_uint32]),
     "pico_gpu_render_probe_read": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(C.c_double)]),
     "pico_gpu_render_probe_read_shade": (C.c_int, [_vp, C.POINTER(_u64), C.POINTER(C.c_double)]),
     "pico_gpu_l2_read_bandwidth": (C.c_int, [_vp, _u64, _u32, C.POINTER(C.c_double)]),
@@ -199,6 +200,10 @@ class Context:
         self.check(self.lib.pico_gpu_host_buffer_in_place(self.handle, ptr, nbytes, C.byref(out)),
                    "host_buffer_in_place")
         return bool(out.value)
+
+    def set_path_limit(self, max_paths: int = 0):
+        """pico_gpu_set_path_limit: the most paths a render batch holds (0: the default, 2^26)."""
+        self.check(self.lib.pico_gpu_set_path_limit(self.handle, int(max_paths)), "set_path_limit")
 
     def set_render_probe(self, time_extend: bool = False, count_work: bool = False):
         """Measurement hooks on the closest-hit launches of renders (events / work counters); clears totals."""

@@ -88,6 +88,7 @@ struct pico_gpu_ctx {
     uint32_t max_iterations = pico::kTraceMaxIter;   // pico_gpu_set_traversal_limits
     uint32_t stack_entries = pico::kTraceStack;
     int triangle_test = PICO_TRIANGLE_MOLLER_TRUMBORE;   // pico_gpu_set_triangle_test
+    uint32_t max_paths = 0;   // pico_gpu_set_path_limit; 0: the default (kMaxPaths)
     uint64_t render_stats[5] = {0, 0, 0, 0, 0}; // tallies of the last pico_gpu_render call
     // the last render was pico_gpu_render_device: its tallies are read from the
     // device (after its stream) when asked for

@@ -136,14 +136,17 @@ bool valid_camera(const pico_camera* c) { return c && c->resolution[0] > 0 && c-
 // max_train_steps optimiser steps of at most train_batch records, spread over all
 // records of the pass) and every active pixel takes one sample whose path ends
 // in the cache.  The pixel list is on the device already.
+// Paths a render's batch may hold: the context's limit, else kMaxPaths.
+static uint32_t path_limit(const pico_gpu_ctx* ctx) { return ctx->max_paths ? ctx->max_paths : kMaxPaths; }
+
 int render_with_cache(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, pico_gpu_nrc* c, const pico_render_config* cfg,
                       const CameraView& cam, RenderBuffers& r, size_t nactive, const volatile int32_t* should_quit,
                       bool& cancelled)
 {
     cudaStream_t st = ctx->stream;
     const uint32_t W = cfg->width, H = cfg->height;
-    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, kMaxPaths);
-    const uint32_t ntrain = std::min<uint32_t>(c->cfg.train_paths, kMaxPaths);
+    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, path_limit(ctx));
+    const uint32_t ntrain = std::min<uint32_t>(c->cfg.train_paths, path_limit(ctx));
     const uint32_t max_depth = cfg->max_ray_depth;
     const size_t rec_cap = (size_t)ntrain * std::max(max_depth, 1u);
     const size_t q_cap = std::max<size_t>(chunk_pix, rec_cap);
@@ -262,9 +265,9 @@ static bool early_exit_on(const pico_render_config* cfg)
 }
 
 // Exit-aware rounds over the first `nactive` pixels of r.pix_list (at most
-// kMaxPaths of them): the first round takes kFirstExitSamples samples per pixel;
+// the path limit of them): the first round takes kFirstExitSamples samples per pixel;
 // after every round a compaction keeps the pixels still sampling and the next round
-// takes as many samples per pixel as fill the path state (kMaxPaths), so that
+// takes as many samples per pixel as fill the path state (the path limit), so that
 // rounds after the exits are dense.  Both are decided on the device (RoundPlan), so
 // nothing here waits for it: the host enqueues as many rounds as a render with no
 // exit needs, and rounds with nothing left to do launch empty kernels.  Images are
@@ -276,15 +279,16 @@ static int run_exit_aware_rounds(pico_gpu_ctx* ctx, const pico_gpu_scene* scene,
                                  cudaStream_t st, bool& cancelled)
 {
     const uint32_t cap = should_quit ? kCancelSamplesPerBatch : cfg->max_samples;
-    const uint32_t paths = (uint32_t)std::min<uint64_t>(kMaxPaths, (uint64_t)nactive * cfg->max_samples);
+    const uint32_t paths = (uint32_t)std::min<uint64_t>(path_limit(ctx), (uint64_t)nactive * cfg->max_samples);
     cudaError_t e = reserve_paths(r, paths);
     if (e == cudaSuccess) e = r.pix_list2.reserve((size_t)nactive * sizeof(uint32_t));
     if (e == cudaSuccess) e = r.plan.reserve(sizeof(RoundPlan));
     if (e != cudaSuccess) return cuda_error(ctx, e, "path state");
-    // rounds a render with no exit needs: the first, then rounds of the smallest
-    // later size (every pixel still sampling)
-    const uint32_t first = std::min({kFirstExitSamples, cfg->max_samples, cap});
+    // rounds a render with no exit needs: the first (as plan_round sizes it for all nactive
+    // pixels: at most kFirstExitSamples, and no more than the path state holds), then rounds of
+    // the smallest later size (every pixel still sampling)
     const uint32_t later = std::max(1u, std::min(paths / nactive, cap));
+    const uint32_t first = std::min({kFirstExitSamples, cfg->max_samples, later});
     const uint32_t rounds = 1 + (cfg->max_samples - first + later - 1) / later;
     RoundPlan* plan = as<RoundPlan>(r.plan);
     uint32_t* lists[2] = {as<uint32_t>(r.pix_list), as<uint32_t>(r.pix_list2)};
@@ -319,11 +323,11 @@ int run_sample_batches(pico_gpu_ctx* ctx, const pico_gpu_scene* scene, const pic
                        const CameraView& cam, RenderBuffers& r, size_t nactive, float* pixels, float* variance,
                        uint32_t* count, const volatile int32_t* should_quit, cudaStream_t st, bool& cancelled)
 {
-    if (early_exit_on(cfg) && nactive <= kMaxPaths)
+    if (early_exit_on(cfg) && nactive <= path_limit(ctx))
         return run_exit_aware_rounds(ctx, scene, cfg, cam, r, (uint32_t)nactive, pixels, variance, count, should_quit,
                                      st, cancelled);
-    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, kMaxPaths);
-    uint32_t spb_cap = kMaxPaths / chunk_pix;
+    const uint32_t chunk_pix = (uint32_t)std::min<size_t>(nactive, path_limit(ctx));
+    uint32_t spb_cap = path_limit(ctx) / chunk_pix;
     if (should_quit) spb_cap = std::min(spb_cap, kCancelSamplesPerBatch);
     const uint32_t spb_max = std::max<uint32_t>(1u, std::min<uint32_t>(cfg->max_samples, spb_cap));
     cudaError_t e = reserve_paths(r, (size_t)chunk_pix * spb_max);
@@ -532,6 +536,15 @@ int pico_gpu_render_stats(const pico_gpu_ctx* cctx, uint64_t* out5)
         ctx->stats_on_device = false;
     }
     for (int k = 0; k < 5; ++k) out5[k] = ctx->render_stats[k];
+    return PICO_OK;
+}
+
+int pico_gpu_set_path_limit(pico_gpu_ctx* ctx, uint32_t max_paths)
+{
+    if (!ctx) return PICO_ERR_INVALID_ARG;
+    if (max_paths != 0 && (max_paths < 64 || max_paths > kMaxPaths))
+        return set_error(ctx, PICO_ERR_INVALID_ARG, "path limit: 0 (the default, 2^26) or 64 .. 2^26");
+    ctx->max_paths = max_paths;
     return PICO_OK;
 }
 

@@ -56,6 +56,37 @@ def test_device_render_equals_host_render(ctx, estimator):
     assert got_stats["samples"] == int(got[1].sum()) > 0
 
 
+@pytest.mark.parametrize("estimator", [0, 1])
+@pytest.mark.parametrize("limit", [100_000, 20_000, 3_000, 64])
+def test_images_do_not_depend_on_the_path_limit(ctx, estimator, limit):
+    """A path depends only on its pixel and sample index and every pixel takes its samples in
+    order, so the batching cannot change an image: the Cornell box at 96 x 80 (7,680 pixels, 16 spp,
+    some pixels resumed from a first render) is rendered bit for bit alike, through both entry
+    points, with the default limit and with 100,000 paths (exit-aware rounds of 6, then 13 samples
+    per pixel), 20,000 (the first round capped below its 6 samples: rounds of 2), 3,000 (fewer paths
+    than pixels: the chunked schedule) and 64."""
+    gs = ctx.upload(scenes.cornell_box())
+    cam = scenes.cornell_camera(96, 80)
+    try:
+        start = gs.render(cam, 5, 3, seed=8)
+        start[1][::7] = 0                       # some pixels start afresh, the others resume
+        runs = []
+        for lim in (0, limit):
+            ctx.set_path_limit(lim)
+            runs.append(gs.render(cam, 5, 16, seed=9, estimator=estimator, pixels=start[0].copy(),
+                                  sample_count=start[1].copy(), variance=start[2].copy(), denoise=True))
+            runs.append(device_render(ctx, gs, cam, 5, 16, 9, estimator=estimator, denoise=True,
+                                      start=(start[0], start[1], start[2])))
+    finally:
+        ctx.set_path_limit(0)
+        gs.free()
+    for other in runs[1:]:
+        for g, w, name in zip(other, runs[0], ("pixels", "sample counts", "variance")):
+            np.testing.assert_array_equal(g, w, err_msg=name)
+    with pytest.raises(pico_gb300.PicoError):
+        ctx.set_path_limit(10)
+
+
 def test_device_render_continues_progressive_buffers(ctx):
     gs = ctx.upload(scenes.cornell_box())
     cam = scenes.cornell_camera(32, 32)
