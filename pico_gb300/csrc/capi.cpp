@@ -198,7 +198,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     const GpuNode* nodes; const GpuTri* tris; const GpuTriShade* tshade; const GpuInstance* insts;
     const GpuInstanceShade* ishade; const uint32_t* irank; const GpuMaterial* mats; const GpuLight* lights;
     const float* law; const uint32_t* lai; const float* lpos; const unsigned char* skypx; const uint32_t* titems;
-    const float* lgeo; const uint32_t* lofi; const float* lpick;
+    const float* lgeo; const uint32_t* lofi; const float* lpick; const float* lbox;
     if (e == cudaSuccess) e = upload(fs.nodes, nodes);
     if (e == cudaSuccess) e = upload(fs.tris, tris);
     if (e == cudaSuccess) e = upload(fs.tri_shade, tshade);
@@ -213,6 +213,7 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     if (e == cudaSuccess) e = upload(fs.light_tri_geo, lgeo);
     if (e == cudaSuccess) e = upload(fs.light_of_inst, lofi);
     if (e == cudaSuccess) e = upload(fs.light_pick, lpick);
+    if (e == cudaSuccess) e = upload(fs.light_boxes, lbox);
     if (e == cudaSuccess) e = upload(fs.sky_pixels, skypx);
     if (e == cudaSuccess) e = upload(fs.tlas_items, titems);
     if (e != cudaSuccess) {
@@ -223,6 +224,8 @@ int pico_gpu_scene_upload(pico_gpu_ctx* ctx, const pico_scene_desc* desc, pico_g
     v.inst_rank = irank; v.tlas_items = titems; v.materials = mats; v.lights = lights; v.light_alias_weight = law;
     v.light_alias_index = lai; v.light_positions = lpos; v.light_tri_geo = lgeo; v.light_of_inst = lofi;
     v.light_pick = lpick;
+    v.light_boxes = lbox;
+    v.light_bounds = fs.light_bounds ? 1u : 0u;
     v.nlights = (uint32_t)fs.lights.size();
     v.tlas_root_ref = fs.tlas_root_ref;
     v.tlas_fast_root_ref = fs.tlas_fast_root_ref;

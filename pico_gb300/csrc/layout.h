@@ -129,4 +129,8 @@ struct SceneView {
     uint32_t max_iterations;
     uint32_t stack_entries;
     uint32_t watertight;                // the launching context's triangle test is the watertight one
+    // per NEE light its widened world box (lo x, y, z, 0, hi x, y, z, 0): no hit on
+    // the light lies outside it.  light_bounds: every light has one (else none is used).
+    const float* light_boxes;
+    uint32_t light_bounds;
 };

@@ -778,6 +778,31 @@ std::string build_flat_scene(const pico_scene_desc& desc, FlatScene& fs)
         fs.light_alias_index.insert(fs.light_alias_index.end(), ba.begin(), ba.end());
         fs.lights.push_back(l);
     }
+    // World boxes of the NEE lights, for the early exit of the closest-hit shadow
+    // rays: every point a hit on a light reports (T times an object-space point of
+    // its triangles, or of its implicit shape's unit box) lies in its light's box up
+    // to float error, so no hit on a light lies nearer than the nearest box.  The
+    // boxes are widened by 1e-4 of the scene's largest coordinate magnitude, ten
+    // times the near-first TLAS's widening.  None when a light's vertices were not
+    // transformed, a box is not finite, or there are too many lights to scan per ray.
+    fs.light_boxes.clear();
+    fs.light_bounds = fs.lights.size() <= kMaxBoundedLights;
+    const double lpad = 1e-4 * mag;
+    for (size_t l = 0; fs.light_bounds && l < fs.lights.size(); ++l) {
+        const std::array<double, 6>& e = extent[fs.lights[l].inst];
+        bool ok = e[0] <= e[3] && e[1] <= e[4] && e[2] <= e[5];
+        for (int a = 0; a < 6; ++a) ok = ok && std::isfinite(e[a]);
+        if (!ok) {
+            fs.light_bounds = false;
+            break;
+        }
+        for (int a = 0; a < 3; ++a) fs.light_boxes.push_back((float)(e[a] - lpad));
+        fs.light_boxes.push_back(0.0f);
+        for (int a = 0; a < 3; ++a) fs.light_boxes.push_back((float)(e[3 + a] + lpad));
+        fs.light_boxes.push_back(0.0f);
+    }
+    if (!fs.light_bounds) fs.light_boxes.clear();
+
     for (int a = 0; a < 3; ++a) fs.sky[a] = desc.sky_rgb[a];
     const bool sun = desc.sky && desc.sky->use_sun;
     light_pick_table(desc, fs.lights, sun, fs.light_pick);

@@ -21,6 +21,9 @@ struct TreeDump {
     std::vector<uint32_t> values;
 };
 
+// The most NEE lights whose boxes a shadow ray scans for its early exit.
+constexpr size_t kMaxBoundedLights = 64;
+
 // Host image of everything pico_gpu_scene_upload copies to the device.
 struct FlatScene {
     // kept only when keep_trees is set before build_flat_scene: the reference-layout
@@ -48,6 +51,11 @@ struct FlatScene {
     // to their power (sum of emitted radiance channels x world area), implicit
     // lights get 0 (the physical estimator reaches them by BSDF sampling only).
     std::vector<float> light_pick;
+    // Per NEE light, its widened world box (lo x, y, z, 0, hi x, y, z, 0): no hit on
+    // the light lies outside it.  light_bounds: the boxes exist for every light
+    // (none may be missing for the shadow rays' early exit to hold).
+    std::vector<float> light_boxes;
+    bool light_bounds = false;
     uint32_t tlas_root_ref = PICO_REF_EMPTY;
     float tlas_lo[3] = {0, 0, 0}, tlas_hi[3] = {0, 0, 0};
     uint32_t tlas_fast_root_ref = PICO_REF_EMPTY;   // refitted TLAS for the near-first walk

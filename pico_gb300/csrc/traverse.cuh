@@ -370,10 +370,14 @@ __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t ra
 
 // kAnyHit: only hits at a world distance below tmax count, and the walk returns
 // at the first instance whose candidate is one (an occlusion query: a hit is
-// reported exactly when the closest hit lies below tmax).
+// reported exactly when the closest hit lies below tmax).  Otherwise the walk
+// returns early once its best hit lies below exit_below: the closest hit then
+// lies below it too, and a caller that only asks what kind of instance is hit
+// (a shadow ray whose lights all lie at or beyond exit_below) has its answer.
 template <bool kCount, bool kImplicit, bool kAnyHit = false, bool kRuntimeBounds = false, bool kWT = false>
 __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
-                                                TraceCounters* cnt, float tmax = INFINITY)
+                                                TraceCounters* cnt, float tmax = INFINITY,
+                                                float exit_below = -INFINITY)
 {
     using namespace ex;
     const uint32_t max_iter = kRuntimeBounds ? sc.max_iterations : kTraceMaxIter;
@@ -464,7 +468,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
                 const float tw = world_distance(sc, cur, ltri, lu, lv, o);
                 if (kAnyHit ? tw < best.t : (tw < best.t || (tw == best.t && cur < best.rank))) {
                     best.t = tw; best.rank = cur; best.tri = ltri; best.u = lu; best.v = lv;
-                    if (kAnyHit) return kTraceOk;
+                    if (kAnyHit || tw < exit_below) return kTraceOk;
                 }
             }
             in_blas = false;
@@ -509,7 +513,7 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
             if (implicit_candidate(sc.insts + rank, o, d, tw, t) &&
                 (kAnyHit ? tw < best.t : (tw < best.t || (tw == best.t && rank < best.rank)))) {
                 best.t = tw; best.rank = rank; best.tri = kImplicitTri; best.u = t; best.v = 0.0f;
-                if (kAnyHit) return kTraceOk;
+                if (kAnyHit || tw < exit_below) return kTraceOk;
                 limit = fminf(best.t, kMaxFinite);
             }
             ref = sp ? stack[--sp] : PICO_REF_DONE;
@@ -670,16 +674,38 @@ __device__ __forceinline__ int trace_reference_order(const SceneView& sc, const 
     return kTraceOk;
 }
 
+// The closest hit; the near-first walk may return early with a hit below
+// exit_below instead (see trace_near_first), the reference order never does.
 template <bool kCount, int kVariant>
 __device__ __forceinline__ int trace_closest(const SceneView& sc, const float4 o, const float4 d, TraceHit& best,
-                                             TraceCounters* cnt)
+                                             TraceCounters* cnt, float exit_below = -INFINITY)
 {
     constexpr bool kImplicit = (kVariant & kWithImplicit) != 0;
     constexpr bool kRuntime = (kVariant & kBounded) != 0;
     constexpr bool kWT = (kVariant & kWatertight) != 0;
     if ((kVariant & kReferenceOrder) != 0)
         return trace_reference_order<kCount, kImplicit, kRuntime, kWT>(sc, o, d, best, cnt);
-    return trace_near_first<kCount, kImplicit, false, kRuntime, kWT>(sc, o, d, best, cnt);
+    return trace_near_first<kCount, kImplicit, false, kRuntime, kWT>(sc, o, d, best, cnt, INFINITY, exit_below);
+}
+
+// A lower bound on the world distance of every hit on a NEE light seen from o:
+// the distance from o to the nearest light's widened world box (a hit's world
+// distance |T p - o| is at least that of its xyz part, and T p lies in its light's
+// box up to float error far below the widening), or -inf when the scene has no
+// such boxes.  A NaN origin gives 0.
+__device__ __forceinline__ float light_distance_bound(const SceneView& sc, const float4 o)
+{
+    if (!sc.light_bounds) return -INFINITY;
+    const float4* box = reinterpret_cast<const float4*>(sc.light_boxes);
+    float b2 = INFINITY;
+    for (uint32_t l = 0; l < sc.nlights; ++l) {
+        const float4 lo = __ldg(box + 2 * l), hi = __ldg(box + 2 * l + 1);
+        const float gx = fmaxf(fmaxf(lo.x - o.x, o.x - hi.x), 0.0f);
+        const float gy = fmaxf(fmaxf(lo.y - o.y, o.y - hi.y), 0.0f);
+        const float gz = fmaxf(fmaxf(lo.z - o.z, o.z - hi.z), 0.0f);
+        b2 = fminf(b2, gx * gx + gy * gy + gz * gz);
+    }
+    return sqrtf(b2);
 }
 
 // Whether anything lies at a world distance below tmax along the ray (closest-hit

@@ -417,3 +417,54 @@ def test_render_with_btdfs_and_implicit_lights_statistically_matches(ctx, oracle
     assert frac >= 0.995, f"only {frac:.4f} of pixel channels within 4 standard errors"
     assert z_.mean() < 1.0, f"mean |z| {z_.mean():.3f}"
     assert abs(g_mean.mean() - r_mean.mean()) < 0.02 * r_mean.mean()
+
+
+def stacked_lights_scene() -> "pico_gb300.types.SceneData":
+    """Quad lights over a few icospheres and a ground, built so that shadow rays end at
+    every distance from their lights: light B hangs just below light A (rays aimed at A
+    end on B), a sphere sits just under light C and another right beside it, and a sun
+    shines through the gaps."""
+    from pico_gb300.types import DIFFUSE, DIELECTRIC, LIGHT, Instance, SceneData, Sky
+    s = SceneData(materials=[Material(diffuse=(0.6, 0.6, 0.6))], sky=(0.0, 0.0, 0.0))
+    s.sky_image = Sky(use_sun=True, sun_direction=(0.3, -1.0, 0.2), sun_colour=(2.0, 1.8, 1.5))
+    s.meshes.append(scenes.quad_mesh([[-30, 0, -30], [-30, 0, 30], [30, 0, 30], [30, 0, -30]], [0, 1, 0]))
+    s.instances.append(Instance(0, scenes.glm_storage(np.eye(4)), DIFFUSE, 0))
+    s.meshes.append(scenes.icosphere(2))
+    s.materials.append(scenes.metalness_roughness((0.7, 0.4, 0.3), 0.0, 0.6))
+    for pos, r in (((0, 1.5, 0), 1.5), ((4, 1, 3), 1.0), ((-5, 2, -2), 2.0), ((8, 8.6, 0), 1.0),
+                   ((9.4, 8.0, 1.5), 0.5), ((-3, 6, 4), 1.2)):
+        T = scenes.translate(pos) @ scenes.scale(r)
+        s.instances.append(Instance(1, scenes.glm_storage(T), DIELECTRIC, 1))
+    for (cx, y, cz, h, le) in ((0, 10, 0, 3, 8.0), (0, 9.6, 0, 1.2, 20.0), (8, 10, 0, 2, 15.0),
+                               (-8, 12, 6, 2.5, 5.0)):
+        s.meshes.append(scenes.quad_mesh([[cx - h, y, cz - h], [cx + h, y, cz - h], [cx + h, y, cz + h],
+                                          [cx - h, y, cz + h]], [0, -1, 0]))
+        s.materials.append(Material(diffuse=(0.8, 0.8, 0.8), emissive=(le, le, le)))
+        s.instances.append(Instance(len(s.meshes) - 1, scenes.glm_storage(np.eye(4)), LIGHT, len(s.materials) - 1))
+    return s
+
+
+@pytest.mark.parametrize("scene_name", ["stacked_lights", "lit_field"])
+def test_shadow_early_exit_keeps_images(ctx, scene_name):
+    """A closest-hit shadow ray of the near-first walk stops at a hit nearer than every
+    light's box (a sun ray at its first hit), the reference order never stops early; both
+    walks return the oracle's hits, so the renders must agree bit for bit."""
+    if scene_name == "stacked_lights":
+        scene = stacked_lights_scene()
+        cam = pico_gb300.types.Camera(position=(0.0, 6.0, -22.0), direction=(0.0, -0.1, 1.0),
+                                      resolution=(64, 48), aspect=64 / 48)
+    else:
+        scene = scenes.lit_field(n_instances=256, level=2, seed=77, n_lights=6, extent=20.0)
+        cam = scenes.lit_field_camera(64, 48)
+    gs = ctx.upload(scene)
+    out = {}
+    try:
+        for order in (1, 0):
+            ctx.set_traversal_order(order)
+            out[order] = gs.render(cam, 5, 16, seed=9, max_variance=-1.0)
+    finally:
+        ctx.set_traversal_order(0)
+        gs.free()
+    for g, w, name in zip(out[0], out[1], ("pixels", "sample counts", "variance")):
+        np.testing.assert_array_equal(g, w, err_msg=name)
+    assert out[0][0].mean() > 0.0
