@@ -368,12 +368,14 @@ __device__ __forceinline__ float world_distance(const SceneView& sc, uint32_t ra
     return world_distance_at(sc, rank, px, py, pz, o);
 }
 
-// Lanes of a warp that must wait at a leaf, an instance entry or an instance exit
-// before the warp runs those branches while other lanes are at inner nodes (0:
-// never wait).  The 1080p lit-field renders: 4 lanes 1.5 % slower than no waiting,
-// 8 2.4 % faster, 12 3.4 %, 16 2.8 %, 20 1.6 %, 24 no faster, 32 (a while-while
-// walk) 1.5 % slower; exempting the BLAS leaves from the wait made them 9 % slower.
-constexpr int kPostponeLanes = 12;
+// Whether lanes wait at a leaf, an instance entry or an instance exit while other
+// lanes of their warp walk inner nodes, until half of the warp's live lanes wait.
+// The 1080p lit-field renders, against no waiting: a fixed count of 4 waiting
+// lanes 1.5 % slower, 8 2.4 % faster, 12 3.4 %, 16 2.8 %, 20 1.6 %, 24 no
+// faster, 32 (a while-while walk) 1.5 % slower; exempting the BLAS leaves 9 %
+// slower; a share of the live lanes instead of a count: 3/8 6 %, 7/16 6.8 %,
+// 1/2 7.1 %, 9/16 6.6 %, 5/8 6.5 %, 3/4 5.1 % faster.
+constexpr bool kPostpone = true;
 
 // kAnyHit: only hits at a world distance below tmax count, and the walk returns
 // at the first instance whose candidate is one (an occlusion query: a hit is
@@ -432,15 +434,15 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
     for (uint32_t iter = 0;; ++iter) {
         if (iter >= max_iter) return kTraceIterLimit;
         if (ref == PICO_REF_DONE) break;
-        if constexpr (kPostponeLanes > 0) {
+        if constexpr (kPostpone) {
             // A move other than an inner node (a leaf, an instance entry or exit)
-            // waits while lanes of the warp walk inner nodes, until kPostponeLanes
-            // lanes wait: the warp then runs those rarer branches for several lanes
-            // at once instead of for one or two in most of its steps.
+            // waits while lanes of the warp walk inner nodes, until half of the
+            // live lanes wait: the warp then runs those rarer branches for many
+            // lanes at once instead of for one or two in most of its steps.
             const unsigned act = __activemask();
             const bool inner = !pico_is_leaf(ref);
             const unsigned at_node = __ballot_sync(act, inner);
-            if (!inner && at_node != 0 && __popc(act & ~at_node) < kPostponeLanes) {
+            if (!inner && at_node != 0 && 2 * __popc(act & ~at_node) < __popc(act)) {
                 --iter;   // a wait is no move
                 continue;
             }
