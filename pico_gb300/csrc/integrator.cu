@@ -160,8 +160,71 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
     }
 }
 
-// Persistent: 32 queue entries per warp fetch, each lane runs its ray to
-// completion.  One launch traces two queues back to back: the paths' next segments q[0, *count)
+// The entries of an extension launch for walk_queue: the depth's path segments
+// q[0, n0), then the shadow rays sq[0, n - n0); a lane's tag is its path index
+// with the ray's kind in the top two bits (0 segment, 1 shadow ray, 2 occlusion
+// query of the physical estimator).
+struct ExtendRays {
+    using Tag = uint32_t;
+    const SceneView& sc;
+    PathBatch& b;
+    const uint32_t* q;
+    const uint32_t* sq;
+    uint32_t n0;
+    int* err;
+
+    __device__ __forceinline__ uint32_t load(uint64_t k, float4& o, float4& d, float& tmax, float& exit_below,
+                                             bool& occlusion) const
+    {
+        const bool shadow = k >= n0;
+        const uint32_t i = shadow ? sq[k - n0] : q[k];
+        uint32_t kind = 0;
+        tmax = INFINITY;
+        exit_below = -INFINITY;
+        occlusion = false;
+        if (shadow) {
+            o = b.sorg[i];
+            d = b.sdir[i];
+            const float ew = b.senergy[i].w;
+            if (ew == 2.0f) {
+                // physical estimator: an occlusion query bounded by the light sample's distance
+                kind = 2;
+                tmax = b.scontrib[i].w;
+                occlusion = true;
+            } else {
+                // only whether the closest hit is a light (or, for a sun ray, nothing)
+                // counts: the walk may stop at a hit nearer than every light
+                kind = 1;
+                exit_below = ew != 0.0f ? INFINITY : light_distance_bound(sc, o);
+            }
+        } else {
+            o = b.org[i];
+            d = b.dir[i];
+        }
+        return i | (kind << 30);
+    }
+
+    __device__ __forceinline__ void finish(uint32_t tag, const TraceHit& h, int s) const
+    {
+        const uint32_t i = tag & 0x3fffffffu, kind = tag >> 30;
+        if (s != kTraceOk) atomicOr(err, s);
+        if (kind == 2) {
+            if (s == kTraceOk && h.tri == kNoHit) {
+                const float4 c = b.scontrib[i];
+                float4 p = b.pay[i];
+                p.x += c.x; p.y += c.y; p.z += c.z;
+                b.pay[i] = p;
+            }
+        } else {
+            extend_finish(sc, b, i, h, s, kind == 1);
+        }
+    }
+};
+
+// Persistent: in the near-first order the warps walk the launch's entries with
+// walk_queue (idle lanes refilled in batches); in the reference order each warp
+// takes 32 entries at a time and each lane runs its ray to completion.  One
+// launch traces two queues back to back: the paths' next segments q[0, *count)
 // and, when sq is given, the shadow rays sq[0, *scount) the previous shade left
 // (they write disjoint path fields and both finish before the next shade), so a
 // depth pays one launch and one tail.  kThreads per CTA (64, 128 or 256): the
@@ -189,38 +252,45 @@ __global__ void __launch_bounds__(kThreads, extend_threads_per_sm<kOrder>() / kT
         atomicAdd(tally, (unsigned long long)n0);
         if (sq) atomicAdd(stally, (unsigned long long)n1);
     }
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(work, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const unsigned long long k = base + lane;
-        if (k < n) {
-            const bool shadow = k >= n0;
-            const uint32_t i = shadow ? sq[k - n0] : q[k];
-            if (shadow && b.senergy[i].w == 2.0f) {
-                // physical estimator: an occlusion query bounded by the light sample's distance
-                const float4 c = b.scontrib[i];
-                bool occluded = true;
-                const int s = trace_occluded<kOrder, kCount>(sc, b.sorg[i], b.sdir[i], c.w, occluded, &cnt);
-                if (s != kTraceOk) atomicOr(err, s);
-                if (s == kTraceOk && !occluded) {
-                    float4 p = b.pay[i];
-                    p.x += c.x; p.y += c.y; p.z += c.z;
-                    b.pay[i] = p;
+    if constexpr ((kOrder & kReferenceOrder) == 0) {
+        ExtendRays rays{sc, b, q, sq, n0, err};
+        walk_queue<kCount, (kOrder & kWithImplicit) != 0, (kOrder & kBounded) != 0, (kOrder & kWatertight) != 0>(
+            sc, rays, n, work, &cnt);
+    } else {
+        // the reference order: each lane runs its ray to completion, 32 rays per warp fetch
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(work, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            const unsigned long long k = base + lane;
+            if (k < n) {
+                const bool shadow = k >= n0;
+                const uint32_t i = shadow ? sq[k - n0] : q[k];
+                if (shadow && b.senergy[i].w == 2.0f) {
+                    // physical estimator: an occlusion query bounded by the light sample's distance
+                    const float4 c = b.scontrib[i];
+                    bool occluded = true;
+                    const int s = trace_occluded<kOrder, kCount>(sc, b.sorg[i], b.sdir[i], c.w, occluded, &cnt);
+                    if (s != kTraceOk) atomicOr(err, s);
+                    if (s == kTraceOk && !occluded) {
+                        float4 p = b.pay[i];
+                        p.x += c.x; p.y += c.y; p.z += c.z;
+                        b.pay[i] = p;
+                    }
+                } else {
+                    // A shadow ray only asks whether its closest hit is a light (or, for a
+                    // sun ray, nothing), so its walk may stop at a hit nearer than every
+                    // light: the closest hit is then no light either.  A sun ray stops at
+                    // its first hit.
+                    const float4 o = shadow ? b.sorg[i] : b.org[i];
+                    float exit_below = -INFINITY;
+                    if (shadow) exit_below = b.senergy[i].w != 0.0f ? INFINITY : light_distance_bound(sc, o);
+                    TraceHit h;
+                    const int s = trace_closest<kCount, kOrder>(sc, o, shadow ? b.sdir[i] : b.dir[i], h, &cnt, exit_below);
+                    if (s != kTraceOk) atomicOr(err, s);
+                    extend_finish(sc, b, i, h, s, shadow);
                 }
-            } else {
-                // A shadow ray only asks whether its closest hit is a light (or, for a
-                // sun ray, nothing), so its walk may stop at a hit nearer than every
-                // light: the closest hit is then no light either.  A sun ray stops at
-                // its first hit.
-                const float4 o = shadow ? b.sorg[i] : b.org[i];
-                float exit_below = -INFINITY;
-                if (shadow) exit_below = b.senergy[i].w != 0.0f ? INFINITY : light_distance_bound(sc, o);
-                TraceHit h;
-                const int s = trace_closest<kCount, kOrder>(sc, o, shadow ? b.sdir[i] : b.dir[i], h, &cnt, exit_below);
-                if (s != kTraceOk) atomicOr(err, s);
-                extend_finish(sc, b, i, h, s, shadow);
             }
         }
     }

@@ -1,12 +1,14 @@
 // Closest-hit kernel for ray batches (UpperLevelBVH::get_closest_intersection
 // over many rays, Core/UpperLevelBVH.cpp:12-20).
 //
-// Persistent: the grid is a whole number of CTAs per SM and every warp pulls
-// 32 rays at a time from a global counter, so long rays do not leave SMs idle
-// at the tail of the batch.  Each lane then runs its ray to completion in a
-// tight loop (no warp-wide synchronisation per step: a ballot per step costs
-// about a third of the throughput).  128 threads with at most 64 registers each
-// keep eight CTAs resident per SM.  Rays are 32 B (two 16-byte loads), hits 20 B.
+// Persistent: the grid is a whole number of CTAs per SM and the warps pull rays
+// from a global counter, so long rays do not leave SMs idle at the tail of the
+// batch.  In the near-first order a warp's lanes walk the batch with
+// walk_queue: one ballot per move decides whether the rarer moves wait, and
+// idle lanes take new rays in batches; in the reference order each warp takes
+// 32 rays at a time and each lane runs its ray to completion.  128 threads with
+// at most 64 registers each keep eight CTAs resident per SM.  Rays are 32 B
+// (two 16-byte loads), hits 20 B.
 #include "kernels.h"
 #include "traverse.cuh"
 
@@ -33,6 +35,32 @@ __device__ __forceinline__ void write_hit(const SceneView& sc, const TraceHit& h
     *out = r;
 }
 
+// The rays of a batch for walk_queue: a lane's tag is the ray's index.
+struct BatchRays {
+    using Tag = uint64_t;
+    const SceneView& sc;
+    const float4* rays;
+    pico_hit* hits;
+    DeviceStatus* status;
+
+    __device__ __forceinline__ uint64_t load(uint64_t k, float4& o, float4& d, float& tmax, float& exit_below,
+                                             bool& occlusion) const
+    {
+        o = __ldg(rays + 2 * k);
+        d = __ldg(rays + 2 * k + 1);
+        tmax = INFINITY;
+        exit_below = -INFINITY;
+        occlusion = false;
+        return k;
+    }
+
+    __device__ __forceinline__ void finish(uint64_t tag, const TraceHit& h, int s) const
+    {
+        if (s != kTraceOk) atomicOr(&status->trace_error, s);
+        write_hit(sc, h, s, hits + tag);
+    }
+};
+
 template <bool kCount, int kOrder>
 __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
     trace_kernel(SceneView sc, const float4* __restrict__ rays, uint64_t n, pico_hit* __restrict__ hits,
@@ -40,6 +68,13 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
 {
     TraceCounters cnt{0, 0, 0, 0};
     const unsigned lane = threadIdx.x & 31u;
+    if constexpr ((kOrder & kReferenceOrder) == 0) {
+        BatchRays src{sc, rays, hits, status};
+        walk_queue<kCount, (kOrder & kWithImplicit) != 0, (kOrder & kBounded) != 0, (kOrder & kWatertight) != 0>(
+            sc, src, n, &status->work, &cnt);
+        if (kCount) flush_counters(cnt, status->counters);
+        return;
+    }
     for (;;) {
         unsigned long long base = 0;
         if (lane == 0) base = atomicAdd(&status->work, 32ull);
