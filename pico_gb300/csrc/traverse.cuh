@@ -581,20 +581,23 @@ __device__ __forceinline__ int nf_move(NearFirstState& w, const SceneView& sc, u
 
 // Whether a lane's next move waits: a move other than an inner node (a leaf, an
 // instance entry or exit, or handing in a finished walk) waits while lanes of the
-// warp walk inner nodes, until half of the busy lanes wait.  The warp then runs
+// warp walk inner nodes, until 5/8 of the busy lanes wait.  The warp then runs
 // those rarer branches for many lanes at once instead of for one or two in most
-// of its steps.  The 1080p lit-field renders, against no waiting: a fixed count
-// of 4 waiting lanes 1.5 % slower, 8 2.4 % faster, 12 3.4 %, 16 2.8 %, 20 1.6 %,
-// 24 no faster, 32 (a while-while walk) 1.5 % slower; exempting the BLAS leaves
-// 9 % slower; a share of the busy lanes instead of a count: 3/8 6 %, 7/16 6.8 %,
+// of its steps.  Measured on the 1080p lit-field renders, first with warps that
+// held their 32 rays to the end, against no waiting: a fixed count of 4 waiting
+// lanes 1.5 % slower, 8 2.4 % faster, 12 3.4 %, 16 2.8 %, 20 1.6 %, 24 no
+// faster, 32 (a while-while walk) 1.5 % slower; exempting the BLAS leaves 9 %
+// slower; a share of the busy lanes instead of a count: 3/8 6 %, 7/16 6.8 %,
 // 1/2 7.1 %, 9/16 6.6 %, 5/8 6.5 %, 3/4 5.1 % faster; releasing one kind of move
-// at a time 2 % slower than all at once.  `busy`: the lanes holding a walk,
-// `inner`: this lane's next move is an inner node (false for a lane without a
-// walk).  Every lane of `busy` must call it.
+// at a time 2 % slower than all at once.  Then with idle lanes refilled (see
+// walk_queue), against 1/2: 3/8 4.8 % slower, 5/8 1.3 % faster, 11/16 1.0 %,
+// 3/4 no faster, 7/8 2.5 % slower.  `busy`: the lanes holding a walk, `inner`:
+// this lane's next move is an inner node (false for a lane without a walk).
+// Every lane of `busy` must call it.
 __device__ __forceinline__ bool nf_release(unsigned busy, bool inner, unsigned& at_node)
 {
     at_node = __ballot_sync(busy, inner);
-    return at_node == 0 || 2 * __popc(busy & ~at_node) >= __popc(busy);
+    return at_node == 0 || 8 * __popc(busy & ~at_node) >= 5 * __popc(busy);
 }
 
 // One ray's closest hit by the near-first walk (or its occlusion query, kAnyHit).
