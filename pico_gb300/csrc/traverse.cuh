@@ -624,18 +624,24 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 }
 
 // Walks every ray of a queue of n entries with a warp's lanes, refilling idle
-// lanes from the shared counter `work` in batches.  The walks and their hits are
-// trace_near_first's; only the order in which a warp's lanes make their moves
-// differs.  `Rays` supplies the entries:
+// lanes in batches.  The walks and their hits are trace_near_first's; only the
+// order in which a warp's lanes make their moves differs.  `Rays` supplies the
+// entries:
 //   rays.load(k, o, d, tmax, exit_below, occlusion) -> a lane tag for entry k,
-//   rays.finish(tag, best, status) hands in a finished walk.
-// `Rays::Tag` is the tag's type.
-// A lane whose walk ended waits (see nf_release) to hand it in; once kRefillIdle
-// lanes of the warp are idle they take the next entries together, with one
-// atomic.  The earlier form, a warp holding its 32 rays until the slowest ended,
-// left lanes idle for most of a walk's tail: refilling at 8 idle lanes made the
-// 1080p renders 4.4 % faster (16 lanes 2.3 %, 12 4.3 %, 4 2.2 %, 2 and 1 slower).
+//   rays.finish(tag, best, status) hands in a finished walk;
+// `Rays::Tag` is the tag's type.  A lane whose walk ended waits (see
+// nf_release) to hand it in; once kRefillIdle lanes of the warp are idle they
+// take the next entries of the warp's claim together, and the warp claims
+// kClaim entries of the shared counter `work` at a time.  The earlier form, a
+// warp holding its 32 rays until the slowest ended, left lanes idle for most
+// of a walk's tail.  The 1080p renders: refilling at 8 idle lanes with one
+// atomic per refill 4.4 % faster (16 lanes 2.3 %, 12 4.3 %, 4 2.2 %, 2 and 1
+// slower), then claims of 64 entries another 4.8 % (the atomics on one counter
+// had become frequent); switching both off for launches with fewer than 256,
+// 1024 or 4096 rays per warp was 7-16 % slower, the small late-depth launches
+// being the long-tailed ones.
 constexpr uint32_t kRefillIdle = 8;
+constexpr uint32_t kClaim = 64;   // queue entries a warp claims at a time
 template <bool kCount, bool kImplicit, bool kRuntimeBounds, bool kWT, class Rays>
 __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, uint64_t n, unsigned long long* work,
                                            TraceCounters* cnt)
@@ -647,15 +653,29 @@ __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, uint
     bool live = false;
     unsigned busy = 0;   // warp-uniform: the lanes holding a walk (lanes whose walk ended on a bound may linger)
     bool more = true;    // warp-uniform: the queue may hold entries
+    uint64_t next = 0, end = 0;   // warp-uniform: the warp's claimed entries [next, end)
     for (;;) {
         if (more && __popc(busy) <= 32 - kRefillIdle) {
             const unsigned idle = ~busy;
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(work, (unsigned long long)__popc(idle));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base + __popc(idle) >= n) more = false;
-            const uint64_t k = base + __popc(idle & ((1u << lane) - 1u));
-            if (!live && ((idle >> lane) & 1u) && k < n) {
+            const uint32_t need = __popc(idle);
+            const uint32_t avail = (uint32_t)(end - next);
+            uint64_t fresh = 0;
+            if (need > avail) {
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(work, (unsigned long long)kClaim);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                fresh = base;
+                if (base >= n) more = false;
+            }
+            const uint32_t r = __popc(idle & ((1u << lane) - 1u));
+            const uint64_t k = r < avail ? next + r : fresh + (r - avail);
+            if (need > avail) {
+                next = fresh + (need - avail);
+                end = fresh + kClaim;
+            } else {
+                next += need;
+            }
+            if (!live && ((idle >> lane) & 1u) && k < n && (r < avail || more)) {
                 float4 o, d;
                 float tmax, exit_below;
                 bool occlusion;
