@@ -166,6 +166,7 @@ __device__ __forceinline__ void extend_finish(const SceneView& sc, PathBatch& b,
 // query of the physical estimator).
 struct ExtendRays {
     using Tag = uint32_t;
+    using Index = uint32_t;   // at most 2^26 segments and 2^26 shadow rays
     const SceneView& sc;
     PathBatch& b;
     const uint32_t* q;
@@ -173,7 +174,7 @@ struct ExtendRays {
     uint32_t n0;
     int* err;
 
-    __device__ __forceinline__ uint32_t load(uint64_t k, float4& o, float4& d, float& tmax, float& exit_below,
+    __device__ __forceinline__ uint32_t load(uint32_t k, float4& o, float4& d, float& tmax, float& exit_below,
                                              bool& occlusion) const
     {
         const bool shadow = k >= n0;
@@ -255,7 +256,7 @@ __global__ void __launch_bounds__(kThreads, extend_threads_per_sm<kOrder>() / kT
     if constexpr ((kOrder & kReferenceOrder) == 0) {
         ExtendRays rays{sc, b, q, sq, n0, err};
         walk_queue<kCount, (kOrder & kWithImplicit) != 0, (kOrder & kBounded) != 0, (kOrder & kWatertight) != 0>(
-            sc, rays, n, work, &cnt);
+            sc, rays, (uint32_t)n, work, &cnt);
     } else {
         // the reference order: each lane runs its ray to completion, 32 rays per warp fetch
         for (;;) {

@@ -38,6 +38,7 @@ __device__ __forceinline__ void write_hit(const SceneView& sc, const TraceHit& h
 // The rays of a batch for walk_queue: a lane's tag is the ray's index.
 struct BatchRays {
     using Tag = uint64_t;
+    using Index = uint64_t;
     const SceneView& sc;
     const float4* rays;
     pico_hit* hits;

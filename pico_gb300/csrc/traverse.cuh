@@ -629,7 +629,8 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // entries:
 //   rays.load(k, o, d, tmax, exit_below, occlusion) -> a lane tag for entry k,
 //   rays.finish(tag, best, status) hands in a finished walk;
-// `Rays::Tag` is the tag's type.  A lane whose walk ended waits (see
+// `Rays::Tag` is the tag's type, `Rays::Index` that of the entry indices.  A
+// lane whose walk ended waits (see
 // nf_release) to hand it in; once kRefillIdle lanes of the warp are idle they
 // take the next entries of the warp's claim together, and the warp claims
 // kClaim entries of the shared counter `work` at a time.  The earlier form, a
@@ -637,15 +638,19 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // of a walk's tail.  The 1080p renders: refilling at 8 idle lanes with one
 // atomic per refill 4.4 % faster (16 lanes 2.3 %, 12 4.3 %, 4 2.2 %, 2 and 1
 // slower), then claims of 64 entries another 4.8 % (the atomics on one counter
-// had become frequent); switching both off for launches with fewer than 256,
-// 1024 or 4096 rays per warp was 7-16 % slower, the small late-depth launches
-// being the long-tailed ones.
+// had become frequent), but 35 % slower Cornell-box renders, whose launches
+// hold a few dozen rays per warp: a warp then walked two or three claims'
+// worth of rays while others had none, so a launch with fewer than kClaim rays
+// per warp claims 32 at a time (the Cornell box back to 21 % slower than before
+// the refills, the 1080p renders unchanged).  A 32-bit Index for queues of
+// fewer than 2^32 entries keeps the extension kernel free of spills.
 constexpr uint32_t kRefillIdle = 8;
 constexpr uint32_t kClaim = 64;   // queue entries a warp claims at a time
 template <bool kCount, bool kImplicit, bool kRuntimeBounds, bool kWT, class Rays>
-__device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, uint64_t n, unsigned long long* work,
-                                           TraceCounters* cnt)
+__device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, typename Rays::Index n,
+                                           unsigned long long* work, TraceCounters* cnt)
 {
+    using Index = typename Rays::Index;
     const unsigned lane = threadIdx.x & 31u;
     NearFirstState w;
     uint32_t stack[kTraceStack];
@@ -653,25 +658,31 @@ __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, uint
     bool live = false;
     unsigned busy = 0;   // warp-uniform: the lanes holding a walk (lanes whose walk ended on a bound may linger)
     bool more = true;    // warp-uniform: the queue may hold entries
-    uint64_t next = 0, end = 0;   // warp-uniform: the warp's claimed entries [next, end)
+    Index next = 0, end = 0;   // warp-uniform: the warp's claimed entries [next, end)
+    // a launch with fewer than kClaim rays per warp claims 32 at a time, so that its rays spread over the warps
+    const uint32_t claim = (uint64_t)n >= (uint64_t)gridDim.x * (blockDim.x >> 5) * kClaim ? kClaim : 32u;
     for (;;) {
         if (more && __popc(busy) <= 32 - kRefillIdle) {
             const unsigned idle = ~busy;
             const uint32_t need = __popc(idle);
             const uint32_t avail = (uint32_t)(end - next);
-            uint64_t fresh = 0;
+            Index fresh = 0;
             if (need > avail) {
                 unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(work, (unsigned long long)kClaim);
+                if (lane == 0) base = atomicAdd(work, (unsigned long long)claim);
                 base = __shfl_sync(0xffffffffu, base, 0);
-                fresh = base;
-                if (base >= n) more = false;
+                if (base >= (unsigned long long)n) {
+                    more = false;
+                    fresh = n;
+                } else {
+                    fresh = (Index)base;
+                }
             }
             const uint32_t r = __popc(idle & ((1u << lane) - 1u));
-            const uint64_t k = r < avail ? next + r : fresh + (r - avail);
+            const Index k = r < avail ? next + r : fresh + (r - avail);
             if (need > avail) {
                 next = fresh + (need - avail);
-                end = fresh + kClaim;
+                end = fresh + claim;
             } else {
                 next += need;
             }
