@@ -646,6 +646,9 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // fewer than 2^32 entries keeps the extension kernel free of spills.
 constexpr uint32_t kRefillIdle = 8;
 constexpr uint32_t kClaim = 64;   // queue entries a warp claims at a time
+// A claim must cover a refill of all 32 lanes, or the claimed range [next, end)
+// could run backwards and the warp would never claim again.
+static_assert(kClaim >= 32, "a claim covers a whole warp's refill");
 template <bool kCount, bool kImplicit, bool kRuntimeBounds, bool kWT, class Rays>
 __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, typename Rays::Index n,
                                            unsigned long long* work, TraceCounters* cnt)
