@@ -642,13 +642,18 @@ __device__ __forceinline__ int trace_near_first(const SceneView& sc, const float
 // hold a few dozen rays per warp: a warp then walked two or three claims'
 // worth of rays while others had none, so a launch with fewer than kClaim rays
 // per warp claims 32 at a time (the Cornell box back to 21 % slower than before
-// the refills, the 1080p renders unchanged).  A 32-bit Index for queues of
-// fewer than 2^32 entries keeps the extension kernel free of spills.
+// the refills, the 1080p renders unchanged), and the bar at 1024 rays per warp
+// instead of 64 brought the Cornell box to 17 % slower (the 1080p renders 0.1 %
+// faster); refilling only fully idle warps below the bar would bring it to 8 %
+// slower but cost the 1080p renders 1.5 %, whose small late-depth launches are
+// long-tailed.  A 32-bit Index for queues of fewer than 2^32 entries keeps the
+// extension kernel free of spills.
 constexpr uint32_t kRefillIdle = 8;
 constexpr uint32_t kClaim = 64;   // queue entries a warp claims at a time
 // A claim must cover a refill of all 32 lanes, or the claimed range [next, end)
 // could run backwards and the warp would never claim again.
 static_assert(kClaim >= 32, "a claim covers a whole warp's refill");
+constexpr uint32_t kBigLaunch = 1024;   // rays per warp from which a launch claims kClaim at a time
 template <bool kCount, bool kImplicit, bool kRuntimeBounds, bool kWT, class Rays>
 __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, typename Rays::Index n,
                                            unsigned long long* work, TraceCounters* cnt)
@@ -662,8 +667,9 @@ __device__ __forceinline__ void walk_queue(const SceneView& sc, Rays& rays, type
     unsigned busy = 0;   // warp-uniform: the lanes holding a walk (lanes whose walk ended on a bound may linger)
     bool more = true;    // warp-uniform: the queue may hold entries
     Index next = 0, end = 0;   // warp-uniform: the warp's claimed entries [next, end)
-    // a launch with fewer than kClaim rays per warp claims 32 at a time, so that its rays spread over the warps
-    const uint32_t claim = (uint64_t)n >= (uint64_t)gridDim.x * (blockDim.x >> 5) * kClaim ? kClaim : 32u;
+    // a launch with fewer than kBigLaunch rays per warp claims 32 at a time, so that its rays spread over the warps
+    const bool big = (uint64_t)n >= (uint64_t)gridDim.x * (blockDim.x >> 5) * kBigLaunch;
+    const uint32_t claim = big ? kClaim : 32u;
     for (;;) {
         if (more && __popc(busy) <= 32 - kRefillIdle) {
             const unsigned idle = ~busy;
