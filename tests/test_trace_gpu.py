@@ -238,3 +238,26 @@ def test_implicit_cubes_in_near_first_order(ctx, oracle):
     rays = random_rays(np.random.default_rng(5), 20000, 0.02, 0.98)
     got, want = check(ctx, oracle, s, rays, "cubes")
     assert (want["prim"] == 0xFFFFFFFE).sum() > 1000
+
+
+@pytest.mark.parametrize("n", [1, 7, 31, 32, 33, 63, 64, 65, 100, 1000, 4097, 50021])
+def test_ragged_batches(ctx, oracle, n):
+    """Warps claim rays in chunks of 64 (32 when a launch holds fewer than 1024 rays
+    per warp) and refill idle lanes from them: every batch size, around the chunk and
+    warp sizes and far below one ray per warp of the grid, gives the oracle's hits,
+    device-resident and from host memory, with each ray's hit in its own slot."""
+    torch = pytest.importorskip("torch")
+    scene = scenes.instance_field(n_instances=128, level=2, seed=41, extent=15.0)
+    rng = np.random.default_rng(n)
+    rays = np.concatenate([scenes.surface_rays(scene, n // 2 + 1, seed=n),
+                           random_rays(rng, n, -20.0, 20.0)])[:n]
+    want = oracle.scene(scene).trace(rays)
+    gs = ctx.upload(scene)
+    assert_same_hits(gs.trace_closest(rays), want, f"host, {n} rays")
+    d_rays = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_hits = torch.full((n * HIT_DTYPE.itemsize,), 0xAB, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    gs.trace_closest_device(d_rays.data_ptr(), n, d_hits.data_ptr(), stream)
+    gs.check(stream)
+    assert_same_hits(d_hits.cpu().numpy().view(HIT_DTYPE), want, f"device, {n} rays")
+    gs.free()
