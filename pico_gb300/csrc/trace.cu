@@ -68,26 +68,25 @@ __global__ void __launch_bounds__(kTraceThreads, kTraceMinBlocks)
                  DeviceStatus* status)
 {
     TraceCounters cnt{0, 0, 0, 0};
-    const unsigned lane = threadIdx.x & 31u;
     if constexpr ((kOrder & kReferenceOrder) == 0) {
         BatchRays src{sc, rays, hits, status};
         walk_queue<kCount, (kOrder & kWithImplicit) != 0, (kOrder & kBounded) != 0, (kOrder & kWatertight) != 0>(
             sc, src, n, &status->work, &cnt);
-        if (kCount) flush_counters(cnt, status->counters);
-        return;
-    }
-    for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(&status->work, 32ull);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        const unsigned long long i = base + lane;
-        if (i < n) {
-            const float4 o = __ldg(rays + 2 * i), d = __ldg(rays + 2 * i + 1);
-            TraceHit h;
-            const int s = trace_closest<kCount, kOrder>(sc, o, d, h, &cnt);
-            if (s != kTraceOk) atomicOr(&status->trace_error, s);
-            write_hit(sc, h, s, hits + i);
+    } else {
+        const unsigned lane = threadIdx.x & 31u;
+        for (;;) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(&status->work, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= n) break;
+            const unsigned long long i = base + lane;
+            if (i < n) {
+                const float4 o = __ldg(rays + 2 * i), d = __ldg(rays + 2 * i + 1);
+                TraceHit h;
+                const int s = trace_closest<kCount, kOrder>(sc, o, d, h, &cnt);
+                if (s != kTraceOk) atomicOr(&status->trace_error, s);
+                write_hit(sc, h, s, hits + i);
+            }
         }
     }
     if (kCount) flush_counters(cnt, status->counters);
