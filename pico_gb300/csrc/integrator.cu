@@ -280,15 +280,10 @@ __global__ void __launch_bounds__(kThreads, extend_threads_per_sm<kOrder>() / kT
                         b.pay[i] = p;
                     }
                 } else {
-                    // A shadow ray only asks whether its closest hit is a light (or, for a
-                    // sun ray, nothing), so its walk may stop at a hit nearer than every
-                    // light: the closest hit is then no light either.  A sun ray stops at
-                    // its first hit.
-                    const float4 o = shadow ? b.sorg[i] : b.org[i];
-                    float exit_below = -INFINITY;
-                    if (shadow) exit_below = b.senergy[i].w != 0.0f ? INFINITY : light_distance_bound(sc, o);
+                    // the reference order walks every shadow ray to its closest hit
                     TraceHit h;
-                    const int s = trace_closest<kCount, kOrder>(sc, o, shadow ? b.sdir[i] : b.dir[i], h, &cnt, exit_below);
+                    const int s = trace_closest<kCount, kOrder>(sc, shadow ? b.sorg[i] : b.org[i],
+                                                                shadow ? b.sdir[i] : b.dir[i], h, &cnt);
                     if (s != kTraceOk) atomicOr(err, s);
                     extend_finish(sc, b, i, h, s, shadow);
                 }
